@@ -1,0 +1,181 @@
+/*
+ * shci_gpu.h - C ABI of the GB300 SHCI hot path (libshci_gpu.so).
+ *
+ * Replaces, for one process on one GPU, the reference's in-process C++ interfaces on the
+ * SHCI hot path (QMC-Cornell/shci):
+ *   - the system plugin API, class BaseSystem (src/base_system.h:43-136), as implemented by
+ *     ChemSystem (src/chem/chem_system.{h,cc});
+ *   - the solver-level operators Hamiltonian<S>::update (src/solver/hamiltonian.h:87-112),
+ *     SparseMatrix::mul (src/solver/sparse_matrix.cc:28-56), Davidson::diagonalize
+ *     (src/solver/davidson.cc:8-196) and the selection / PT2 / RDM stages of
+ *     Solver<S> (src/solver/solver.h) and RDM (src/chem/rdm.cc).
+ *
+ * Conventions.  Plain pointers and sizes only.  Pointers are HOST pointers unless the name
+ * ends in _dev (device pointers on the context's device).  The caller owns host buffers;
+ * the context owns all device memory it allocates.  Every call returns a status and never
+ * throws across the ABI; shci_last_error() gives the message of the last failure.  Calls on
+ * one context are not thread safe; separate contexts are independent.  Determinants are two
+ * 64-bit spin strings (bit k = spatial orbital k occupied), so n_orbs <= 64.
+ */
+#ifndef SHCI_GPU_H
+#define SHCI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct shci_ctx shci_ctx;
+
+typedef enum {
+  SHCI_OK = 0,
+  SHCI_ERR_OOM = 1,      /* device allocation failed or budget exceeded */
+  SHCI_ERR_ARG = 2,      /* invalid argument / state (message says which) */
+  SHCI_ERR_CUDA = 3,     /* CUDA runtime error */
+  SHCI_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+  SHCI_ERR_OVERFLOW = 5, /* a device buffer bound was exceeded (host splits and retries) */
+  SHCI_ERR_CHECK = 6,    /* a device-side consistency check failed */
+  SHCI_ERR_IO = 7        /* file could not be read / parsed */
+} shci_status;
+
+/* Matrix-element storage precision for shci_update_hamiltonian. */
+typedef enum {
+  SHCI_PREC_FP64 = 0,  /* off-diagonal elements stored as FP64 */
+  SHCI_PREC_MIXED = 1  /* off-diagonal elements stored as FP32 (+ FP32 residual for the
+                          final FP64 correction); accumulation always FP64 */
+} shci_precision;
+
+/* ---- lifecycle --------------------------------------------------------------------- */
+
+/* Create a context on `device`.  hbm_budget_bytes = 0: no explicit budget. */
+shci_status shci_create(shci_ctx** out, int device, size_t hbm_budget_bytes);
+shci_status shci_destroy(shci_ctx* ctx);
+const char* shci_last_error(const shci_ctx* ctx);
+/* The CUDA stream all work of this context is issued on (a cudaStream_t). */
+void* shci_stream(shci_ctx* ctx);
+
+/* ---- integrals (ChemSystem::setup / Integrals::load) --------------------------------- */
+
+/* Read FCIDUMP at `path` and prepare integrals exactly as Integrals::load does
+ * (src/chem/integrals.cc:17-35, 37-114, 155-384): |v| < 1e-9 dropped, duplicates keep the
+ * larger |v|, HF det filled lowest (or from occs_up/occs_dn when both non-NULL), orbitals
+ * reordered by HF orbital energy when reorder = -1 (default: unless occs given) or 1.
+ * point_group: "C1", "C2", "Cs", "Ci", "C2v", "C2h", "D2", "D2h" (case-insensitive). */
+shci_status shci_load_fcidump(shci_ctx* ctx, const char* path, unsigned n_up, unsigned n_dn,
+                              const char* point_group, int reorder, const unsigned* occs_up,
+                              const unsigned* occs_dn);
+
+/* Set already-prepared integrals: h1[n*n] (h_pq), g2[n^4] (chemists' (pq|rs) at
+ * ((p*n+q)*n+r)*n+s), orb_sym[n] (irreps 1..8, NULL = all 1).  The HF det is given. */
+shci_status shci_set_integrals(shci_ctx* ctx, int n_orbs, unsigned n_up, unsigned n_dn,
+                               double e_core, const double* h1, const double* g2,
+                               const unsigned* orb_sym, const char* point_group,
+                               uint64_t hf_up, uint64_t hf_dn);
+
+/* Reordered dense integrals as used on the device (any pointer may be NULL). */
+shci_status shci_get_integrals(shci_ctx* ctx, int* n_orbs, double* e_core, double* h1,
+                               double* g2, unsigned* orb_sym, unsigned* orb_order);
+
+/* HF det and its energy (ChemSystem::setup, chem_system.cc:50-60). */
+shci_status shci_get_hf(shci_ctx* ctx, uint64_t* up, uint64_t* dn, double* energy_hf);
+
+/* Heat-bath queues (ChemSystem::setup_hci_queue / setup_singles_queue,
+ * chem_system.cc:74-196); built on the host, uploaded to HBM.  info[4] =
+ * {max hci elem, n hci entries, max singles elem, n singles entries}. */
+shci_status shci_build_queues(shci_ctx* ctx, double* info);
+
+/* ---- determinants and coefficients (BaseSystem::dets / coefs) ------------------------ */
+
+shci_status shci_set_dets(shci_ctx* ctx, const uint64_t* up, const uint64_t* dn,
+                          const double* coefs, size_t n);
+shci_status shci_get_n_dets(shci_ctx* ctx, size_t* n);
+shci_status shci_get_dets(shci_ctx* ctx, uint64_t* up, uint64_t* dn, double* coefs, size_t cap);
+shci_status shci_set_coefs(shci_ctx* ctx, const double* coefs, size_t n);
+
+/* ---- matrix elements (BaseSystem::get_hamiltonian_elem, base_system.h:94-95) --------- */
+
+/* out[k] = H(det_i[k], det_j[k]) for k < n (n_excite = -1 semantics: degree computed,
+ * 0 for degree > 2; equal dets give the diagonal). */
+shci_status shci_hamiltonian_elems(shci_ctx* ctx, const uint64_t* up_i, const uint64_t* dn_i,
+                                   const uint64_t* up_j, const uint64_t* dn_j, size_t n,
+                                   double* out);
+
+/* ---- Hamiltonian build (Hamiltonian<S>::update, hamiltonian.h:87-112, 415-598) -------- */
+
+/* Build the upper-triangle sparse Hamiltonian of the current dets on the device.
+ * nnz_out[0] = stored strict-upper elements, nnz_out[1] = the reference's symmetric count
+ * (2 * (strict + n) - n, sparse_matrix.cc:13-26).  Elements with |H| < 1e-12 are dropped. */
+shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_out);
+
+/* Copy the Hamiltonian to the host: row_ptr[n+1] (strict upper), cols[nnz], vals[nnz]
+ * (as FP64), diag[n].  Rows list their columns in the device traversal order. */
+shci_status shci_get_hamiltonian(shci_ctx* ctx, uint64_t* row_ptr, uint32_t* cols,
+                                 double* vals, double* diag);
+
+/* ---- H*v and Davidson (SparseMatrix::mul, Davidson::diagonalize) --------------------- */
+
+/* y_dev = H x_dev on the context stream (n = number of dets, FP64 vectors).
+ * use_residual = 1 adds the FP32 residual of mixed storage (FP64-accurate product). */
+shci_status shci_hv(shci_ctx* ctx, const double* x_dev, double* y_dev, int use_residual);
+
+/* Host-buffer variant of shci_hv (copies in and out). */
+shci_status shci_hv_host(shci_ctx* ctx, const double* x, double* y, int use_residual);
+
+/* One Davidson::diagonalize call (n_states = 1) on the current Hamiltonian, starting from the
+ * context's coefficients; on return they hold the Ritz vector.  eval = lowest eigenvalue,
+ * converged as in davidson.cc:174-185.  trace (may be NULL) receives the eigenvalue estimate
+ * after each step (up to trace_cap); n_trace its count. */
+shci_status shci_davidson(shci_ctx* ctx, double tol, double* eval, int* converged,
+                          double* trace, size_t trace_cap, size_t* n_trace);
+
+/* Rayleigh quotient <c|H|c>/<c|c> of the context's coefficients with the FP64-accurate
+ * product (mixed storage: FP32 value + FP32 residual) - the final FP64 correction. */
+shci_status shci_energy_fp64(shci_ctx* ctx, double* energy);
+
+/* Davidson on a caller-supplied upper-triangle CSR (strict upper + diag), e.g. the Hilbert
+ * matrix of src/solver/davidson_test.cc.  init/evec are host vectors of length n. */
+shci_status shci_davidson_csr(shci_ctx* ctx, size_t n, const uint64_t* row_ptr,
+                              const uint32_t* cols, const double* vals, const double* diag,
+                              const double* init, double tol, double* eval, double* evec,
+                              int* converged);
+
+/* ---- heat-bath selection (Solver<S>::run_variation, solver.h:435-495) ---------------- */
+
+/* One selection step with the context's coefficients: five passes over var dets i = j mod 5,
+ * each pass's new dets appended in ascending Det order with coefficient 1e-16.  Keeps the
+ * eps_tried_prev memo (solver.h:445-448, 465-468) across calls.  n_new = dets added. */
+shci_status shci_select(shci_ctx* ctx, double eps_var, int var_sd, size_t* n_new);
+
+/* eps_tried_prev memo (length = n dets at the last selection). */
+shci_status shci_get_eps_tried(shci_ctx* ctx, double* out, size_t cap);
+
+/* Whole variational stage (solver.h:338-397, 413-539): eps_vars[n_eps] with the
+ * eps_vars_schedule; energies[n_eps] out.  precision as for shci_update_hamiltonian. */
+shci_status shci_run_variation(shci_ctx* ctx, const double* eps_vars, size_t n_eps,
+                               const double* schedule, size_t n_sched, double target_error,
+                               int precision, double* energies);
+
+/* Per-iteration record of the last shci_run_variation (the reference's "Iteration N ...
+ * ndets= ... energy=" log lines and "Number of nonzero elems"): n_dets, symmetric nnz and
+ * energy of each iteration; *n = number of iterations (entries beyond cap not written). */
+shci_status shci_get_var_trace(shci_ctx* ctx, uint64_t* n_dets, uint64_t* nnz, double* energy,
+                               size_t cap, size_t* n);
+
+/* Number of kernel launches issued by this context so far (for launch accounting). */
+shci_status shci_get_launch_count(shci_ctx* ctx, uint64_t* n);
+
+/* ---- PT2 (Solver<S>::get_energy_pt_dtm, solver.h:636-764) ---------------------------- */
+
+/* Deterministic Epstein-Nesbet PT2 over n_batches hash batches (rehash(DetHasher(a)) %
+ * n_batches).  energy_var = E_var of the context's wavefunction.  out: correction, its
+ * uncertainty (0 when all batches ran), number of unique PT dets. */
+shci_status shci_pt2_dtm(shci_ctx* ctx, double energy_var, double eps_pt_dtm, size_t n_batches,
+                         double* correction, double* uncert, size_t* n_pt_dets);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHCI_GPU_H */

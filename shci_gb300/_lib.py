@@ -1,0 +1,295 @@
+"""ctypes binding to libshci_gpu.so (the C ABI declared in include/shci_gpu.h).
+
+There is no CPU fallback: if the library is missing, or no GPU is present, the calls fail
+with an exception naming the cause.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libshci_gpu.so")
+HEADER = os.path.join(HERE, "..", "include", "shci_gpu.h")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+STATUS = {0: "SHCI_OK", 1: "SHCI_ERR_OOM", 2: "SHCI_ERR_ARG", 3: "SHCI_ERR_CUDA",
+          4: "SHCI_ERR_TIMEOUT", 5: "SHCI_ERR_OVERFLOW", 6: "SHCI_ERR_CHECK", 7: "SHCI_ERR_IO"}
+
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+_lib = None
+
+
+class ShciError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+def load():
+    """Loads the library (building it first if needed); raises if that is impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, d, i, u = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_int, ctypes.c_uint
+    u64 = ctypes.c_uint64
+    P = ctypes.POINTER
+    sig = {
+        "shci_create": [P(vp), i, sz],
+        "shci_destroy": [vp],
+        "shci_load_fcidump": [vp, ctypes.c_char_p, u, u, ctypes.c_char_p, i, vp, vp],
+        "shci_set_integrals": [vp, i, u, u, d, _f64p, _f64p, vp, ctypes.c_char_p, u64, u64],
+        "shci_get_integrals": [vp, P(i), P(d), vp, vp, vp, vp],
+        "shci_get_hf": [vp, P(u64), P(u64), P(d)],
+        "shci_build_queues": [vp, _f64p],
+        "shci_set_dets": [vp, _u64p, _u64p, vp, sz],
+        "shci_get_n_dets": [vp, P(sz)],
+        "shci_get_dets": [vp, _u64p, _u64p, vp, sz],
+        "shci_set_coefs": [vp, _f64p, sz],
+        "shci_hamiltonian_elems": [vp, _u64p, _u64p, _u64p, _u64p, sz, _f64p],
+        "shci_update_hamiltonian": [vp, i, P(sz)],
+        "shci_get_hamiltonian": [vp, _u64p, _u32p, _f64p, _f64p],
+        "shci_hv": [vp, vp, vp, i],
+        "shci_hv_host": [vp, _f64p, _f64p, i],
+        "shci_davidson": [vp, d, P(d), P(i), _f64p, sz, P(sz)],
+        "shci_energy_fp64": [vp, P(d)],
+        "shci_davidson_csr": [vp, sz, _u64p, _u32p, _f64p, _f64p, _f64p, d, P(d), _f64p, P(i)],
+        "shci_select": [vp, d, i, P(sz)],
+        "shci_get_eps_tried": [vp, _f64p, sz],
+        "shci_run_variation": [vp, _f64p, sz, vp, sz, d, i, _f64p],
+        "shci_get_var_trace": [vp, _u64p, _u64p, _f64p, sz, P(sz)],
+        "shci_get_launch_count": [vp, P(u64)],
+        "shci_pt2_dtm": [vp, d, d, sz, P(d), P(d), P(sz)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = args
+    L.shci_last_error.restype = ctypes.c_char_p
+    L.shci_last_error.argtypes = [vp]
+    L.shci_stream.restype = vp
+    L.shci_stream.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def header_symbols():
+    """Names of the functions declared in include/shci_gpu.h."""
+    import re
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(shci_[a-z0-9_]+)\s*\(", txt)))
+
+
+class Context:
+    """One SHCI instance on one GPU (owns all device memory of the instance)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        st = self.L.shci_create(ctypes.byref(h), device, hbm_budget)
+        if st != 0:
+            raise ShciError(st, "shci_create failed (is a CUDA GPU visible?)")
+        self.h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.shci_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, st):
+        if st != 0:
+            raise ShciError(st, self.L.shci_last_error(self.h).decode())
+
+    # ---- integrals -------------------------------------------------------------------
+    def load_fcidump(self, path, n_up, n_dn, point_group="C1", reorder=-1, occs_up=None,
+                     occs_dn=None):
+        ou = od = None
+        if occs_up is not None:
+            a = np.ascontiguousarray(occs_up, np.uint32)
+            b = np.ascontiguousarray(occs_dn, np.uint32)
+            self._keep += [a, b]
+            ou, od = a.ctypes.data, b.ctypes.data
+        self._ck(self.L.shci_load_fcidump(self.h, str(path).encode(), n_up, n_dn,
+                                          point_group.encode(), reorder, ou, od))
+        self.n_up, self.n_dn = n_up, n_dn
+        n = ctypes.c_int()
+        self._ck(self.L.shci_get_integrals(self.h, ctypes.byref(n), None, None, None, None, None))
+        self.n_orbs = n.value
+
+    def set_integrals(self, h1, g2, n_up, n_dn, hf_up, hf_dn, e_core=0.0, orb_sym=None,
+                      point_group="C1"):
+        n = h1.shape[0]
+        sym = None
+        if orb_sym is not None:
+            s = np.ascontiguousarray(orb_sym, np.uint32)
+            self._keep.append(s)
+            sym = s.ctypes.data
+        self._ck(self.L.shci_set_integrals(self.h, n, n_up, n_dn, e_core,
+                                           np.ascontiguousarray(h1, np.float64).ravel(),
+                                           np.ascontiguousarray(g2, np.float64).ravel(), sym,
+                                           point_group.encode(), hf_up, hf_dn))
+        self.n_up, self.n_dn, self.n_orbs = n_up, n_dn, n
+
+    def integrals(self):
+        n = self.n_orbs
+        h1 = np.zeros((n, n))
+        g2 = np.zeros((n, n, n, n))
+        sym = np.zeros(n, np.uint32)
+        order = np.zeros(n, np.uint32)
+        ec = ctypes.c_double()
+        self._ck(self.L.shci_get_integrals(self.h, None, ctypes.byref(ec), h1.ctypes.data,
+                                           g2.ctypes.data, sym.ctypes.data, order.ctypes.data))
+        return h1, g2, sym, order, ec.value
+
+    def hf(self):
+        u, d, e = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        self._ck(self.L.shci_get_hf(self.h, ctypes.byref(u), ctypes.byref(d), ctypes.byref(e)))
+        return u.value, d.value, e.value
+
+    def build_queues(self):
+        info = np.zeros(4)
+        self._ck(self.L.shci_build_queues(self.h, info))
+        return dict(max_hci=info[0], n_hci=int(info[1]), max_singles=info[2],
+                    n_singles=int(info[3]))
+
+    # ---- dets ------------------------------------------------------------------------
+    def set_dets(self, up, dn, coefs=None):
+        up = np.ascontiguousarray(up, np.uint64)
+        dn = np.ascontiguousarray(dn, np.uint64)
+        c = None
+        if coefs is not None:
+            cc = np.ascontiguousarray(coefs, np.float64)
+            self._keep.append(cc)
+            c = cc.ctypes.data
+        self._ck(self.L.shci_set_dets(self.h, up, dn, c, len(up)))
+
+    def n_dets(self):
+        n = ctypes.c_size_t()
+        self._ck(self.L.shci_get_n_dets(self.h, ctypes.byref(n)))
+        return n.value
+
+    def dets(self):
+        n = self.n_dets()
+        up = np.zeros(n, np.uint64)
+        dn = np.zeros(n, np.uint64)
+        c = np.zeros(n)
+        self._ck(self.L.shci_get_dets(self.h, up, dn, c.ctypes.data, n))
+        return up, dn, c
+
+    def set_coefs(self, c):
+        c = np.ascontiguousarray(c, np.float64)
+        self._ck(self.L.shci_set_coefs(self.h, c, len(c)))
+
+    def h_elems(self, ui, di, uj, dj):
+        ui, di, uj, dj = (np.ascontiguousarray(x, np.uint64) for x in (ui, di, uj, dj))
+        out = np.zeros(len(ui))
+        self._ck(self.L.shci_hamiltonian_elems(self.h, ui, di, uj, dj, len(ui), out))
+        return out
+
+    # ---- Hamiltonian / Davidson --------------------------------------------------------
+    def update_hamiltonian(self, precision=PREC_FP64):
+        nnz = (ctypes.c_size_t * 2)()
+        self._ck(self.L.shci_update_hamiltonian(self.h, precision, nnz))
+        return nnz[0], nnz[1]
+
+    def hamiltonian(self, nnz):
+        n = self.n_dets()
+        rp = np.zeros(n + 1, np.uint64)
+        cols = np.zeros(max(nnz, 1), np.uint32)
+        vals = np.zeros(max(nnz, 1))
+        diag = np.zeros(n)
+        self._ck(self.L.shci_get_hamiltonian(self.h, rp, cols, vals, diag))
+        return rp, cols[:nnz], vals[:nnz], diag
+
+    def hv(self, x, residual=False):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self._ck(self.L.shci_hv_host(self.h, x, y, int(residual)))
+        return y
+
+    def hv_dev(self, x_ptr, y_ptr, residual=False):
+        self._ck(self.L.shci_hv(self.h, x_ptr, y_ptr, int(residual)))
+
+    def davidson(self, tol):
+        e = ctypes.c_double()
+        conv = ctypes.c_int()
+        tr = np.zeros(64)
+        nt = ctypes.c_size_t()
+        self._ck(self.L.shci_davidson(self.h, tol, ctypes.byref(e), ctypes.byref(conv), tr, 64,
+                                      ctypes.byref(nt)))
+        return e.value, bool(conv.value), tr[: nt.value]
+
+    def energy_fp64(self):
+        e = ctypes.c_double()
+        self._ck(self.L.shci_energy_fp64(self.h, ctypes.byref(e)))
+        return e.value
+
+    def davidson_csr(self, row_ptr, cols, vals, diag, init, tol):
+        n = len(diag)
+        e = ctypes.c_double()
+        conv = ctypes.c_int()
+        vec = np.zeros(n)
+        self._ck(self.L.shci_davidson_csr(self.h, n, np.ascontiguousarray(row_ptr, np.uint64),
+                                          np.ascontiguousarray(cols, np.uint32),
+                                          np.ascontiguousarray(vals, np.float64),
+                                          np.ascontiguousarray(diag, np.float64),
+                                          np.ascontiguousarray(init, np.float64), tol,
+                                          ctypes.byref(e), vec, ctypes.byref(conv)))
+        return e.value, vec, bool(conv.value)
+
+    # ---- selection / variation / PT2 ------------------------------------------------------
+    def select(self, eps_var, var_sd=False):
+        n = ctypes.c_size_t()
+        self._ck(self.L.shci_select(self.h, eps_var, int(var_sd), ctypes.byref(n)))
+        return n.value
+
+    def eps_tried(self):
+        n = self.n_dets()
+        out = np.zeros(n)
+        self._ck(self.L.shci_get_eps_tried(self.h, out, n))
+        return out
+
+    def run_variation(self, eps_vars, schedule=(), target_error=5e-5, precision=PREC_FP64):
+        ev = np.ascontiguousarray(eps_vars, np.float64)
+        sc = np.ascontiguousarray(schedule, np.float64)
+        out = np.zeros(len(ev))
+        self._ck(self.L.shci_run_variation(self.h, ev, len(ev), sc.ctypes.data if len(sc) else None,
+                                           len(sc), target_error, precision, out))
+        return out
+
+    def var_trace(self):
+        n = ctypes.c_size_t()
+        self._ck(self.L.shci_get_var_trace(self.h, np.zeros(1, np.uint64), np.zeros(1, np.uint64),
+                                           np.zeros(1), 0, ctypes.byref(n)))
+        nd = np.zeros(n.value, np.uint64)
+        nz = np.zeros(n.value, np.uint64)
+        e = np.zeros(n.value)
+        self._ck(self.L.shci_get_var_trace(self.h, nd, nz, e, n.value, ctypes.byref(n)))
+        return nd, nz, e
+
+    def launches(self):
+        n = ctypes.c_uint64()
+        self._ck(self.L.shci_get_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def pt2_dtm(self, energy_var, eps_pt_dtm, n_batches=1):
+        v, u, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
+        self._ck(self.L.shci_pt2_dtm(self.h, energy_var, eps_pt_dtm, n_batches, ctypes.byref(v),
+                                     ctypes.byref(u), ctypes.byref(n)))
+        return v.value, u.value, n.value
+
+    def stream(self):
+        return self.L.shci_stream(self.h)

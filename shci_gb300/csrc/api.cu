@@ -1,0 +1,471 @@
+// C ABI of libshci_gpu.so (declared in include/shci_gpu.h).  Every entry point catches
+// exceptions and CUDA errors and turns them into a status plus shci_last_error().
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "ctx.h"
+#include "kernels.h"
+#include "solver.h"
+
+using namespace shci;
+
+namespace {
+
+template <class F>
+shci_status guard(shci_ctx* c, F f) {
+  try {
+    if (c) {
+      c->err.clear();
+      SHCI_CUDA(cudaSetDevice(c->device));
+    }
+    f();
+    return SHCI_OK;
+  } catch (const OomError& e) {
+    if (c) c->err = e.what();
+    return SHCI_ERR_OOM;
+  } catch (const ArgError& e) {
+    if (c) c->err = e.what();
+    return SHCI_ERR_ARG;
+  } catch (const OverflowError& e) {
+    if (c) c->err = e.what();
+    return SHCI_ERR_OVERFLOW;
+  } catch (const CudaError& e) {
+    if (c) c->err = e.what();
+    return e.code == cudaErrorMemoryAllocation ? SHCI_ERR_OOM : SHCI_ERR_CUDA;
+  } catch (const std::bad_alloc&) {
+    if (c) c->err = "host allocation failed";
+    return SHCI_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (c) c->err = e.what();
+    return SHCI_ERR_IO;
+  }
+}
+
+void need_integrals(shci_ctx* c) {
+  if (!c->have_integrals) throw ArgError("no integrals loaded");
+}
+
+void need_dets(shci_ctx* c) {
+  if (c->up.empty()) throw ArgError("no determinants set");
+}
+
+void after_integrals(shci_ctx* c) {
+  upload_integrals(c);
+  c->have_integrals = true;
+  c->Q.built = false;
+  c->up.assign(1, c->I.hf_up);
+  c->dn.assign(1, c->I.hf_dn);
+  c->coefs.assign(1, 1.0);
+  c->dets_dirty = true;
+  c->eps_tried.clear();
+  c->H.valid = false;
+}
+
+}  // namespace
+
+extern "C" {
+
+shci_status shci_create(shci_ctx** out, int device, size_t hbm_budget_bytes) {
+  if (!out) return SHCI_ERR_ARG;
+  *out = nullptr;
+  shci_ctx* c = new (std::nothrow) shci_ctx();
+  if (!c) return SHCI_ERR_OOM;
+  c->device = device;
+  c->mem.budget = hbm_budget_bytes;
+  shci_status st = guard(c, [&]() {
+    int n = 0;
+    SHCI_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) throw ArgError("no such CUDA device");
+    SHCI_CUDA(cudaSetDevice(device));
+    SHCI_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // every device buffer of the context is accounted against the budget
+    for (auto* b : {&c->h1, &c->g2, &c->dtab, &c->xtab, &c->jtab, &c->ktab, &c->d_coef, &c->f0,
+                    &c->f1})
+      b->mt = &c->mem;
+    for (auto* b : {&c->d_up, &c->d_dn, &c->set_up, &c->set_dn, &c->k0, &c->k1, &c->k2})
+      b->mt = &c->mem;
+    for (auto* b : {&c->u0, &c->u1, &c->u2}) b->mt = &c->mem;
+    c->err_word.mt = &c->mem;
+    c->sort.set_tracker(&c->mem);
+    auto& ix = c->idx;
+    for (auto* b : {&ix.det_aid, &ix.det_bid, &ix.a_start, &ix.b_start, &ix.am_idx, &ix.bm_idx,
+                    &ix.as_off, &ix.as_list})
+      b->mt = &c->mem;
+    for (auto* b : {&ix.am_dn, &ix.bm_up, &ix.ua}) b->mt = &c->mem;
+    auto& H = c->H;
+    H.row_ptr.mt = H.col.mt = H.row_cnt.mt = &c->mem;
+    H.val64.mt = H.diag.mt = &c->mem;
+    H.val32.mt = H.res32.mt = &c->mem;
+    c->dav.scal.mt = c->dav.partial.mt = &c->mem;
+  });
+  if (st != SHCI_OK) {
+    delete c;
+    return st;
+  }
+  *out = c;
+  return SHCI_OK;
+}
+
+shci_status shci_destroy(shci_ctx* c) {
+  if (!c) return SHCI_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaStream_t s = c->stream;
+  delete c;  // buffers free themselves
+  if (s) cudaStreamDestroy(s);
+  return SHCI_OK;
+}
+
+const char* shci_last_error(const shci_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+void* shci_stream(shci_ctx* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
+
+shci_status shci_load_fcidump(shci_ctx* c, const char* path, unsigned n_up, unsigned n_dn,
+                              const char* point_group, int reorder, const unsigned* occs_up,
+                              const unsigned* occs_dn) {
+  if (!c) return SHCI_ERR_ARG;
+  shci_status st = guard(c, [&]() {
+    if (!path) throw ArgError("null path");
+    HostIntegrals I;
+    try {
+      load_fcidump(I, path, n_up, n_dn, point_group ? point_group : "C1", reorder, occs_up,
+                   occs_dn);
+    } catch (const std::runtime_error& e) {
+      throw;  // mapped to SHCI_ERR_IO below
+    }
+    c->I = std::move(I);
+    after_integrals(c);
+  });
+  return st;
+}
+
+shci_status shci_set_integrals(shci_ctx* c, int n_orbs, unsigned n_up, unsigned n_dn,
+                               double e_core, const double* h1, const double* g2,
+                               const unsigned* orb_sym, const char* point_group, uint64_t hf_up,
+                               uint64_t hf_dn) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (n_orbs <= 0 || n_orbs > 64) throw ArgError("n_orbs must be in [1, 64]");
+    if (!h1 || !g2) throw ArgError("null integral array");
+    HostIntegrals I;
+    const size_t n = n_orbs;
+    I.n = n_orbs;
+    I.n_up = n_up;
+    I.n_dn = n_dn;
+    I.e_core = e_core;
+    I.n_syms = point_group_order(point_group ? point_group : "C1");
+    I.h1.assign(h1, h1 + n * n);
+    I.g2.assign(g2, g2 + n * n * n * n);
+    I.orb_sym.resize(n);
+    I.orb_order.resize(n);
+    for (size_t i = 0; i < n; i++) {
+      I.orb_sym[i] = orb_sym ? orb_sym[i] : 1u;
+      I.orb_order[i] = static_cast<unsigned>(i);
+    }
+    if (__builtin_popcountll(hf_up) != (int)n_up || __builtin_popcountll(hf_dn) != (int)n_dn)
+      throw ArgError("HF det does not match n_up / n_dn");
+    I.hf_up = hf_up;
+    I.hf_dn = hf_dn;
+    c->I = std::move(I);
+    after_integrals(c);
+  });
+}
+
+shci_status shci_get_integrals(shci_ctx* c, int* n_orbs, double* e_core, double* h1, double* g2,
+                               unsigned* orb_sym, unsigned* orb_order) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    const auto& I = c->I;
+    if (n_orbs) *n_orbs = static_cast<int>(I.n);
+    if (e_core) *e_core = I.e_core;
+    if (h1) std::memcpy(h1, I.h1.data(), I.h1.size() * 8);
+    if (g2) std::memcpy(g2, I.g2.data(), I.g2.size() * 8);
+    if (orb_sym) std::memcpy(orb_sym, I.orb_sym.data(), I.n * sizeof(unsigned));
+    if (orb_order) std::memcpy(orb_order, I.orb_order.data(), I.n * sizeof(unsigned));
+  });
+}
+
+shci_status shci_get_hf(shci_ctx* c, uint64_t* up, uint64_t* dn, double* e) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    if (up) *up = c->I.hf_up;
+    if (dn) *dn = c->I.hf_dn;
+    if (e) *e = c->energy_hf;
+  });
+}
+
+shci_status shci_build_queues(shci_ctx* c, double* info) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    upload_queues(c);
+    if (info) {
+      info[0] = c->Q.max_hci;
+      info[1] = static_cast<double>(c->Q.n_hci);
+      info[2] = c->Q.max_singles;
+      info[3] = static_cast<double>(c->Q.n_singles);
+    }
+  });
+}
+
+shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
+                          const double* coefs, size_t n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    if (n == 0 || !up || !dn) throw ArgError("empty det list");
+    const uint64_t full = c->I.n == 64 ? ~0ull : ((1ull << c->I.n) - 1ull);
+    for (size_t i = 0; i < n; i++) {
+      if ((up[i] & ~full) || (dn[i] & ~full) ||
+          __builtin_popcountll(up[i]) != (int)c->I.n_up ||
+          __builtin_popcountll(dn[i]) != (int)c->I.n_dn)
+        throw ArgError("det " + std::to_string(i) + " has the wrong electron count or orbitals");
+    }
+    c->up.assign(up, up + n);
+    c->dn.assign(dn, dn + n);
+    if (coefs) c->coefs.assign(coefs, coefs + n);
+    else {
+      c->coefs.assign(n, 1e-16);
+      c->coefs[0] = 1.0;
+    }
+    c->dets_dirty = true;
+    c->eps_tried.clear();
+    c->H.valid = false;
+    sync_dets(c);
+  });
+}
+
+shci_status shci_get_n_dets(shci_ctx* c, size_t* n) {
+  if (!c || !n) return SHCI_ERR_ARG;
+  *n = c->up.size();
+  return SHCI_OK;
+}
+
+shci_status shci_get_dets(shci_ctx* c, uint64_t* up, uint64_t* dn, double* coefs, size_t cap) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    const size_t n = c->up.size();
+    if (cap < n) throw ArgError("buffer too small for " + std::to_string(n) + " dets");
+    if (up) std::memcpy(up, c->up.data(), n * 8);
+    if (dn) std::memcpy(dn, c->dn.data(), n * 8);
+    if (coefs) {
+      sync_dets(c);
+      SHCI_CUDA(cudaMemcpyAsync(coefs, c->d_coef.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+      SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    }
+  });
+}
+
+shci_status shci_set_coefs(shci_ctx* c, const double* coefs, size_t n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (n != c->up.size() || !coefs) throw ArgError("coefficient count != det count");
+    sync_dets(c);
+    SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, coefs, n * 8, cudaMemcpyHostToDevice, c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+shci_status shci_hamiltonian_elems(shci_ctx* c, const uint64_t* ui, const uint64_t* di,
+                                   const uint64_t* uj, const uint64_t* dj, size_t n, double* out) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    hamiltonian_elems(c, ui, di, uj, dj, n, out);
+  });
+}
+
+shci_status shci_update_hamiltonian(shci_ctx* c, int precision, size_t* nnz_out) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (precision != SHCI_PREC_FP64 && precision != SHCI_PREC_MIXED)
+      throw ArgError("unknown precision");
+    sync_dets(c);
+    build_index(c);
+    const size_t nnz = build_hamiltonian(c, precision);
+    if (nnz_out) {
+      nnz_out[0] = nnz;
+      nnz_out[1] = 2 * (nnz + c->up.size()) - c->up.size();
+    }
+  });
+}
+
+shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols, double* vals,
+                                 double* diag) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    auto& H = c->H;
+    if (!H.valid) throw ArgError("no Hamiltonian built");
+    cudaStream_t s = c->stream;
+    const size_t n = H.n, nnz = H.nnz;
+    if (row_ptr) SHCI_CUDA(cudaMemcpyAsync(row_ptr, H.row_ptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (cols) SHCI_CUDA(cudaMemcpyAsync(cols, H.col.p, nnz * 4, cudaMemcpyDeviceToHost, s));
+    if (diag) SHCI_CUDA(cudaMemcpyAsync(diag, H.diag.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (vals) {
+      if (H.precision == SHCI_PREC_FP64) {
+        SHCI_CUDA(cudaMemcpyAsync(vals, H.val64.p, nnz * 8, cudaMemcpyDeviceToHost, s));
+      } else {
+        std::vector<float> hi(nnz), lo(nnz);
+        SHCI_CUDA(cudaMemcpyAsync(hi.data(), H.val32.p, nnz * 4, cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaMemcpyAsync(lo.data(), H.res32.p, nnz * 4, cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaStreamSynchronize(s));
+        for (size_t k = 0; k < nnz; k++) vals[k] = (double)hi[k] + (double)lo[k];
+      }
+    }
+    SHCI_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+shci_status shci_hv(shci_ctx* c, const double* x_dev, double* y_dev, int use_residual) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() { spmv(c, x_dev, y_dev, use_residual != 0); });
+}
+
+shci_status shci_hv_host(shci_ctx* c, const double* x, double* y, int use_residual) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    const size_t n = c->H.n;
+    if (!c->H.valid) throw ArgError("no Hamiltonian built");
+    c->f0.resize(n, 1.1);
+    c->f1.resize(n, 1.1);
+    SHCI_CUDA(cudaMemcpyAsync(c->f0.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
+    spmv(c, c->f0.p, c->f1.p, use_residual != 0);
+    SHCI_CUDA(cudaMemcpyAsync(y, c->f1.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+shci_status shci_davidson(shci_ctx* c, double tol, double* eval, int* converged, double* trace,
+                          size_t trace_cap, size_t* n_trace) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!c->H.valid || c->H.n != c->up.size()) throw ArgError("Hamiltonian not up to date");
+    sync_dets(c);
+    auto r = davidson(c, tol);
+    if (eval) *eval = r.eval;
+    if (converged) *converged = r.converged ? 1 : 0;
+    if (trace)
+      for (size_t i = 0; i < r.trace.size() && i < trace_cap; i++) trace[i] = r.trace[i];
+    if (n_trace) *n_trace = r.trace.size();
+  });
+}
+
+shci_status shci_energy_fp64(shci_ctx* c, double* energy) {
+  if (!c || !energy) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!c->H.valid) throw ArgError("no Hamiltonian built");
+    *energy = rayleigh_fp64(c);
+  });
+}
+
+shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
+                              const uint32_t* cols, const double* vals, const double* diag,
+                              const double* init, double tol, double* eval, double* evec,
+                              int* converged) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    auto& H = c->H;
+    cudaStream_t s = c->stream;
+    const size_t nnz = row_ptr[n];
+    H.n = n;
+    H.nnz = nnz;
+    H.precision = SHCI_PREC_FP64;
+    H.row_ptr.resize(n + 1);
+    H.col.resize(nnz ? nnz : 1);
+    H.val64.resize(nnz ? nnz : 1);
+    H.diag.resize(n);
+    SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p, row_ptr, (n + 1) * 8, cudaMemcpyHostToDevice, s));
+    if (nnz) {
+      SHCI_CUDA(cudaMemcpyAsync(H.col.p, cols, nnz * 4, cudaMemcpyHostToDevice, s));
+      SHCI_CUDA(cudaMemcpyAsync(H.val64.p, vals, nnz * 8, cudaMemcpyHostToDevice, s));
+    }
+    SHCI_CUDA(cudaMemcpyAsync(H.diag.p, diag, n * 8, cudaMemcpyHostToDevice, s));
+    c->d_coef.resize(n);
+    SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, init, n * 8, cudaMemcpyHostToDevice, s));
+    H.valid = true;
+    auto r = davidson(c, tol);
+    SHCI_CUDA(cudaMemcpyAsync(evec, c->d_coef.p, n * 8, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    *eval = r.eval;
+    if (converged) *converged = r.converged ? 1 : 0;
+    H.valid = false;       // the context's own Hamiltonian is gone
+    c->dets_dirty = true;  // coefficients were overwritten
+  });
+}
+
+shci_status shci_select(shci_ctx* c, double eps_var, int var_sd, size_t* n_new) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    const size_t k = select_dets(c, eps_var, var_sd != 0);
+    if (n_new) *n_new = k;
+    c->H.valid = false;
+  });
+}
+
+shci_status shci_get_eps_tried(shci_ctx* c, double* out, size_t cap) {
+  if (!c || !out) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (cap < c->eps_tried.size()) throw ArgError("buffer too small");
+    std::memcpy(out, c->eps_tried.data(), c->eps_tried.size() * 8);
+  });
+}
+
+shci_status shci_run_variation(shci_ctx* c, const double* eps_vars, size_t n_eps,
+                               const double* schedule, size_t n_sched, double target_error,
+                               int precision, double* energies) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (!eps_vars || n_eps == 0) throw ArgError("no eps_vars");
+    std::vector<double> ev(eps_vars, eps_vars + n_eps);
+    std::vector<double> sc;
+    if (schedule) sc.assign(schedule, schedule + n_sched);
+    c->var_trace.clear();
+    auto e = run_all_variations(c, ev, sc, target_error, precision, false, &c->var_trace);
+    if (energies)
+      for (size_t i = 0; i < e.size(); i++) energies[i] = e[i];
+  });
+}
+
+shci_status shci_get_launch_count(shci_ctx* c, uint64_t* n) {
+  if (!c || !n) return SHCI_ERR_ARG;
+  *n = c->launches;
+  return SHCI_OK;
+}
+
+shci_status shci_get_var_trace(shci_ctx* c, uint64_t* n_dets, uint64_t* nnz, double* energy,
+                               size_t cap, size_t* n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    const auto& t = c->var_trace;
+    if (n) *n = t.size();
+    for (size_t i = 0; i < t.size() && i < cap; i++) {
+      if (n_dets) n_dets[i] = t[i].n_dets;
+      if (nnz) nnz[i] = t[i].nnz_sym;
+      if (energy) energy[i] = t[i].energy;
+    }
+  });
+}
+
+shci_status shci_pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches,
+                         double* correction, double* uncert, size_t* n_pt_dets) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    auto r = pt2_dtm(c, energy_var, eps_pt_dtm, n_batches);
+    if (correction) *correction = r.value;
+    if (uncert) *uncert = r.uncert;
+    if (n_pt_dets) *n_pt_dets = r.n_pt_dets;
+  });
+}
+
+}  // extern "C"

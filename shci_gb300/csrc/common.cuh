@@ -1,0 +1,193 @@
+// Shared device-side definitions for the SHCI GB300 path.
+//
+// Determinants are two 64-bit spin strings (alpha = "up", beta = "dn"), n_orbs <= 64.  Integrals
+// live in HBM as dense FP64 tables (the 8-fold packed FCIDUMP set expanded on the host), plus
+// per-(i,j) contiguous slices used by the single-excitation rule.
+//
+// The Slater-Condon functions below follow src/chem/chem_system.cc:409-609 of the reference
+// term by term and in the same summation order, so FP64 matrix elements agree bit for bit
+// with a CPU evaluation of the same rules (the only multiplications are by +-1 and 2, which
+// are exact, so FMA contraction cannot change a result).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace shci {
+
+constexpr double kEps = 1.0e-12;  // src/util.h:50: |H| below this is not stored
+constexpr unsigned kFull = 0xffffffffu;
+
+struct DevIntegrals {
+  int n;                 // spatial orbitals
+  double e_core;
+  const double* h1;      // [n*n]      h(p,q)
+  const double* g2;      // [n^4]      (pq|rs) at ((p*n+q)*n+r)*n+s
+  const double* dtab;    // [n^3]      (ij|oo) at (i*n+j)*n+o       (direct)
+  const double* xtab;    // [n^3]      (io|oj) at (i*n+j)*n+o       (exchange)
+  const double* jtab;    // [n^2]      (aa|bb) at a*n+b
+  const double* ktab;    // [n^2]      (ab|ba) at a*n+b
+};
+
+__device__ __forceinline__ int popc64(uint64_t x) { return __popcll(x); }
+__device__ __forceinline__ int ctz64(uint64_t x) { return __ffsll((long long)x) - 1; }
+__device__ __forceinline__ uint64_t below(int b) { return (1ull << b) - 1ull; }
+
+__device__ __forceinline__ double g2at(const DevIntegrals& I, int p, int q, int r, int s) {
+  const int n = I.n;
+  return I.g2[((size_t)(p * n + q) * n + r) * n + s];
+}
+
+// Diagonal element (chem_system.cc:426-432, 444-457, 495-542 without the cache).
+__device__ __forceinline__ double h_diag(const DevIntegrals& I, uint64_t up, uint64_t dn) {
+  const int n = I.n;
+  double ob = 0.0;
+  for (uint64_t m = up; m; m &= m - 1) {
+    const int o = ctz64(m);
+    ob += I.h1[o * n + o];
+  }
+  if (up == dn) {
+    ob *= 2;
+  } else {
+    for (uint64_t m = dn; m; m &= m - 1) {
+      const int o = ctz64(m);
+      ob += I.h1[o * n + o];
+    }
+  }
+  double direct = 0.0, exch = 0.0;
+  for (uint64_t m = up; m; m &= m - 1) {
+    const int a = ctz64(m);
+    for (uint64_t m2 = m & (m - 1); m2; m2 &= m2 - 1) {
+      const int b = ctz64(m2);
+      direct += I.jtab[a * n + b];
+      exch -= I.ktab[a * n + b];
+    }
+  }
+  if (up == dn) {
+    direct *= 2;
+    exch *= 2;
+  } else {
+    for (uint64_t m = dn; m; m &= m - 1) {
+      const int a = ctz64(m);
+      for (uint64_t m2 = m & (m - 1); m2; m2 &= m2 - 1) {
+        const int b = ctz64(m2);
+        direct += I.jtab[a * n + b];
+        exch -= I.ktab[a * n + b];
+      }
+    }
+  }
+  for (uint64_t m = up; m; m &= m - 1) {
+    const int a = ctz64(m);
+    for (uint64_t m2 = dn; m2; m2 &= m2 - 1) {
+      const int b = ctz64(m2);
+      direct += I.jtab[a * n + b];
+    }
+  }
+  return ob + (direct + exch) + I.e_core;
+}
+
+// Single excitation oi -> oj within the spin string `same` (the other string is `oppo`);
+// `same` is the spin string of the ket-side det i.  perm = +-1.  chem_system.cc:544-577.
+__device__ __forceinline__ double h_single(const DevIntegrals& I, uint64_t same, uint64_t oppo,
+                                           int oi, int oj, int perm) {
+  const int n = I.n;
+  const double ob = perm * I.h1[oi * n + oj];
+  const double* D = I.dtab + (size_t)(oi * n + oj) * n;
+  const double* X = I.xtab + (size_t)(oi * n + oj) * n;
+  double e = 0.0;
+  for (uint64_t m = same & ~(1ull << oi) & ~(1ull << oj); m; m &= m - 1) {
+    const int o = ctz64(m);
+    e -= X[o];
+    const double direct = D[o];
+    if (oppo >> o & 1) {
+      oppo &= ~(1ull << o);
+      e += 2 * direct;
+    } else {
+      e += direct;
+    }
+  }
+  for (uint64_t m = oppo; m; m &= m - 1) e += D[ctz64(m)];
+  e *= perm;
+  return ob + e;
+}
+
+// Parity helper of src/det/half_det.cc:120-206 for one moved orbital: electrons of `s` below b.
+__device__ __forceinline__ int below_count(uint64_t s, int b) { return popc64(s & below(b)); }
+
+// H_ij for dets whose excitation degree is known to be 1 or 2 (or 0: diagonal).  up/dn
+// differences are given; returns 0 for degree > 2.  Equivalent to get_hamiltonian_elem(i,j,-1).
+__device__ __forceinline__ double h_offdiag(const DevIntegrals& I, uint64_t ui, uint64_t di,
+                                            uint64_t uj, uint64_t dj) {
+  const uint64_t xu = ui ^ uj, xd = di ^ dj;
+  const int nu = popc64(xu) >> 1, nd = popc64(xd) >> 1;
+  if (nu + nd > 2 || nu + nd == 0) return 0.0;
+  if (nu == 1 && nd == 0) {
+    const int oi = ctz64(ui & xu), oj = ctz64(uj & xu);
+    const int par = below_count(ui, oi) + below_count(uj, oj);
+    return h_single(I, ui, di, oi, oj, (par & 1) ? -1 : 1);
+  }
+  if (nd == 1 && nu == 0) {
+    const int oi = ctz64(di & xd), oj = ctz64(dj & xd);
+    const int par = below_count(di, oi) + below_count(dj, oj);
+    return h_single(I, di, ui, oi, oj, (par & 1) ? -1 : 1);
+  }
+  if (nu == 1 && nd == 1) {
+    const int ai = ctz64(ui & xu), aj = ctz64(uj & xu);
+    const int bi = ctz64(di & xd), bj = ctz64(dj & xd);
+    const int par = below_count(ui, ai) + below_count(uj, aj) + below_count(di, bi) +
+                    below_count(dj, bj);
+    const double e = g2at(I, ai, aj, bi, bj);
+    const int pu = ((below_count(ui, ai) + below_count(uj, aj)) & 1) ? -1 : 1;
+    const int pd = ((below_count(di, bi) + below_count(dj, bj)) & 1) ? -1 : 1;
+    (void)par;
+    return e * (pu * pd);
+  }
+  // same-spin double
+  const uint64_t si = nu == 2 ? ui : di, sj = nu == 2 ? uj : dj, x = nu == 2 ? xu : xd;
+  const uint64_t li = si & x, rj = sj & x;
+  const int l0 = ctz64(li), l1 = ctz64(li & (li - 1));
+  const int r0 = ctz64(rj), r1 = ctz64(rj & (rj - 1));
+  const int par = below_count(si, l0) + below_count(si, l1) + below_count(sj, r0) +
+                  below_count(sj, r1);
+  double e = g2at(I, l0, r0, l1, r1) - g2at(I, l0, r1, l1, r0);
+  e *= (par & 1) ? -1 : 1;
+  return e;
+}
+
+// ---------------------------------------------------------------- hashing (C21, a16)
+// src/det/half_det.cc:71-89 (two chunks, the second always zero) and src/det/det.h:42-49.
+__host__ __device__ __forceinline__ uint64_t half_hash(uint64_t c0) {
+  uint64_t h = 0;
+  h += c0;
+  h += (h << 10);
+  h ^= (h >> 6);
+  h += (h << 10);
+  h ^= (h >> 6);
+  h += (h << 3);
+  h ^= (h >> 11);
+  h += (h << 15);
+  return h;
+}
+__host__ __device__ __forceinline__ uint64_t det_hash(uint64_t up, uint64_t dn) {
+  uint64_t seed = half_hash(up);
+  seed ^= half_hash(dn) + 0x9e3779b9ull + (seed << 6) + (seed >> 2);
+  return seed;
+}
+// src/util.cc:111-122
+__host__ __device__ __forceinline__ uint64_t rehash(uint64_t a) {
+  uint64_t h = a;
+  h += (h << 10);
+  h ^= (h >> 6);
+  h += 982451653ull;
+  h += (h << 10);
+  h ^= (h >> 6);
+  h += (h << 3);
+  h ^= (h >> 11);
+  h += (h << 15);
+  return h;
+}
+
+// Error word written by kernels (never __trap): host checks it after each launch group.
+enum DevError : unsigned { kDevOk = 0, kDevOverflow = 1, kDevCheck = 2 };
+
+}  // namespace shci

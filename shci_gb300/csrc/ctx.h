@@ -1,0 +1,109 @@
+// The library context: every device buffer of one SHCI instance, on one stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/shci_gpu.h"
+#include "common.cuh"
+#include "devbuf.h"
+#include "host_system.h"
+#include "solver.h"
+#include "sort.cuh"
+
+namespace shci {
+
+// Determinant index used by the Hamiltonian build (rebuilt from the det list each update).
+struct DetIndex {
+  size_t n = 0;
+  size_t n_alpha = 0, n_beta = 0;
+  DevBuf<uint32_t> det_aid, det_bid;      // [n] unique alpha / beta id of each det
+  DevBuf<uint32_t> a_start, b_start;      // [n_alpha+1], [n_beta+1] group offsets
+  DevBuf<uint32_t> am_idx, bm_idx;        // [n] det ids in alpha-major / beta-major order
+  DevBuf<uint64_t> am_dn, bm_up;          // [n] the other spin string in that order
+  DevBuf<uint64_t> ua;                    // [n_alpha] sorted unique alpha strings
+  DevBuf<uint32_t> as_off;                // [n_alpha+1] alpha-singles CSR
+  DevBuf<uint32_t> as_list;               // alpha ids one single excitation away
+};
+
+// Upper-triangle Hamiltonian (strict upper part in CSR; FP64 diagonal kept apart).
+struct DevHamiltonian {
+  size_t n = 0;
+  size_t nnz = 0;
+  int precision = SHCI_PREC_FP64;
+  DevBuf<uint64_t> row_ptr;   // [n+1]
+  DevBuf<uint32_t> col;       // [nnz]
+  DevBuf<double> val64;       // [nnz]   FP64 storage
+  DevBuf<float> val32;        // [nnz]   mixed storage: FP32 value
+  DevBuf<float> res32;        // [nnz]   mixed storage: FP32 residual (value - (double)val32)
+  DevBuf<double> diag;        // [n]
+  DevBuf<uint32_t> row_cnt;   // [n] scratch
+  bool valid = false;
+};
+
+struct DevQueues {
+  size_t n_pairs = 0;
+  DevBuf<uint64_t> d_off;
+  DevBuf<double> d_H;
+  DevBuf<uint32_t> d_rs;
+  DevBuf<uint32_t> s_off;
+  DevBuf<double> s_S;
+  DevBuf<uint32_t> s_r;
+  double max_hci = 0.0, max_singles = 0.0;
+  size_t n_hci = 0, n_singles = 0;
+  bool built = false;
+};
+
+struct Davidson {
+  DevBuf<double> v[5], Hv[5], w, Hw;
+  DevBuf<double> scal;     // device scalars
+  DevBuf<double> partial;  // dot partial sums
+};
+
+}  // namespace shci
+
+struct shci_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  shci::MemTracker mem;
+
+  bool have_integrals = false;
+  shci::HostIntegrals I;
+  shci::DevBuf<double> h1, g2, dtab, xtab, jtab, ktab;
+  shci::DevIntegrals dI{};
+  double energy_hf = 0.0;
+
+  shci::DevQueues Q;
+
+  // determinants (host mirror + device) in the canonical order
+  std::vector<uint64_t> up, dn;
+  std::vector<double> coefs;
+  shci::DevBuf<uint64_t> d_up, d_dn;
+  shci::DevBuf<double> d_coef;
+  bool dets_dirty = true;  // device copy out of date
+
+  // sorted membership keys of the current det list (for selection / PT2)
+  shci::DevBuf<uint64_t> set_up, set_dn;
+
+  std::vector<double> eps_tried;
+
+  shci::DetIndex idx;
+  shci::DevHamiltonian H;
+  shci::Davidson dav;
+  shci::SortScratch sort;
+
+  // generic scratch
+  shci::DevBuf<uint64_t> k0, k1, k2;
+  shci::DevBuf<uint32_t> u0, u1, u2;
+  shci::DevBuf<double> f0, f1;
+  shci::DevBuf<unsigned> err_word;
+
+  // per-iteration record of the last variational run
+  std::vector<shci::VarIter> var_trace;
+
+  // counters for the bench: kernels launched by this context
+  size_t launches = 0;
+};

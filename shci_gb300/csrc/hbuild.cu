@@ -1,0 +1,352 @@
+// Determinant index (K1/K2) and Hamiltonian build (K3).
+//
+// Replaces Hamiltonian<S>::update_abdet / update_abm1 / update_absingles / update_matrix
+// (src/solver/hamiltonian.h:157-598).  The reference keeps hash maps from alpha / beta
+// strings to det lists and intersects alpha-single lists with beta-single lists per row.
+// Here the det list is radix-sorted twice on the device:
+//   alpha-major order (by up, then dn): groups of dets sharing an alpha string;
+//   beta-major order  (by dn, then up): groups of dets sharing a beta string;
+// and each unique alpha string gets the list of unique alphas one single excitation away
+// (found by binary search of the n_up * (n - n_up) single excitations in the sorted unique
+// alphas, which replaces the alpha-minus-one hash map).  A warp then builds one row:
+//   (a) same beta string, any alpha: scan the beta group      (hamiltonian.h:430-442)
+//   (b) same alpha string, any beta: scan the alpha group     (hamiltonian.h:456-468)
+//   (c) alpha single x beta single:  scan the alpha groups of the alpha singles and keep the
+//       members whose beta string differs by one electron (popc(xor) == 2)  (:482-532)
+// keeping j > i (strict upper triangle) and |H_ij| >= 1e-12 (:440).  The result is the same
+// element set the reference builds (its incremental update only changes the order in
+// which rows are filled).  A count pass sizes each row, a scan gives row offsets, and a
+// fill pass writes the columns/values in the same deterministic traversal order.
+#include "ctx.h"
+#include "kernels.h"
+
+namespace shci {
+
+namespace {
+
+constexpr int kWarps = 8;  // warps per block in the row kernels
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+__global__ void k_group_flags(const uint64_t* sorted, size_t n, uint32_t* flags) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    flags[k] = (k == 0 || sorted[k] != sorted[k - 1]) ? 1u : 0u;
+}
+
+// After the exclusive scan of the flags: g = scan[k] + flag[k] - 1 is the group of k.
+__global__ void k_group_fill(const uint64_t* sorted, const uint32_t* perm, const uint32_t* flags,
+                             const uint32_t* scan, const uint64_t* other, size_t n,
+                             uint32_t* start, uint64_t* uniq, uint32_t* det_gid,
+                             uint64_t* other_sorted) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t g = scan[k] + flags[k] - 1u;
+    const uint32_t d = perm[k];
+    if (flags[k]) {
+      start[g] = static_cast<uint32_t>(k);
+      if (uniq) uniq[g] = sorted[k];
+    }
+    det_gid[d] = g;
+    other_sorted[k] = other[d];
+  }
+}
+
+__device__ __forceinline__ bool bsearch_u64(const uint64_t* a, uint32_t n, uint64_t key,
+                                            uint32_t* pos) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint64_t v = a[mid];
+    if (v < key) lo = mid + 1;
+    else hi = mid;
+  }
+  *pos = lo;
+  return lo < n && a[lo] == key;
+}
+
+// Alpha singles: for each unique alpha, the unique alphas one single excitation away.
+template <bool FILL>
+__global__ void k_alpha_singles(const uint64_t* ua, uint32_t n_alpha, int n_orbs,
+                                uint32_t* cnt, const uint32_t* off, uint32_t* list) {
+  const uint64_t full = n_orbs == 64 ? ~0ull : ((1ull << n_orbs) - 1ull);
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_alpha;
+       g += gridDim.x * blockDim.x) {
+    const uint64_t a = ua[g];
+    uint32_t c = 0;
+    const uint32_t base = FILL ? off[g] : 0;
+    for (uint64_t mo = a; mo; mo &= mo - 1) {
+      const uint64_t ob = mo & (~mo + 1);
+      for (uint64_t mv = full & ~a; mv; mv &= mv - 1) {
+        const uint64_t vb = mv & (~mv + 1);
+        uint32_t pos;
+        if (bsearch_u64(ua, n_alpha, a ^ ob ^ vb, &pos)) {
+          if (FILL) list[base + c] = pos;
+          c++;
+        }
+      }
+    }
+    if (!FILL) cnt[g] = c;
+  }
+}
+
+struct IndexView {
+  const uint32_t *det_aid, *det_bid, *a_start, *b_start, *am_idx, *bm_idx, *as_off, *as_list;
+  const uint64_t *am_dn, *bm_up, *ua;
+};
+
+// MODE 0: count (and diagonal), MODE 1: fill FP64, MODE 2: fill mixed (FP32 value+residual)
+template <int MODE>
+__global__ void __launch_bounds__(kWarps * 32)
+    k_hbuild(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
+             uint32_t n, IndexView ix, uint32_t* row_cnt, const uint64_t* row_ptr,
+             uint32_t* col, double* v64, float* v32, float* r32, double* diag,
+             unsigned* work) {
+  const unsigned lane = threadIdx.x & 31;
+  while (true) {
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(work, 1u);
+    i = __shfl_sync(kFull, i, 0);
+    if (i >= n) break;
+    const uint64_t ui = up[i], di = dn[i];
+    if (MODE == 0 && lane == 0) diag[i] = h_diag(I, ui, di);
+    const uint32_t a = ix.det_aid[i], b = ix.det_bid[i];
+    uint64_t base = MODE ? row_ptr[i] : 0;
+    uint32_t cnt = 0;
+    auto emit = [&](bool keep, uint32_t j, double H) {
+      const unsigned bal = __ballot_sync(kFull, keep);
+      if (MODE && keep) {
+        const uint64_t pos = base + cnt + __popc(bal & lanemask_lt());
+        col[pos] = j;
+        if (MODE == 1) {
+          v64[pos] = H;
+        } else {
+          const float hi = static_cast<float>(H);
+          v32[pos] = hi;
+          r32[pos] = static_cast<float>(H - static_cast<double>(hi));
+        }
+      }
+      cnt += __popc(bal);
+    };
+    // (a) same beta string
+    {
+      const uint32_t s = ix.b_start[b], e = ix.b_start[b + 1];
+      for (uint32_t k0 = s; k0 < e; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        bool keep = false;
+        uint32_t j = 0;
+        double H = 0.0;
+        if (k < e) {
+          j = ix.bm_idx[k];
+          if (j > i) {
+            const uint64_t uj = ix.bm_up[k];
+            if (popc64(uj ^ ui) <= 4) {
+              H = h_offdiag(I, ui, di, uj, di);
+              keep = fabs(H) >= kEps;
+            }
+          }
+        }
+        emit(keep, j, H);
+      }
+    }
+    // (b) same alpha string
+    {
+      const uint32_t s = ix.a_start[a], e = ix.a_start[a + 1];
+      for (uint32_t k0 = s; k0 < e; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        bool keep = false;
+        uint32_t j = 0;
+        double H = 0.0;
+        if (k < e) {
+          j = ix.am_idx[k];
+          if (j > i) {
+            const uint64_t dj = ix.am_dn[k];
+            if (popc64(dj ^ di) <= 4) {
+              H = h_offdiag(I, ui, di, ui, dj);
+              keep = fabs(H) >= kEps;
+            }
+          }
+        }
+        emit(keep, j, H);
+      }
+    }
+    // (c) alpha single x beta single: flatten (alpha single, group member) pairs over lanes
+    {
+      const uint32_t s0 = ix.as_off[a], s1 = ix.as_off[a + 1];
+      for (uint32_t c0 = s0; c0 < s1; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        uint32_t g = 0, gs = 0, gn = 0;
+        if (c < s1) {
+          g = ix.as_list[c];
+          gs = ix.a_start[g];
+          gn = ix.a_start[g + 1] - gs;
+        }
+        // inclusive scan of group sizes across the chunk
+        uint32_t inc = gn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(kFull, inc, o);
+          if (lane >= (unsigned)o) inc += t;
+        }
+        const uint32_t total = __shfl_sync(kFull, inc, 31);
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+          const uint32_t t = t0 + lane;
+          bool keep = false;
+          uint32_t j = 0;
+          double H = 0.0;
+          // owner lane = number of lanes whose inclusive prefix is <= t (prefixes are
+          // non-decreasing); a fixed 5-step search so every lane runs the same shuffles
+          uint32_t lo = 0;
+#pragma unroll
+          for (uint32_t step = 16; step; step >>= 1) {
+            const uint32_t v = __shfl_sync(kFull, inc, lo + step - 1);
+            if (v <= t) lo += step;
+          }
+          const uint32_t o_inc = __shfl_sync(kFull, inc, lo);
+          const uint32_t o_gn = __shfl_sync(kFull, gn, lo);
+          const uint32_t o_gs = __shfl_sync(kFull, gs, lo);
+          const uint32_t o_g = __shfl_sync(kFull, g, lo);
+          if (t < total) {
+            const uint32_t k = o_gs + (t - (o_inc - o_gn));
+            j = ix.am_idx[k];
+            if (j > i) {
+              const uint64_t dj = ix.am_dn[k];
+              if (popc64(dj ^ di) == 2) {
+                H = h_offdiag(I, ui, di, ix.ua[o_g], dj);
+                keep = fabs(H) >= kEps;
+              }
+            }
+          }
+          emit(keep, j, H);
+        }
+      }
+    }
+    if (MODE == 0 && lane == 0) row_cnt[i] = cnt;
+  }
+}
+
+}  // namespace
+
+void build_index(shci_ctx* c) {
+  auto& ix = c->idx;
+  const size_t n = c->up.size();
+  cudaStream_t s = c->stream;
+  const int nb = c->I.n;
+  ix.n = n;
+  c->k0.resize(n, 1.25);
+  c->k1.resize(n, 1.25);
+  c->u0.resize(n, 1.25);
+  c->u1.resize(n, 1.25);
+  c->u2.resize(n, 1.25);
+  ix.det_aid.resize(n, 1.25);
+  ix.det_bid.resize(n, 1.25);
+  ix.am_idx.resize(n, 1.25);
+  ix.bm_idx.resize(n, 1.25);
+  ix.am_dn.resize(n, 1.25);
+  ix.bm_up.resize(n, 1.25);
+  for (int major = 0; major < 2; major++) {
+    // major 0: alpha-major (sort by dn, then stably by up); major 1: beta-major.
+    const uint64_t* first = major == 0 ? c->d_dn.p : c->d_up.p;
+    const uint64_t* second = major == 0 ? c->d_up.p : c->d_dn.p;
+    SHCI_CUDA(cudaMemcpyAsync(c->k0.p, first, n * 8, cudaMemcpyDeviceToDevice, s));
+    iota_u32(c->u0.p, n, s);
+    radix_sort_pairs(c->k0, c->u0, n, 0, nb, s, c->sort);
+    gather_u64(second, c->u0.p, c->k1.p, n, s);
+    radix_sort_pairs(c->k1, c->u0, n, 0, nb, s, c->sort);
+    k_group_flags<<<grid_for(n, 256), 256, 0, s>>>(c->k1.p, n, c->u1.p);
+    SHCI_LAUNCH_CHECK();
+    const uint32_t ng = exclusive_scan_u32(c->u1.p, c->u2.p, n, s, c->sort);
+    auto& start = major == 0 ? ix.a_start : ix.b_start;
+    auto& perm = major == 0 ? ix.am_idx : ix.bm_idx;
+    auto& other_sorted = major == 0 ? ix.am_dn : ix.bm_up;
+    auto& gid = major == 0 ? ix.det_aid : ix.det_bid;
+    start.resize(ng + 1, 1.25);
+    if (major == 0) ix.ua.resize(ng, 1.25);
+    SHCI_CUDA(cudaMemcpyAsync(perm.p, c->u0.p, n * 4, cudaMemcpyDeviceToDevice, s));
+    k_group_fill<<<grid_for(n, 256), 256, 0, s>>>(c->k1.p, c->u0.p, c->u1.p, c->u2.p, first, n,
+                                                  start.p, major == 0 ? ix.ua.p : nullptr,
+                                                  gid.p, other_sorted.p);
+    SHCI_LAUNCH_CHECK();
+    const uint32_t nn = static_cast<uint32_t>(n);
+    SHCI_CUDA(cudaMemcpyAsync(start.p + ng, &nn, 4, cudaMemcpyHostToDevice, s));
+    if (major == 0) ix.n_alpha = ng;
+    else ix.n_beta = ng;
+    SHCI_CUDA(cudaStreamSynchronize(s));  // nn lives on the host stack
+  }
+  // alpha singles
+  const uint32_t na = static_cast<uint32_t>(ix.n_alpha);
+  ix.as_off.resize(na + 1, 1.25);
+  c->u1.reserve(na + 1, 1.25);
+  k_alpha_singles<false><<<grid_for(na, 128), 128, 0, s>>>(ix.ua.p, na, nb, c->u1.p, nullptr,
+                                                           nullptr);
+  SHCI_LAUNCH_CHECK();
+  const uint32_t tot = exclusive_scan_u32(c->u1.p, ix.as_off.p, na, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(ix.as_off.p + na, &tot, 4, cudaMemcpyHostToDevice, s));
+  ix.as_list.resize(tot ? tot : 1, 1.25);
+  k_alpha_singles<true><<<grid_for(na, 128), 128, 0, s>>>(ix.ua.p, na, nb, nullptr, ix.as_off.p,
+                                                          ix.as_list.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 2 * (4 * 2 + 4) + 3;
+}
+
+size_t build_hamiltonian(shci_ctx* c, int precision) {
+  auto& H = c->H;
+  auto& ix = c->idx;
+  const size_t n = c->up.size();
+  cudaStream_t s = c->stream;
+  if (n >= 0xffffffffull) throw ArgError("more than 2^32-1 dets");
+  H.n = n;
+  H.precision = precision;
+  H.valid = false;
+  H.row_ptr.resize(n + 1, 1.25);
+  H.row_cnt.resize(n + 1, 1.25);
+  H.diag.resize(n, 1.25);
+  c->err_word.resize(2);
+  IndexView v{ix.det_aid.p, ix.det_bid.p, ix.a_start.p, ix.b_start.p, ix.am_idx.p, ix.bm_idx.p,
+              ix.as_off.p,  ix.as_list.p, ix.am_dn.p,   ix.bm_up.p,   ix.ua.p};
+  int dev_sms = 0;
+  SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
+  unsigned* work = c->err_word.p;
+  SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                           H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
+                                           nullptr, H.diag.p, work);
+  SHCI_LAUNCH_CHECK();
+  // row_ptr = exclusive scan of counts (counts widened to 64 bit)
+  widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
+  const uint64_t nnz = exclusive_scan_u64(H.row_ptr.p, H.row_ptr.p, n, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p + n, &nnz, 8, cudaMemcpyHostToDevice, s));
+  H.nnz = nnz;
+  const size_t cap = nnz ? nnz : 1;
+  H.col.resize(cap, 1.1);
+  if (precision == SHCI_PREC_FP64) {
+    H.val64.resize(cap, 1.1);
+    H.val32.release();
+    H.res32.release();
+  } else {
+    H.val32.resize(cap, 1.1);
+    H.res32.resize(cap, 1.1);
+    H.val64.release();
+  }
+  SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  if (precision == SHCI_PREC_FP64) {
+    k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                             nullptr, H.row_ptr.p, H.col.p, H.val64.p, nullptr,
+                                             nullptr, nullptr, work);
+  } else {
+    k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                             nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
+                                             H.res32.p, nullptr, work);
+  }
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  H.valid = true;
+  c->launches += 5;
+  return nnz;
+}
+
+}  // namespace shci

@@ -1,0 +1,170 @@
+// Heat-bath candidate generation shared by selection (select.cu) and PT2 (pt2.cu).
+//
+// The reference's ChemSystem::find_connected_dets (src/chem/chem_system.cc:289-402) walks
+// singles_queue[p] and hci_queue[pq] (sorted by descending |H|) until the first entry below
+// eps_min, skipping doubles with |H| >= eps_max.  The same queues sit in HBM in CSR form and
+// a binary search gives each (det, slot) its exact entry range.  A det has n_elecs "single"
+// slots (one per electron) and n_elecs (n_elecs - 1) / 2 "double" slots (one per electron
+// pair, in the reference's p_id < q_id order).
+#pragma once
+
+#include "common.cuh"
+
+namespace shci {
+
+constexpr int kSelWarps = 8;
+constexpr uint64_t kInvalid = ~0ull;
+
+struct SelParams {
+  DevIntegrals I;
+  const uint64_t* up;
+  const uint64_t* dn;
+  const double* coef;
+  double* eps_tried;
+  const uint64_t* d_off;
+  const double* d_H;
+  const uint32_t* d_rs;
+  const uint32_t* s_off;
+  const double* s_S;
+  const uint32_t* s_r;
+  const uint32_t* pair_tab;  // pair k -> p_id | q_id << 16
+  const uint64_t* set_up;    // sorted variational set
+  const uint64_t* set_dn;
+  uint32_t set_n;
+  double eps_var;
+  double max_hci, max_singles;
+  int n_orbs, n_up, n_elecs, n_pairs;
+  int var_sd;
+  uint32_t pass, n_src_total;  // sources are i = pass + 5 k, i < n_src_total
+};
+
+__device__ __forceinline__ int nth_bit(uint64_t x, int k) {
+  const unsigned lo = static_cast<unsigned>(x), hi = static_cast<unsigned>(x >> 32);
+  const int cl = __popc(lo);
+  if (k < cl) return __fns(lo, 0, k + 1);
+  return 32 + __fns(hi, 0, k - cl + 1);
+}
+
+// spin-orbital index of electron e (up electrons first, then dn + n)
+__device__ __forceinline__ int elec_orb(uint64_t up, uint64_t dn, int e, int n_up, int n) {
+  return e < n_up ? nth_bit(up, e) : nth_bit(dn, e - n_up) + n;
+}
+
+__device__ __forceinline__ uint32_t first_below(const double* a, uint32_t lo, uint32_t hi,
+                                                double x) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ size_t c2(size_t a, size_t b) {
+  return a > b ? (a * (a + 1)) / 2 + b : (b * (b + 1)) / 2 + a;
+}
+
+// Entry range [lo, lo + cnt) of slot `slot` for the det (eps window [eps_min, eps_max)).
+__device__ __forceinline__ void slot_range(const SelParams& P, uint64_t up, uint64_t dn, int slot,
+                                           double eps_min, double eps_max, uint32_t* lo,
+                                           uint32_t* cnt) {
+  *lo = 0;
+  *cnt = 0;
+  const int n = P.n_orbs;
+  if (slot < P.n_elecs) {
+    if (eps_min > P.max_singles) return;
+    const int p = slot < P.n_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
+    const uint32_t a = P.s_off[p], b = P.s_off[p + 1];
+    *lo = a;
+    *cnt = first_below(P.s_S, a, b, eps_min) - a;
+    return;
+  }
+  if (eps_min > P.max_hci) return;
+  const uint32_t pr = P.pair_tab[slot - P.n_elecs];
+  const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
+  const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
+  int p2 = p, q2 = q;
+  if (p >= n && q >= n) {
+    p2 -= n;
+    q2 -= n;
+  } else if (p < n && q >= n && p > q - n) {
+    p2 = q - n;
+    q2 = p + n;
+  }
+  const size_t pq = c2(p2, q2);
+  const uint32_t a = static_cast<uint32_t>(P.d_off[pq]), b = static_cast<uint32_t>(P.d_off[pq + 1]);
+  const uint32_t s = first_below(P.d_H, a, b, eps_max);
+  const uint32_t e = first_below(P.d_H, s, b, eps_min);
+  *lo = s;
+  *cnt = e - s;
+}
+
+__device__ __forceinline__ bool in_set(const SelParams& P, uint64_t u, uint64_t d) {
+  uint32_t lo = 0, hi = P.set_n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint64_t su = P.set_up[mid], sd = P.set_dn[mid];
+    if (su < u || (su == u && sd < d)) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < P.set_n && P.set_up[lo] == u && P.set_dn[lo] == d;
+}
+
+__device__ __forceinline__ double src_eps_min(const SelParams& P, uint32_t i) {
+  double e = P.eps_var / fabs(P.coef[i]);
+  if (i == 0 && P.var_sd) e = 0.0;
+  return e;
+}
+
+
+// Candidate det for entry e of slot `slot` of det (up, dn).  Returns false when the target
+// orbitals are occupied (the reference's occupancy checks).  *single tells the slot kind.
+__device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, uint64_t dn,
+                                               int slot, uint32_t e, uint64_t* cu,
+                                               uint64_t* cd, bool* single) {
+  const int n = P.n_orbs;
+  *cu = up;
+  *cd = dn;
+  if (slot < P.n_elecs) {
+    *single = true;
+    const bool is_up = slot < P.n_up;
+    const int p = is_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
+    const int r = static_cast<int>(P.s_r[e]);
+    if (is_up) {
+      if (up >> r & 1) return false;
+      *cu = (up & ~(1ull << p)) | (1ull << r);
+    } else {
+      if (dn >> r & 1) return false;
+      *cd = (dn & ~(1ull << p)) | (1ull << r);
+    }
+    return true;
+  }
+  *single = false;
+  const uint32_t pr = P.pair_tab[slot - P.n_elecs];
+  const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
+  const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
+  const uint32_t rs = P.d_rs[e];
+  int r = rs & 0xffff, s = rs >> 16;
+  if (p >= n && q >= n) {
+    r += n;
+    s += n;
+  } else if (p < n && q >= n && p > q - n) {
+    const int tmp = s - n;
+    s = r + n;
+    r = tmp;
+  }
+  const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
+  if (occ_r) return false;
+  const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);
+  if (occ_s) return false;
+  uint64_t u = up, d = dn;
+  if (p < n) u &= ~(1ull << p); else d &= ~(1ull << (p - n));
+  if (q < n) u &= ~(1ull << q); else d &= ~(1ull << (q - n));
+  if (r < n) u |= 1ull << r; else d |= 1ull << (r - n);
+  if (s < n) u |= 1ull << s; else d |= 1ull << (s - n);
+  *cu = u;
+  *cd = d;
+  return true;
+}
+
+}  // namespace shci

@@ -1,0 +1,57 @@
+// Host-side chemistry system of the product library: FCIDUMP reading, orbital reordering,
+// dense integral tables and the heat-bath queues that are uploaded to HBM.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace shci {
+
+struct HostIntegrals {
+  unsigned n = 0;            // spatial orbitals
+  unsigned n_up = 0, n_dn = 0;
+  double e_core = 0.0;
+  std::vector<unsigned> orb_sym;    // 1-based irreps, reordered
+  std::vector<unsigned> orb_order;  // new index -> FCIDUMP index (0-based)
+  std::vector<double> h1;           // [n*n]
+  std::vector<double> g2;           // [n^4]
+  uint64_t hf_up = 0, hf_dn = 0;
+  unsigned n_syms = 1;
+
+  double h(unsigned p, unsigned q) const { return h1[p * n + q]; }
+  double g(unsigned p, unsigned q, unsigned r, unsigned s) const {
+    return g2[((size_t)(p * n + q) * n + r) * n + s];
+  }
+};
+
+// Reads FCIDUMP and prepares the integrals like Integrals::load (src/chem/integrals.cc:17-384).
+// Throws std::runtime_error with a message on failure.
+void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsigned n_dn,
+                  const std::string& point_group, int reorder, const unsigned* occs_up,
+                  const unsigned* occs_dn);
+
+unsigned point_group_order(const std::string& pg);
+
+// Heat-bath queues in CSR form (src/chem/chem_system.cc:74-196).
+struct HostQueues {
+  // doubles: pair index pq = combine2(p, q) over spin-orbitals (q may be >= n)
+  std::vector<uint64_t> d_off;   // [n_pairs + 1]
+  std::vector<double> d_H;       // |H|, descending within a pair
+  std::vector<uint32_t> d_rs;    // r | s << 16 (spin-orbital indices as the reference stores)
+  // singles: per spatial orbital p
+  std::vector<uint32_t> s_off;   // [n + 1]
+  std::vector<double> s_S;       // upper bound S, descending
+  std::vector<uint32_t> s_r;
+  double max_hci = 0.0, max_singles = 0.0;
+};
+
+void build_queues(const HostIntegrals& I, HostQueues& Q);
+
+double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn);
+
+inline size_t combine2(size_t a, size_t b) {
+  return a > b ? (a * (a + 1)) / 2 + b : (b * (b + 1)) / 2 + a;
+}
+
+}  // namespace shci

@@ -1,0 +1,58 @@
+// Host-callable entry points of the device kernels (one translation unit per stage).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "devbuf.h"
+
+struct shci_ctx;
+
+namespace shci {
+
+// misc.cu
+void widen_u32_u64(const uint32_t* in, uint64_t* out, size_t n, cudaStream_t s);
+void upload_integrals(shci_ctx* c);
+void upload_queues(shci_ctx* c);
+void sync_dets(shci_ctx* c);          // host det list -> device (if dirty)
+void hamiltonian_elems(shci_ctx* c, const uint64_t* ui, const uint64_t* di, const uint64_t* uj,
+                       const uint64_t* dj, size_t n, double* out);
+
+// hbuild.cu
+void build_index(shci_ctx* c);
+size_t build_hamiltonian(shci_ctx* c, int precision);
+
+// spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
+void spmv(shci_ctx* c, const double* x, double* y, bool residual);
+
+// davidson.cu
+struct DavidsonOut {
+  double eval = 0.0;
+  bool converged = false;
+  std::vector<double> trace;
+  int n_matvec = 0;
+};
+// Runs on c->H with the initial vector c->d_coef (length H.n); Ritz vector left in d_coef.
+DavidsonOut davidson(shci_ctx* c, double tol);
+double rayleigh_fp64(shci_ctx* c);
+void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs);
+
+// select.cu
+size_t select_dets(shci_ctx* c, double eps_var, bool var_sd);
+void rebuild_det_set(shci_ctx* c);
+size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, size_t m,
+                         DevBuf<double>* vals = nullptr);
+void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const double* v, size_t m,
+                   DevBuf<uint64_t>& oa, DevBuf<uint64_t>& ob, DevBuf<double>* ov, size_t* n_out);
+
+// pt2.cu
+struct Pt2Out {
+  double value = 0.0, uncert = 0.0;
+  size_t n_pt_dets = 0;
+};
+Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches);
+
+}  // namespace shci

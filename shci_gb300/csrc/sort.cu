@@ -1,0 +1,294 @@
+// Device-wide exclusive scan and stable LSD radix sort.
+//
+// Radix sort: 8-bit digits, one pass per digit over [begin_bit, end_bit).  Each pass is
+//   (1) per-tile digit histograms (warp-aggregated shared atomics),
+//   (2) an exclusive scan of the digit-major [256 x tiles] histogram -> scatter bases,
+//   (3) a stable scatter: each 4096-item tile is walked in 16 rounds of 256 consecutive items;
+//       within a round an item's rank among equal digits comes from __match_any_sync (inside
+//       its warp) plus the per-warp counts of lower warps, so input order is preserved.
+// Passes whose digit is constant over all keys are skipped (detected from the histogram).
+#include "sort.cuh"
+
+namespace shci {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive prefix and
+// writes the block total to *total.
+template <class T>
+__device__ __forceinline__ T block_exclusive(T v, T* total) {
+  __shared__ T s_w[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const T inc = warp_inclusive(v);
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < kScanThreads / 32 ? s_w[lane] : T(0);
+    w = warp_inclusive(w);
+    if (lane < kScanThreads / 32) s_w[lane] = w;
+  }
+  __syncthreads();
+  const T before = warp ? s_w[warp - 1] : T(0);
+  *total = s_w[kScanThreads / 32 - 1];
+  __syncthreads();
+  return before + inc - v;
+}
+
+template <class T>
+__global__ void k_tile_sums(const T* in, size_t n, T* sums) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  T acc = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+    if (base + k < n) acc += in[base + k];
+  T tot;
+  block_exclusive(acc, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+template <class T>
+__global__ void k_tile_scan(const T* in, T* out, size_t n, const T* offsets, T* total_dev) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  T items[kScanItems];
+  T acc = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    items[k] = base + k < n ? in[base + k] : T(0);
+    acc += items[k];
+  }
+  T tot;
+  T pre = block_exclusive(acc, &tot);
+  if (offsets) pre += offsets[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < n) {
+      out[base + k] = pre;
+      if (total_dev && base + k == n - 1) *total_dev = pre + items[k];
+    }
+    pre += items[k];
+  }
+}
+
+template <class T>
+void scan_rec(const T* in, T* out, size_t n, cudaStream_t s, T* part, T* total_dev) {
+  const size_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb <= 1) {
+    k_tile_scan<T><<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, total_dev);
+    SHCI_LAUNCH_CHECK();
+    return;
+  }
+  k_tile_sums<T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, part);
+  SHCI_LAUNCH_CHECK();
+  scan_rec<T>(part, part, nb, s, part + nb, nullptr);
+  k_tile_scan<T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, part, total_dev);
+  SHCI_LAUNCH_CHECK();
+}
+
+size_t scan_part_size(size_t n) {
+  size_t tot = 2, m = n;
+  while (m > (size_t)kScanTile) {
+    m = (m + kScanTile - 1) / kScanTile;
+    tot += m;
+  }
+  return tot + 1;
+}
+
+// ------------------------------------------------------------------------- radix sort
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 16;
+constexpr int kSortTile = kSortThreads * kSortRounds;
+
+__global__ void k_radix_hist(const uint64_t* keys, size_t n, int shift, uint32_t* hist,
+                             unsigned n_tiles) {
+  __shared__ uint32_t s_h[256];
+  s_h[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t t0 = (size_t)blockIdx.x * kSortTile;
+  const unsigned lane = threadIdx.x & 31;
+  for (int r = 0; r < kSortRounds; r++) {
+    const size_t idx = t0 + (size_t)r * kSortThreads + threadIdx.x;
+    const bool valid = idx < n;
+    const unsigned d = valid ? (unsigned)((keys[idx] >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&s_h[d], __popc(peers));
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * n_tiles + blockIdx.x] = s_h[threadIdx.x];
+}
+
+template <class V>
+__global__ void k_radix_scatter(const uint64_t* kin, const V* vin, uint64_t* kout, V* vout,
+                                size_t n, int shift, const uint32_t* offs, unsigned n_tiles) {
+  __shared__ uint32_t s_base[256];
+  __shared__ uint32_t s_wcnt[kSortThreads / 32][256];
+  const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const size_t t0 = (size_t)blockIdx.x * kSortTile;
+  s_base[tid] = offs[(size_t)tid * n_tiles + blockIdx.x];
+  for (int r = 0; r < kSortRounds; r++) {
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; w++) s_wcnt[w][tid] = 0;
+    __syncthreads();
+    const size_t idx = t0 + (size_t)r * kSortThreads + tid;
+    const bool valid = idx < n;
+    const uint64_t k = valid ? kin[idx] : 0ull;
+    const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) s_wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      unsigned pre = 0;
+      for (unsigned w = 0; w < warp; w++) pre += s_wcnt[w][d];
+      const unsigned pos = s_base[d] + pre + rank;
+      kout[pos] = k;
+      vout[pos] = vin[idx];
+    }
+    __syncthreads();
+    unsigned tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; w++) tot += s_wcnt[w][tid];
+    s_base[tid] += tot;
+    __syncthreads();
+  }
+}
+
+// Bits set in the OR of (k xor k0) over all keys: digits where every key agrees are skipped.
+__global__ void k_key_spread(const uint64_t* keys, size_t n, unsigned long long* spread) {
+  const uint64_t k0 = keys[0];
+  uint64_t acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    acc |= keys[i] ^ k0;
+  for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicOr(spread, (unsigned long long)acc);
+}
+
+template <class V>
+void radix_sort_impl(DevBuf<uint64_t>& keys, DevBuf<V>& vals, size_t n, int begin_bit,
+                     int end_bit, cudaStream_t s, SortScratch& sc, DevBuf<V>& valt) {
+  if (n <= 1 || begin_bit >= end_bit) return;
+  if (n > 0xffffffffull) throw ArgError("radix sort: more than 2^32 items");
+  // Which digits vary at all?
+  sc.part64.reserve(scan_part_size(1));
+  unsigned long long* spread = reinterpret_cast<unsigned long long*>(sc.part64.p);
+  SHCI_CUDA(cudaMemsetAsync(spread, 0, sizeof(unsigned long long), s));
+  k_key_spread<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(keys.p, n, spread);
+  SHCI_LAUNCH_CHECK();
+  unsigned long long sp = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&sp, spread, sizeof(sp), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+
+  const unsigned n_tiles = static_cast<unsigned>((n + kSortTile - 1) / kSortTile);
+  sc.kalt.reserve(n, 1.25);
+  valt.reserve(n, 1.25);
+  sc.hist.reserve((size_t)256 * n_tiles, 1.25);
+  sc.part32.reserve(scan_part_size((size_t)256 * n_tiles), 1.25);
+  uint64_t* kin = keys.p;
+  V* vin = vals.p;
+  uint64_t* kout = sc.kalt.p;
+  V* vout = valt.p;
+  for (int shift = begin_bit; shift < end_bit; shift += 8) {
+    const uint64_t mask = (shift + 8 >= 64 ? ~0ull : ((1ull << (shift + 8)) - 1ull)) &
+                          ~((1ull << shift) - 1ull);
+    if ((sp & mask) == 0) continue;
+    k_radix_hist<<<n_tiles, kSortThreads, 0, s>>>(kin, n, shift, sc.hist.p, n_tiles);
+    SHCI_LAUNCH_CHECK();
+    scan_rec<uint32_t>(sc.hist.p, sc.hist.p, (size_t)256 * n_tiles, s, sc.part32.p, nullptr);
+    k_radix_scatter<V><<<n_tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift,
+                                                        sc.hist.p, n_tiles);
+    SHCI_LAUNCH_CHECK();
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  if (kin != keys.p) {
+    // the result lives in the ping-pong buffers: hand their storage to the caller
+    const size_t kn = keys.n, vn = vals.n;
+    swap_storage(keys, sc.kalt);
+    swap_storage(vals, valt);
+    keys.n = kn;
+    vals.n = vn;
+  }
+}
+
+__global__ void k_iota(uint32_t* v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    v[i] = static_cast<uint32_t>(i);
+}
+
+__global__ void k_gather_u64(const uint64_t* src, const uint32_t* idx, uint64_t* out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = src[idx[i]];
+}
+
+}  // namespace
+
+uint64_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, size_t n, cudaStream_t s,
+                            SortScratch& sc) {
+  if (n == 0) return 0;
+  sc.part64.reserve(scan_part_size(n) + 1, 1.25);
+  uint64_t* total_dev = sc.part64.p + scan_part_size(n);
+  scan_rec<uint64_t>(in, out, n, s, sc.part64.p, total_dev);
+  uint64_t tot = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&tot, total_dev, sizeof(tot), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return tot;
+}
+
+void exclusive_scan_u64_async(const uint64_t* in, uint64_t* out, size_t n, cudaStream_t s,
+                              SortScratch& sc, uint64_t* total_dev) {
+  if (n == 0) return;
+  sc.part64.reserve(scan_part_size(n) + 1, 1.25);
+  scan_rec<uint64_t>(in, out, n, s, sc.part64.p, total_dev);
+}
+
+uint32_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s,
+                            SortScratch& sc) {
+  if (n == 0) return 0;
+  sc.part32.reserve(scan_part_size(n) + 1, 1.25);
+  uint32_t* total_dev = sc.part32.p + scan_part_size(n);
+  scan_rec<uint32_t>(in, out, n, s, sc.part32.p, total_dev);
+  uint32_t tot = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&tot, total_dev, sizeof(tot), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return tot;
+}
+
+void radix_sort_pairs(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, size_t n, int begin_bit,
+                      int end_bit, cudaStream_t s, SortScratch& sc) {
+  radix_sort_impl<uint32_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.valt32);
+}
+
+void radix_sort_pairs64(DevBuf<uint64_t>& keys, DevBuf<uint64_t>& vals, size_t n,
+                        int begin_bit, int end_bit, cudaStream_t s, SortScratch& sc) {
+  radix_sort_impl<uint64_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.valt64);
+}
+
+void iota_u32(uint32_t* v, size_t n, cudaStream_t s) {
+  k_iota<<<grid_for(n, 256), 256, 0, s>>>(v, n);
+  SHCI_LAUNCH_CHECK();
+}
+
+void gather_u64(const uint64_t* src, const uint32_t* idx, uint64_t* out, size_t n,
+                cudaStream_t s) {
+  k_gather_u64<<<grid_for(n, 256), 256, 0, s>>>(src, idx, out, n);
+  SHCI_LAUNCH_CHECK();
+}
+
+}  // namespace shci

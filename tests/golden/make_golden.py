@@ -1,0 +1,94 @@
+"""Regenerate the golden fixtures from the reference tree (run in a checkout that has it).
+
+Reads the reference's committed C-atom example (examples/C: FCIDUMP, config.json, result.json,
+the run log `out`) and its unit-test constants, and writes:
+  c_atom/FCIDUMP, c_atom/config.json  - the example's inputs, copied verbatim
+  c_atom_pins.json                    - numbers parsed from the example's log and result.json
+The Davidson Hilbert-matrix known answers (src/solver/davidson_test.cc:5-51) and the
+HalfDet unit-test cases (src/det/half_det_test.cc:30-46) are transcribed into hilbert_pins.json
+and halfdet_pins.json by reading those files as text.
+
+Usage: python tests/golden/make_golden.py [/path/to/reference]
+"""
+import json
+import os
+import re
+import shutil
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def parse_int(s):
+    return int(s.replace(",", ""))
+
+
+def main(ref):
+    ex = os.path.join(ref, "examples", "C")
+    os.makedirs(os.path.join(HERE, "c_atom"), exist_ok=True)
+    for f in ("FCIDUMP", "config.json"):
+        shutil.copyfile(os.path.join(ex, f), os.path.join(HERE, "c_atom", f))
+    out = open(os.path.join(ex, "out")).read().splitlines()
+    pins = {"source": "examples/C (out, result.json)"}
+    m = next(l for l in out if l.startswith("HF energy:"))
+    pins["energy_hf"] = float(m.split()[2])
+    pins["max_hci_queue_elem"] = float(
+        next(l for l in out if l.startswith("Max hci queue elem")).split()[4])
+    pins["n_hci_queue_entries"] = parse_int(
+        next(l for l in out if l.startswith("Number of entries in hci queue")).split()[-1])
+    pins["max_singles_queue_elem"] = float(
+        next(l for l in out if l.startswith("Max singles_queue elem")).split()[3])
+    pins["n_singles_queue_entries"] = parse_int(
+        next(l for l in out if l.startswith("Number of entries in singles_queue")).split()[-1])
+    # Per variational iteration: dets after selection, nnz (symmetric count), energy.
+    iters = []
+    cur = {}
+    for l in out:
+        m = re.match(r"Number of dets / new dets: ([\d,]+) / ([\d,]+)", l)
+        if m:
+            cur = {"n_dets": parse_int(m.group(1)), "n_new": parse_int(m.group(2))}
+        m = re.match(r"Number of nonzero elems: ([\d,]+)", l)
+        if m:
+            cur["nnz"] = parse_int(m.group(1))
+        m = re.match(r"Iteration (\d+) eps1= (\S+) ndets= ([\d,]+) energy= (\S+)", l)
+        if m:
+            cur.update(iteration=int(m.group(1)), eps1=float(m.group(2)),
+                       ndets=parse_int(m.group(3)), energy=float(m.group(4)))
+            iters.append(cur)
+            cur = {}
+    pins["iterations"] = iters
+    res = json.load(open(os.path.join(ex, "result.json")))
+    pins["energy_var"] = res["energy_var"]
+    pins["energy_total"] = {k: v for k, v in res["energy_total"].items() if k != "extrapolated"}
+    # Deterministic PT stage lines.
+    dtm = []
+    for i, l in enumerate(out):
+        m = re.match(r"PT dtm correction \(eps1= (\S+), eps_pt_dtm= (\S+)\): (\S+)", l)
+        if m:
+            nl = [x for x in out[max(0, i - 4):i] if x.startswith("Number of dtm pt dets")]
+            dtm.append({"eps_var": float(m.group(1)), "eps_pt_dtm": float(m.group(2)),
+                        "correction": float(m.group(3)),
+                        "n_pt_dets": parse_int(nl[-1].split()[-1]) if nl else None})
+    pins["pt_dtm"] = dtm
+    json.dump(pins, open(os.path.join(HERE, "c_atom_pins.json"), "w"), indent=1)
+
+    dt = open(os.path.join(ref, "src", "solver", "davidson_test.cc")).read()
+    vals = re.search(r"expected_eigenvalues\(\s*\{([^}]*)\}", dt).group(1)
+    vecs = re.search(r"expected_eigenvectors\(\s*\{\{([^}]*)\}", dt).group(1)
+    hil = {"source": "src/solver/davidson_test.cc", "n": 1000, "gamma": 10.0,
+           "eigenvalue0": float(vals.split(",")[0]),
+           "eigenvector0_head": [float(x) for x in vecs.split(",")],
+           "tol_value": 1e-6, "tol_vector": 1e-4, "davidson_tol": 1e-6}
+    json.dump(hil, open(os.path.join(HERE, "hilbert_pins.json"), "w"), indent=1)
+
+    hd = open(os.path.join(ref, "src", "det", "half_det_test.cc")).read()
+    assert "EXPECT_EQ(diff.right_only[0], 3)" in hd
+    halfdet = {"source": "src/det/half_det_test.cc:30-46",
+               "cases": [{"a": [0], "b": [1], "n_diffs": 1, "left0": 0, "right0": 1},
+                         {"a": [0, 1], "b": [1, 3], "n_diffs": 1, "left0": 0, "right0": 3}]}
+    json.dump(halfdet, open(os.path.join(HERE, "halfdet_pins.json"), "w"), indent=1)
+    print("wrote golden fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,210 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle and the reference's
+golden data.  Integer / index results must be bit-exact; FP64 matrix elements are compared
+bit for bit as well (same summation order); energies within the stated tolerances."""
+import numpy as np
+import pytest
+
+from conftest import C_ATOM
+
+pytestmark = pytest.mark.gpu
+
+SCHED_C = [2e-3, 1e-3, 5e-4, 2e-4, 1e-4]
+
+
+@pytest.fixture(scope="module")
+def shci():
+    import shci_gb300
+    return shci_gb300
+
+
+def new_ctx(shci, path, n_up, n_dn, pg="C1"):
+    c = shci.Context()
+    c.load_fcidump(path, n_up, n_dn, pg)
+    return c
+
+
+@pytest.fixture(scope="module")
+def c_oracle(oracle_mod):
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o.run_all_variations([5e-5], SCHED_C, 5e-5)
+    return o
+
+
+@pytest.mark.parametrize("which", ["c_atom", "w1"])
+def test_integrals_queues_hf_match_oracle(shci, oracle_mod, which, w1_fcidump):
+    path, nu, nd, pg = (C_ATOM, 4, 2, "d2h") if which == "c_atom" else (w1_fcidump, 5, 5, "C1")
+    o = oracle_mod.Oracle(path, nu, nd, pg)
+    c = new_ctx(shci, path, nu, nd, pg)
+    h1, g2, sym, order, ec = c.integrals()
+    oh1, og2, osym, oorder = o.integrals()
+    assert np.array_equal(h1, oh1) and np.array_equal(g2, og2)
+    assert np.array_equal(sym, osym) and np.array_equal(order, oorder)
+    up, dn, ehf = c.hf()
+    info = o.info()
+    assert (up, dn) == o.hf()
+    assert ehf == info["energy_hf"]
+    q = c.build_queues()
+    assert q["n_hci"] == info["n_hci"] and q["n_singles"] == info["n_singles"]
+    assert q["max_hci"] == info["max_hci"] and q["max_singles"] == info["max_singles"]
+
+
+def test_matrix_elements_bitexact(shci, c_oracle):
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    up, dn, _ = c_oracle.dets()
+    rng = np.random.default_rng(11)
+    ui, di, uj, dj = [], [], [], []
+    for i in rng.choice(len(up), 300, replace=False):
+        cu, cd, nx = c_oracle.find_connected((int(up[i]), int(dn[i])), 1e100, 1e-6)
+        k = rng.choice(len(cu), min(20, len(cu)), replace=False)
+        ui += [up[i]] * len(k) + [up[i]]
+        di += [dn[i]] * len(k) + [dn[i]]
+        uj += list(cu[k]) + [up[i]]
+        dj += list(cd[k]) + [dn[i]]
+    got = c.h_elems(ui, di, uj, dj)
+    want = np.array([c_oracle.h_elem((int(a), int(b)), (int(x), int(y)))
+                     for a, b, x, y in zip(ui, di, uj, dj)])
+    assert np.array_equal(got, want)
+
+
+@pytest.fixture(scope="module")
+def c_ham(shci, oracle_mod, c_oracle):
+    """GPU and oracle Hamiltonians of the 24,087-det C-atom wavefunction (eps_var 5e-5)."""
+    up, dn, coefs = c_oracle.dets()
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o.set_dets(up, dn, coefs)
+    onnz = o.update_hamiltonian()
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.set_dets(up, dn, coefs)
+    nnz, nnz_sym = c.update_hamiltonian(shci.PREC_FP64)
+    return c, o, onnz, nnz, nnz_sym, up, dn, coefs
+
+
+def test_hamiltonian_connections_bitexact(c_ham, c_atom_pins):
+    c, o, onnz, nnz, nnz_sym, up, dn, _ = c_ham
+    n = len(up)
+    assert nnz_sym == 4714387  # reference log, examples/C/out:243
+    assert onnz == nnz + n
+    rp, cols, vals, diag = c.hamiltonian(nnz)
+    orp, ocols, ovals = o.hamiltonian(onnz)
+    for i in range(n):
+        a, b = int(orp[i]), int(orp[i + 1])
+        oc, ov = ocols[a:b], ovals[a:b]
+        assert oc[0] == i and diag[i] == ov[0]
+        g0, g1 = int(rp[i]), int(rp[i + 1])
+        gc, gv = cols[g0:g1], vals[g0:g1]
+        so, sg = np.argsort(oc[1:], kind="stable"), np.argsort(gc, kind="stable")
+        assert np.array_equal(oc[1:][so], gc[sg]), i
+        assert np.array_equal(ov[1:][so], gv[sg]), i
+
+
+def test_spmv_matches_oracle(c_ham):
+    c, o, *_ = c_ham
+    x = np.random.default_rng(5).standard_normal(c.n_dets())
+    y, yo = c.hv(x), o.hv(x)
+    assert np.max(np.abs(y - yo)) <= 1e-12 * np.max(np.abs(yo))
+
+
+def test_davidson_matches_oracle(c_ham):
+    c, o, _, _, _, up, dn, coefs = c_ham
+    e_o, vec_o, conv_o, tr_o = o.davidson(coefs, 5e-5 / 500000)
+    c.set_coefs(coefs)
+    e, conv, tr = c.davidson(5e-5 / 500000)
+    assert conv == conv_o and len(tr) == len(tr_o)
+    assert np.max(np.abs(tr - tr_o)) < 1e-10
+    _, _, vec = c.dets()
+    assert abs(np.dot(vec, vec_o)) / np.linalg.norm(vec) / np.linalg.norm(vec_o) > 1 - 1e-10
+
+
+def test_hilbert_davidson_gpu(shci):
+    import json, os
+    from conftest import GOLDEN
+    pins = json.load(open(os.path.join(GOLDEN, "hilbert_pins.json")))
+    n = pins["n"]
+    rows, cols, vals = [0], [], []
+    diag = np.array([-1.0 / (2 * i + 1) for i in range(n)])
+    for i in range(n):
+        for j in range(i + 1, n):
+            cols.append(j)
+            vals.append(-1.0 / pins["gamma"] / (i + j + 1))
+        rows.append(len(cols))
+    init = np.zeros(n)
+    init[0] = 1.0
+    c = shci.Context()
+    e, vec, conv = c.davidson_csr(rows, cols, vals, diag, init, pins["davidson_tol"])
+    assert abs(e - pins["eigenvalue0"]) < pins["tol_value"]
+    assert np.allclose(vec[:5], pins["eigenvector0_head"], atol=pins["tol_vector"])
+
+
+def test_selection_matches_oracle(shci, oracle_mod):
+    """Two selection steps from the same state produce identical det lists (order included)
+    and identical eps_tried_prev memos."""
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    assert c.select(2e-3) == o.select(2e-3) == 480
+    up, dn, _ = c.dets()
+    oup, odn, _ = o.dets()
+    assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+    # same coefficients in both, then a second step
+    o.update_hamiltonian()
+    _, vec, _, _ = o.davidson(np.r_[1.0, np.full(len(oup) - 1, 1e-16)], 5e-5 / 50)
+    o.set_coefs(vec)
+    c.set_coefs(vec)
+    assert c.select(1e-3) == o.select(1e-3)
+    up, dn, _ = c.dets()
+    oup, odn, _ = o.dets()
+    assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+    assert np.array_equal(c.eps_tried()[: len(vec)], o.eps_tried()[: len(vec)])
+
+
+def test_variation_c_atom_matches_reference_log(shci, c_atom_pins):
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    e = c.run_variation([5e-5], SCHED_C, 5e-5)
+    nd, nz, en = c.var_trace()
+    ref = [it for it in c_atom_pins["iterations"] if it["eps1"] >= 5e-5]
+    assert list(nd) == [it["ndets"] for it in ref]
+    assert [int(z) for z, it in zip(nz, ref) if "nnz" in it] == [it["nnz"] for it in ref if "nnz" in it]
+    assert abs(e[0] - c_atom_pins["energy_var"]["5.00e-05"]) < 1e-8
+
+
+def test_variation_synthetic_matches_oracle(shci, oracle_mod, w1_fcidump):
+    o = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    eo = o.run_all_variations([2e-4, 1e-4], [], 5e-5)
+    c = new_ctx(shci, w1_fcidump, 5, 5)
+    e = c.run_variation([2e-4, 1e-4], [], 5e-5)
+    assert np.max(np.abs(e - eo)) < 1e-9
+    nd, nz, _ = c.var_trace()
+    ond, onz, _ = o.iterations()
+    assert np.array_equal(nd, ond) and np.array_equal(nz, onz)
+    up, dn, _ = c.dets()
+    oup, odn, _ = o.dets()
+    assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+
+
+def test_pt2_dtm_matches_oracle_and_reference(shci, oracle_mod, c_oracle, c_atom_pins):
+    up, dn, coefs = c_oracle.dets()
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    ev = c_oracle.energy_var
+    v, u, n = c.pt2_dtm(ev, 5e-6, 1)
+    vo, uo, no = c_oracle.pt_dtm(5e-6, 1)
+    pin = [p for p in c_atom_pins["pt_dtm"] if p["eps_var"] == 5e-5][0]
+    assert n == no == pin["n_pt_dets"]
+    assert abs(v - vo) < 1e-12
+    assert abs(v - pin["correction"]) < 1e-10
+    v3, u3, n3 = c.pt2_dtm(ev, 5e-6, 3)
+    assert n3 == n and abs(v3 - v) < 1e-12 and u3 == 0.0
+
+
+def test_mixed_precision_energy(shci, c_ham):
+    c, _, _, _, _, up, dn, coefs = c_ham
+    c.set_coefs(coefs)
+    c.update_hamiltonian(shci.PREC_FP64)
+    e64, _, _ = c.davidson(1e-10)
+    c.set_coefs(coefs)
+    c.update_hamiltonian(shci.PREC_MIXED)
+    e32, _, _ = c.davidson(1e-10)
+    ecorr = c.energy_fp64()
+    assert abs(e32 - e64) < 1e-6
+    assert abs(ecorr - e64) < 1e-8

@@ -1,0 +1,150 @@
+"""Pins the CPU oracle to the reference: its own det/hash/alias code (compiled from the
+reference sources where available), its unit-test constants and the committed C-atom run."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import C_ATOM, GOLDEN
+
+
+def test_halfdet_unit_cases(oracle_mod):
+    """src/det/half_det_test.cc:30-46."""
+    pins = json.load(open(os.path.join(GOLDEN, "halfdet_pins.json")))
+    L = oracle_mod.lib()
+    import ctypes
+    for case in pins["cases"]:
+        a = sum(1 << o for o in case["a"])
+        b = sum(1 << o for o in case["b"])
+        out = np.zeros(5, np.uint32)
+        perm = ctypes.c_int()
+        L.orc_diff(a, b, out, ctypes.byref(perm))
+        assert out[4] == case["n_diffs"]
+        assert out[0] == case["left0"] and out[2] == case["right0"]
+
+
+def _rand_half(rng, n, k):
+    return int(sum(1 << int(o) for o in rng.choice(n, k, replace=False)))
+
+
+def test_det_ops_match_reference_code(oracle_mod):
+    """diff / hash / rehash / ordering bit-exact against the reference's own half_det.cc and
+    util.cc (compiled from the reference tree; skipped where that tree is absent)."""
+    ref = oracle_mod.ref_pin()
+    if ref is None:
+        pytest.skip("reference sources not available to build the pin")
+    import ctypes
+    L = oracle_mod.lib()
+    rng = np.random.default_rng(7)
+    for _ in range(3000):
+        n = int(rng.integers(4, 65))
+        k = int(rng.integers(1, n))
+        a, b = _rand_half(rng, n, k), _rand_half(rng, n, k)
+        if rng.random() < 0.5:  # make close pairs common
+            occ = [o for o in range(n) if a >> o & 1]
+            emp = [o for o in range(n) if not a >> o & 1]
+            b = a
+            for _ in range(int(rng.integers(1, 4))):
+                if occ and emp:
+                    o = occ.pop(int(rng.integers(len(occ))))
+                    v = emp.pop(int(rng.integers(len(emp))))
+                    b = (b & ~(1 << o)) | (1 << v)
+        o1, o2 = np.zeros(5, np.uint32), np.zeros(5, np.uint32)
+        p1, p2 = ctypes.c_int(), ctypes.c_int()
+        L.orc_diff(a, b, o1, ctypes.byref(p1))
+        ref.ref_diff(a, b, o2, ctypes.byref(p2))
+        assert o1[4] == o2[4]
+        if o1[4] <= 2:
+            nd = o1[4]
+            assert list(o1[:nd]) == list(o2[:nd]) and list(o1[2:2 + nd]) == list(o2[2:2 + nd])
+            assert p1.value == p2.value
+        assert L.orc_det_hash(a, b) == ref.ref_det_hash(a, b)
+        h = int(rng.integers(0, 2**63))
+        assert L.orc_rehash(h) == ref.ref_rehash(h)
+        assert ref.ref_det_less(a, b, b, a) == int((a, b) < (b, a))
+
+
+def test_alias_table_reference(oracle_mod):
+    """Vose alias tables of src/util.cc:128-175 reproduce the distribution exactly."""
+    ref = oracle_mod.ref_pin()
+    if ref is None:
+        pytest.skip("reference sources not available to build the pin")
+    rng = np.random.default_rng(3)
+    p = rng.random(257)
+    p /= p.sum()
+    np_, al = np.zeros(257), np.zeros(257, np.uint64)
+    ref.ref_alias(p, 257, np_, al)
+    recon = np_ / 257
+    for i in range(257):
+        recon[al[i]] += (1 - np_[i]) / 257
+    assert np.allclose(recon, p, atol=1e-12)
+
+
+def test_hilbert_davidson(oracle_mod):
+    """src/solver/davidson_test.cc:5-51 known answers."""
+    pins = json.load(open(os.path.join(GOLDEN, "hilbert_pins.json")))
+    n = pins["n"]
+    rows, cols, vals = [0], [], []
+    for i in range(n):
+        for j in range(i, n):
+            cols.append(j)
+            vals.append(-1.0 / (2 * i + 1) if i == j else -1.0 / pins["gamma"] / (i + j + 1))
+        rows.append(len(cols))
+    init = np.zeros(n)
+    init[0] = 1.0
+    e, vec, conv = oracle_mod.davidson_csr(rows, cols, vals, init, pins["davidson_tol"])
+    assert abs(e - pins["eigenvalue0"]) < pins["tol_value"]
+    assert np.allclose(vec[:5], pins["eigenvector0_head"], atol=pins["tol_vector"])
+
+
+@pytest.fixture(scope="module")
+def c_atom_run(oracle_mod):
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    info = o.info()
+    e = o.run_all_variations([5e-5], [2e-3, 1e-3, 5e-4, 2e-4, 1e-4], 5e-5)
+    return o, info, e
+
+
+def test_c_atom_setup(c_atom_run, c_atom_pins):
+    o, info, _ = c_atom_run
+    assert abs(info["energy_hf"] - c_atom_pins["energy_hf"]) < 1e-10
+    assert info["n_hci"] == c_atom_pins["n_hci_queue_entries"]
+    assert info["n_singles"] == c_atom_pins["n_singles_queue_entries"]
+    assert abs(info["max_hci"] - c_atom_pins["max_hci_queue_elem"]) < 1e-10
+    assert o.hf() == (0xF, 0x3)
+
+
+def test_c_atom_variation_matches_reference_log(c_atom_run, c_atom_pins):
+    """Per-iteration det counts and symmetric nnz of the eps_var = 5e-5 stage (schedule
+    2e-3 ... 1e-4, then 5e-5 to convergence) equal the reference's log exactly."""
+    o, _, e = c_atom_run
+    nd, nz, en = o.iterations()
+    ref = [it for it in c_atom_pins["iterations"] if it["eps1"] >= 5e-5]
+    assert len(nd) == len(ref)
+    for k, it in enumerate(ref):
+        assert nd[k] == it["ndets"]
+        if "nnz" in it:
+            assert nz[k] == it["nnz"]
+        assert abs(en[k] - it["energy"]) < 6e-9  # log prints 8 decimals
+    assert abs(e[0] - c_atom_pins["energy_var"]["5.00e-05"]) < 1e-8
+
+
+def test_c_atom_pt_dtm(c_atom_run, c_atom_pins):
+    o, _, e = c_atom_run
+    v, u, n = o.pt_dtm(5e-6, 1)
+    pin = [p for p in c_atom_pins["pt_dtm"] if p["eps_var"] == 5e-5][0]
+    assert n == pin["n_pt_dets"]
+    assert abs(v - pin["correction"]) < 1e-10
+    assert u == 0.0
+
+
+def test_oracle_pt_batches_partition(oracle_mod, w1_fcidump):
+    """Hash batches partition the PT space: the batch sum equals the one-batch sum."""
+    o = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    o.run_all_variations([2e-4], [], 5e-5)
+    v1, _, n1 = o.pt_dtm(1e-5, 1)
+    v4, u4, n4 = o.pt_dtm(1e-5, 4)
+    assert n1 == n4
+    assert abs(v1 - v4) < 1e-12
+    assert u4 == 0.0
