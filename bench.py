@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the SHCI hot path on GB300: Hamiltonian build + Davidson.
+
+Workload (the largest configuration of the metric): synthetic FCIDUMP, n = 40 orbitals,
+10 alpha + 10 beta electrons, no symmetry; heat-bath schedule 1e-3, 5e-4, 2e-4, 1e-4, 5e-5
+(one iteration each, as the reference's eps_vars_schedule), then the first eps_var = 2e-5
+iteration: its selection gives the determinant list (~4.5M dets) the timed step works on.
+
+One step = Hamiltonian<S>::update (device det index + count pass + fill pass, mixed storage:
+FP32 value + FP32 residual) + one full Davidson::diagonalize call (the reference's maximum of
+9 H*v products, tol = 0 so every step does the same work, FP64 vectors and accumulation) +
+the FP64 Rayleigh-quotient correction of the Ritz vector.  value = device seconds per step
+(inputs resident in HBM); e2e = the same through the public API with the det list and start
+vector copied from pinned host memory each step and the energy read back.
+
+--impl reference times the CPU restatement of the reference's algorithm (oracle/) on a
+strided sample of the same step's rows with every host thread, scaled to the full step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H-build+Davidson s and PT2 s at ~2e7 dets, mixed vs FP64 on GPU, |dE|<1e-6 Ha"
+WORKLOAD = 3
+SCHEDULE = [1e-3, 5e-4, 2e-4, 1e-4, 5e-5]
+EPS_VAR = 2e-5
+TARGET_ERROR = 5e-5
+DAVIDSON_MATVECS = 9
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 7:
+                self.samples.append(f)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def make_workload(data_dir):
+    from shci_gb300 import synthetic
+    return synthetic.workload_fcidump(WORKLOAD, data_dir), synthetic.WORKLOADS[WORKLOAD]
+
+
+def gpu_setup(ctx, fcidump, w):
+    """Schedule iterations on the device, then the first eps_var selection: returns the det
+    list and the start vector of the timed step (host arrays)."""
+    import shci_gb300 as S
+    ctx.load_fcidump(fcidump, w["n_up"], w["n_dn"])
+    ctx.build_queues()
+    for eps in SCHEDULE:
+        ctx.select(eps)
+        ctx.update_hamiltonian(S.PREC_MIXED)
+        ctx.davidson(TARGET_ERROR / 50)
+    ctx.select(EPS_VAR)
+    return ctx.dets()
+
+
+def cpu_sample(fcidump, w, up, dn, target_rows=2000):
+    """Oracle (CPU restatement) timing of one step on a strided row sample, scaled."""
+    from oracle.oracle import Oracle
+    o = Oracle(fcidump, w["n_up"], w["n_dn"])
+    o.set_dets(up, dn)
+    n = len(up)
+    stride = max(1, n // target_rows)
+    r = o.hbuild_sample(stride, 0)
+    scale = n / max(1, r["rows"])
+    step = r["index_s"] + scale * (r["rows_s"] + DAVIDSON_MATVECS * r["spmv_s"])
+    return step, {"value": step, "unit": "s", "cores": Oracle.threads(), "kind": "port",
+                  "sample": "rows i = 0 mod %d (%d of %d rows, %d upper nnz) of the step's "
+                            "Hamiltonian; full det index built; H-build and %d H*v scaled by %.1f"
+                            % (stride, r["rows"], n, r["nnz"], DAVIDSON_MATVECS, scale),
+                  "index_s": r["index_s"], "rows_s": r["rows_s"], "spmv_s": r["spmv_s"]}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    orc.build(ref=False)
+    fcidump, w = make_workload(args.data)
+    o = orc.Oracle(fcidump, w["n_up"], w["n_dn"])
+    t0 = time.time()
+    for eps in SCHEDULE:
+        o.run_variation_step(eps, False, TARGET_ERROR)
+    o.select(EPS_VAR)
+    up, dn, _ = o.dets()
+    setup_s = time.time() - t0
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        v, info = cpu_sample(fcidump, w, up, dn)
+        if k >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    info["value"] = value
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": workload_name(len(up)), "n_dets": len(up)},
+        "cpu_baseline": info, "setup_s": setup_s,
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def workload_name(n):
+    return ("synthetic n=40 10a10b C1, schedule 1e-3..5e-5 then first eps_var=2e-5 iteration "
+            "(%d dets): H-build + Davidson (9 H*v)" % n)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import shci_gb300 as S
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    fcidump, w = make_workload(args.data)
+    ctx = S.Context(local)
+    t0 = time.time()
+    up, dn, c0 = gpu_setup(ctx, fcidump, w)
+    setup_s = time.time() - t0
+    n = len(up)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    c0_dev = torch.from_numpy(c0).to(f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step(prec):
+        ctx.set_coefs_dev(c0_dev.data_ptr(), n)
+        ctx.update_hamiltonian(prec)
+        e, conv, tr = ctx.davidson(0.0)
+        return ctx.energy_fp64(), e
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step(S.PREC_MIXED)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.profile(True)
+    l0 = ctx.launches()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            e_mixed, e_dav = step(S.PREC_MIXED)
+        ev1.record(stream)
+        barrier()
+    launches = ctx.launches() - l0
+    prof = ctx.profile_get()
+    ctx.profile(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    stats = ctx.hamiltonian_stats()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # all-FP64 form of the same step
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step(S.PREC_FP64)
+    barrier()
+    ev2.record(stream)
+    e_fp64, _ = step(S.PREC_FP64)
+    ev3.record(stream)
+    barrier()
+    ms_fp64 = ev2.elapsed_time(ev3)
+
+    # end to end through the public API with pinned host buffers
+    pin_up = torch.from_numpy(up).pin_memory()
+    pin_dn = torch.from_numpy(dn).pin_memory()
+    pin_c = torch.from_numpy(c0).pin_memory()
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        barrier()
+        ta = time.perf_counter()
+        ctx.set_dets(pin_up.numpy(), pin_dn.numpy(), pin_c.numpy())
+        ctx.update_hamiltonian(S.PREC_MIXED)
+        ctx.davidson(0.0)
+        e_e2e = ctx.energy_fp64()
+        tb = time.perf_counter()
+        if k >= args.warmup:
+            e2e_ms.append((tb - ta) * 1e3)
+    e2e = statistics.median(e2e_ms)
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (per-launch averages over the timed region)
+    hbm, peak_kind = peaks()
+    per = {k: (v[0] / max(1, v[1]), v[1]) for k, v in prof.items()}
+    dom = max(prof, key=lambda k: prof[k][0])
+    nnz, cand = stats["nnz"], stats["candidates"]
+    # algorithmic bytes per launch (per unit = one stored element / one det row)
+    alg = {
+        "hbuild_count": 12.0 * cand + 16 * n + 4 * n + 8 * n,
+        "hbuild_fill": 12.0 * cand + 16 * n + 8 * (n + 1) + 12.0 * nnz,
+        "spmv": 8.0 * nnz + 8 * (n + 1) + 8 * n + 16 * n + 8 * n,
+        "det_index": 0.0,
+    }
+    kernels = {}
+    for k, (ms_l, cnt) in per.items():
+        b = alg.get(k)
+        g = (b / (ms_l * 1e-3) / 1e9) if b else None
+        kernels[k] = {"ms_per_launch": ms_l, "launches": cnt,
+                      "gbs": g, "frac": (g / hbm) if g else None}
+    dk = kernels[dom]
+    roof = {"kernel": dom, "bound": "hbm", "achieved": dk["gbs"], "peak": hbm, "unit": "GB/s",
+            "frac": dk["frac"], "traffic": None, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": alg.get(dom)}
+    cpu = None
+    if not args.no_cpu_baseline:
+        _, cpu = cpu_sample(fcidump, w, up, dn)
+    line = {
+        "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "storage": "f32 value + f32 residual",
+        "data": "synthetic",
+        "config": {"workload": workload_name(n), "n_dets": n, "nnz_upper": nnz,
+                   "nnz_sym": 2 * (nnz + n) - n, "l2": "inputs larger than L2 (H store %.0f GB)"
+                   % (12 * nnz / 1e9), "setup_s": setup_s},
+        "roofline": roof, "kernels": kernels, "cpu_baseline": cpu,
+        "e2e": {"value": e2e / 1e3, "unit": "s", "h2d_bytes_per_step": 24 * n,
+                "d2h_bytes_per_step": 8},
+        "gpu_launches": launches // args.steps,
+        "clocks": clk.summary(),
+        "fp64": {"ms_per_step": ms_fp64, "energy": e_fp64},
+        "energy_mixed_fp64corrected": e_mixed, "energy_davidson_mixed": e_dav,
+        "dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
+        "speedup_mixed_vs_fp64": ms_fp64 / ms,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--data", default=os.environ.get("SHCI_BENCH_DATA", "/tmp/shci_bench_data"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

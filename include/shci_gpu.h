@@ -93,6 +93,8 @@ shci_status shci_set_dets(shci_ctx* ctx, const uint64_t* up, const uint64_t* dn,
 shci_status shci_get_n_dets(shci_ctx* ctx, size_t* n);
 shci_status shci_get_dets(shci_ctx* ctx, uint64_t* up, uint64_t* dn, double* coefs, size_t cap);
 shci_status shci_set_coefs(shci_ctx* ctx, const double* coefs, size_t n);
+/* Same from a device buffer (no host round trip). */
+shci_status shci_set_coefs_dev(shci_ctx* ctx, const double* coefs_dev, size_t n);
 
 /* ---- matrix elements (BaseSystem::get_hamiltonian_elem, base_system.h:94-95) --------- */
 
@@ -108,6 +110,10 @@ shci_status shci_hamiltonian_elems(shci_ctx* ctx, const uint64_t* up_i, const ui
  * nnz_out[0] = stored strict-upper elements, nnz_out[1] = the reference's symmetric count
  * (2 * (strict + n) - n, sparse_matrix.cc:13-26).  Elements with |H| < 1e-12 are dropped. */
 shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_out);
+
+/* Sizes of the last build: stats[0..5] = {n dets, strict-upper nnz, unique alpha strings,
+ * unique beta strings, alpha-single pairs, (row, candidate) pairs scanned}. */
+shci_status shci_hamiltonian_stats(shci_ctx* ctx, uint64_t* stats);
 
 /* Copy the Hamiltonian to the host: row_ptr[n+1] (strict upper), cols[nnz], vals[nnz]
  * (as FP64), diag[n].  Rows list their columns in the device traversal order. */
@@ -165,6 +171,14 @@ shci_status shci_get_var_trace(shci_ctx* ctx, uint64_t* n_dets, uint64_t* nnz, d
 
 /* Number of kernel launches issued by this context so far (for launch accounting). */
 shci_status shci_get_launch_count(shci_ctx* ctx, uint64_t* n);
+
+/* Per-stage device timing with CUDA events on the context stream (replaces the reference's
+ * barriered Timer sections, src/timer.cc:25-63).  enable = 1 starts (and clears) the
+ * record, 0 stops it.  shci_profile_get returns, for up to cap stages, the stage name
+ * (NUL-terminated, 32 bytes each in names[]), total milliseconds and launch count. */
+shci_status shci_profile(shci_ctx* ctx, int enable);
+shci_status shci_profile_get(shci_ctx* ctx, char* names, double* total_ms, uint64_t* count,
+                             size_t cap, size_t* n);
 
 /* ---- PT2 (Solver<S>::get_energy_pt_dtm, solver.h:636-764) ---------------------------- */
 

@@ -71,6 +71,9 @@ def lib():
             "orc_energy_var": (d, [vp]),
             "orc_set_energy_var": (None, [vp, d]),
             "orc_pt_dtm": (None, [vp, d, sz, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(sz)]),
+            "orc_run_variation_step": (d, [vp, d, i, d]),
+            "orc_hbuild_sample": (None, [vp, sz, sz, _f64p]),
+            "orc_threads": (i, []),
             "orc_rdm1": (None, [vp, _f64p]),
             "orc_rdm2": (None, [vp, _f64p]),
         }
@@ -234,6 +237,19 @@ class Oracle:
         self.L.orc_run_all_variations(self.h, ev, len(ev), sc, len(schedule), target_error,
                                       int(second_rejection), out)
         return out
+
+    def run_variation_step(self, eps_var, until_converged, target_error=5e-5):
+        return self.L.orc_run_variation_step(self.h, eps_var, int(until_converged), target_error)
+
+    def hbuild_sample(self, stride, offset=0):
+        out = np.zeros(5)
+        self.L.orc_hbuild_sample(self.h, stride, offset, out)
+        return dict(index_s=out[0], rows_s=out[1], spmv_s=out[2], nnz=int(out[3]),
+                    rows=int(out[4]))
+
+    @staticmethod
+    def threads():
+        return lib().orc_threads()
 
     def iterations(self):
         n = self.L.orc_n_iterations(self.h)

@@ -1727,6 +1727,112 @@ void orc_run_all_variations(void* h, const double* eps_vars, size_t n_eps, const
   std::copy(e.begin(), e.end(), energies);
 }
 
+// One run_variation call (solver.h:413-539); returns the energy.
+double orc_run_variation_step(void* h, double eps_var, int until_converged, double target_error) {
+  auto& s = S(h);
+  s.target_error = target_error;
+  if (s.var_dets.size() != s.sys.dets.size()) {
+    s.var_dets.clear();
+    for (const auto& d : s.sys.dets) s.var_dets.insert(d);
+  }
+  s.run_variation(eps_var, until_converged != 0);
+  return s.sys.energy_var;
+}
+
+// Timing sample of the Hamiltonian build and H*v on the current dets, for a CPU baseline:
+// the full index (update_abdet / abm1 / absingles, hamiltonian.h:157-413) is built, then only
+// rows i = offset (mod stride) are computed (update_matrix, :415-598) and multiplied
+// (sparse_matrix.cc:28-56).  out[0..4] = {index seconds, row seconds, spmv seconds for the
+// sampled rows, sampled upper-triangle nnz (incl. diagonal), sampled rows}.
+void orc_hbuild_sample(void* h, size_t stride, size_t offset, double* out) {
+  auto& s = S(h);
+  auto& H = s.ham;
+  H.clear();
+  const auto t0 = omp_get_wtime();
+  H.n_dets_prev = 0;
+  H.n_dets = s.sys.dets.size();
+  H.sort_by_det_id = false;
+  H.update_abdet(s.sys);
+  H.update_abm1(s.sys);
+  H.update_absingles(s.sys);
+  H.abm1.clear();
+  const auto t1 = omp_get_wtime();
+  // rows of the sample, computed exactly as update_matrix computes a new row
+  const size_t n = H.n_dets;
+  std::vector<size_t> rows;
+  for (size_t i = offset; i < n; i += stride) rows.push_back(i);
+  SparseMatrix m;
+  m.set_dim(n);
+  const auto& dets = s.sys.dets;
+  const auto& sys = s.sys;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (size_t r = 0; r < rows.size(); r++) {
+    const size_t det_id = rows[r];
+    const Det& det = dets[det_id];
+    auto& row = m.rows[det_id];
+    row.emplace_back(static_cast<uint32_t>(det_id), sys.hamiltonian_elem(det, det, 0));
+    const size_t start_id = det_id + 1;
+    const size_t bid = H.beta_to_id.at(det.dn);
+    for (size_t j : H.b2d[bid]) {
+      if (j < start_id) continue;
+      const double v = sys.hamiltonian_elem(det, dets[j], -1);
+      if (std::abs(v) >= EPS) row.emplace_back(static_cast<uint32_t>(j), v);
+    }
+    const size_t aid = H.alpha_to_id.at(det.up);
+    for (size_t j : H.a2d[aid]) {
+      if (j < start_id) continue;
+      const double v = sys.hamiltonian_elem(det, dets[j], -1);
+      if (std::abs(v) >= EPS) row.emplace_back(static_cast<uint32_t>(j), v);
+    }
+    const auto& bs_list = H.beta_singles[bid];
+    for (size_t as : H.alpha_singles[aid]) {
+      const auto& rel_b = H.a2b[as];
+      const auto& rel_d = H.a2d[as];
+      size_t ptr = 0;
+      for (size_t bsd : bs_list) {
+        while (ptr < rel_b.size() && rel_b[ptr] < bsd) ptr++;
+        if (ptr == rel_b.size()) break;
+        if (rel_b[ptr] == bsd) {
+          const size_t j = rel_d[ptr++];
+          if (j < start_id) continue;
+          const double v = sys.hamiltonian_elem(det, dets[j], 2);
+          if (std::abs(v) >= EPS) row.emplace_back(static_cast<uint32_t>(j), v);
+        }
+      }
+    }
+  }
+  const auto t2 = omp_get_wtime();
+  size_t nnz = 0;
+  for (size_t i : rows) nnz += m.rows[i].size();
+  std::vector<double> x(n, 1.0 / std::sqrt((double)n));
+  const int nt = omp_get_max_threads();
+  std::vector<std::vector<double>> part(nt, std::vector<double>(n, 0.0));
+  const auto t3 = omp_get_wtime();
+#pragma omp parallel
+  {
+    auto& y = part[omp_get_thread_num()];
+#pragma omp for schedule(dynamic, 64)
+    for (size_t r = 0; r < rows.size(); r++) {
+      const size_t i = rows[r];
+      double acc = 0.0;
+      for (const auto& e : m.rows[i]) {
+        acc += e.second * x[e.first];
+        if (i != e.first) y[e.first] += e.second * x[i];
+      }
+      y[i] += acc;
+    }
+  }
+  const auto t4 = omp_get_wtime();
+  H.clear();
+  out[0] = t1 - t0;
+  out[1] = t2 - t1;
+  out[2] = t4 - t3;
+  out[3] = static_cast<double>(nnz);
+  out[4] = static_cast<double>(rows.size());
+}
+
+int orc_threads() { return omp_get_max_threads(); }
+
 size_t orc_n_iterations(void* h) { return S(h).iter_ndets.size(); }
 void orc_iterations(void* h, uint64_t* ndets, uint64_t* nnz, double* energy) {
   auto& s = S(h);

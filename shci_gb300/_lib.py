@@ -55,6 +55,7 @@ def load():
         "shci_get_n_dets": [vp, P(sz)],
         "shci_get_dets": [vp, _u64p, _u64p, vp, sz],
         "shci_set_coefs": [vp, _f64p, sz],
+        "shci_set_coefs_dev": [vp, vp, sz],
         "shci_hamiltonian_elems": [vp, _u64p, _u64p, _u64p, _u64p, sz, _f64p],
         "shci_update_hamiltonian": [vp, i, P(sz)],
         "shci_get_hamiltonian": [vp, _u64p, _u32p, _f64p, _f64p],
@@ -69,6 +70,9 @@ def load():
         "shci_get_var_trace": [vp, _u64p, _u64p, _f64p, sz, P(sz)],
         "shci_get_launch_count": [vp, P(u64)],
         "shci_pt2_dtm": [vp, d, d, sz, P(d), P(d), P(sz)],
+        "shci_hamiltonian_stats": [vp, _u64p],
+        "shci_profile": [vp, i],
+        "shci_profile_get": [vp, vp, _f64p, _u64p, sz, P(sz)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -193,6 +197,9 @@ class Context:
         c = np.ascontiguousarray(c, np.float64)
         self._ck(self.L.shci_set_coefs(self.h, c, len(c)))
 
+    def set_coefs_dev(self, ptr, n):
+        self._ck(self.L.shci_set_coefs_dev(self.h, ptr, n))
+
     def h_elems(self, ui, di, uj, dj):
         ui, di, uj, dj = (np.ascontiguousarray(x, np.uint64) for x in (ui, di, uj, dj))
         out = np.zeros(len(ui))
@@ -204,6 +211,12 @@ class Context:
         nnz = (ctypes.c_size_t * 2)()
         self._ck(self.L.shci_update_hamiltonian(self.h, precision, nnz))
         return nnz[0], nnz[1]
+
+    def hamiltonian_stats(self):
+        s = np.zeros(6, np.uint64)
+        self._ck(self.L.shci_hamiltonian_stats(self.h, s))
+        return dict(n=int(s[0]), nnz=int(s[1]), n_alpha=int(s[2]), n_beta=int(s[3]),
+                    alpha_singles=int(s[4]), candidates=int(s[5]))
 
     def hamiltonian(self, nnz):
         n = self.n_dets()
@@ -293,3 +306,21 @@ class Context:
 
     def stream(self):
         return self.L.shci_stream(self.h)
+
+    def profile(self, enable=True):
+        self._ck(self.L.shci_profile(self.h, int(enable)))
+
+    def profile_get(self):
+        """{stage: (total_ms, launches)} recorded since profiling was enabled."""
+        cap = 64
+        names = ctypes.create_string_buffer(32 * cap)
+        ms = np.zeros(cap)
+        cnt = np.zeros(cap, np.uint64)
+        n = ctypes.c_size_t()
+        self._ck(self.L.shci_profile_get(self.h, ctypes.cast(names, ctypes.c_void_p), ms, cnt,
+                                         cap, ctypes.byref(n)))
+        out = {}
+        for k in range(min(n.value, cap)):
+            nm = names.raw[32 * k:32 * k + 32].split(b"\0")[0].decode()
+            out[nm] = (float(ms[k]), int(cnt[k]))
+        return out

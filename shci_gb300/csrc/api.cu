@@ -224,17 +224,37 @@ shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
           __builtin_popcountll(dn[i]) != (int)c->I.n_dn)
         throw ArgError("det " + std::to_string(i) + " has the wrong electron count or orbitals");
     }
+    // device copies straight from the caller's buffers (pinned buffers give async DMA)
+    cudaStream_t s = c->stream;
+    c->d_up.resize(n, 1.1);
+    c->d_dn.resize(n, 1.1);
+    c->d_coef.resize(n, 1.1);
+    SHCI_CUDA(cudaMemcpyAsync(c->d_up.p, up, n * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(c->d_dn.p, dn, n * 8, cudaMemcpyHostToDevice, s));
     c->up.assign(up, up + n);
     c->dn.assign(dn, dn + n);
-    if (coefs) c->coefs.assign(coefs, coefs + n);
-    else {
+    if (coefs) {
+      SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, coefs, n * 8, cudaMemcpyHostToDevice, s));
+      c->coefs.assign(coefs, coefs + n);
+    } else {
       c->coefs.assign(n, 1e-16);
       c->coefs[0] = 1.0;
+      SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, c->coefs.data(), n * 8, cudaMemcpyHostToDevice, s));
     }
-    c->dets_dirty = true;
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    c->dets_dirty = false;
     c->eps_tried.clear();
     c->H.valid = false;
+  });
+}
+
+shci_status shci_set_coefs_dev(shci_ctx* c, const double* coefs_dev, size_t n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (n != c->up.size() || !coefs_dev) throw ArgError("coefficient count != det count");
     sync_dets(c);
+    SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, coefs_dev, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
   });
 }
 
@@ -292,6 +312,22 @@ shci_status shci_update_hamiltonian(shci_ctx* c, int precision, size_t* nnz_out)
       nnz_out[0] = nnz;
       nnz_out[1] = 2 * (nnz + c->up.size()) - c->up.size();
     }
+  });
+}
+
+shci_status shci_hamiltonian_stats(shci_ctx* c, uint64_t* stats) {
+  if (!c || !stats) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!c->H.valid) throw ArgError("no Hamiltonian built");
+    uint32_t n_as = 0;
+    if (c->idx.n_alpha)
+      SHCI_CUDA(cudaMemcpy(&n_as, c->idx.as_off.p + c->idx.n_alpha, 4, cudaMemcpyDeviceToHost));
+    stats[0] = c->H.n;
+    stats[1] = c->H.nnz;
+    stats[2] = c->idx.n_alpha;
+    stats[3] = c->idx.n_beta;
+    stats[4] = n_as;
+    stats[5] = c->H.candidates;
   });
 }
 
@@ -439,6 +475,37 @@ shci_status shci_get_launch_count(shci_ctx* c, uint64_t* n) {
   if (!c || !n) return SHCI_ERR_ARG;
   *n = c->launches;
   return SHCI_OK;
+}
+
+shci_status shci_profile(shci_ctx* c, int enable) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    c->prof.reset();
+    c->prof.on = enable != 0;
+  });
+}
+
+shci_status shci_profile_get(shci_ctx* c, char* names, double* total_ms, uint64_t* count,
+                             size_t cap, size_t* n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    c->prof.flush();
+    size_t k = 0;
+    for (const auto& kv : c->prof.acc) {
+      if (k < cap) {
+        if (names) {
+          std::memset(names + 32 * k, 0, 32);
+          std::strncpy(names + 32 * k, kv.first.c_str(), 31);
+        }
+        if (total_ms) total_ms[k] = kv.second.first;
+        if (count) count[k] = kv.second.second;
+      }
+      k++;
+    }
+    if (n) *n = k;
+  });
 }
 
 shci_status shci_get_var_trace(shci_ctx* c, uint64_t* n_dets, uint64_t* nnz, double* energy,

@@ -10,6 +10,7 @@
 #include "common.cuh"
 #include "devbuf.h"
 #include "host_system.h"
+#include "prof.h"
 #include "solver.h"
 #include "sort.cuh"
 
@@ -32,6 +33,7 @@ struct DetIndex {
 struct DevHamiltonian {
   size_t n = 0;
   size_t nnz = 0;
+  size_t candidates = 0;  // (row, candidate) pairs scanned by the last build
   int precision = SHCI_PREC_FP64;
   DevBuf<uint64_t> row_ptr;   // [n+1]
   DevBuf<uint32_t> col;       // [nnz]
@@ -106,4 +108,5 @@ struct shci_ctx {
 
   // counters for the bench: kernels launched by this context
   size_t launches = 0;
+  shci::Profiler prof;
 };

@@ -290,6 +290,7 @@ DavidsonOut davidson(shci_ctx* c, double tol) {
   SHCI_CUDA(cudaStreamSynchronize(s));
   out.eval = lambda;
   out.converged = converged;
+  c->prof.flush();
   return out;
 }
 

@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(kWarps * 32)
       }
     }
     // (c) alpha single x beta single: flatten (alpha single, group member) pairs over lanes
+    uint64_t n_mixed = 0;
     {
       const uint32_t s0 = ix.as_off[a], s1 = ix.as_off[a + 1];
       for (uint32_t c0 = s0; c0 < s1; c0 += 32) {
@@ -191,6 +192,7 @@ __global__ void __launch_bounds__(kWarps * 32)
           if (lane >= (unsigned)o) inc += t;
         }
         const uint32_t total = __shfl_sync(kFull, inc, 31);
+        n_mixed += total;
         for (uint32_t t0 = 0; t0 < total; t0 += 32) {
           const uint32_t t = t0 + lane;
           bool keep = false;
@@ -223,7 +225,13 @@ __global__ void __launch_bounds__(kWarps * 32)
         }
       }
     }
-    if (MODE == 0 && lane == 0) row_cnt[i] = cnt;
+    if (MODE == 0 && lane == 0) {
+      row_cnt[i] = cnt;
+      // candidates scanned by this row: both groups plus the alpha-single groups
+      const uint64_t nc = (ix.b_start[b + 1] - ix.b_start[b]) + (ix.a_start[a + 1] - ix.a_start[a]) +
+                          n_mixed;
+      atomicAdd(reinterpret_cast<unsigned long long*>(work + 2), (unsigned long long)nc);
+    }
   }
 }
 
@@ -233,6 +241,7 @@ void build_index(shci_ctx* c) {
   auto& ix = c->idx;
   const size_t n = c->up.size();
   cudaStream_t s = c->stream;
+  ProfScope ps(c->prof, s, "det_index");
   const int nb = c->I.n;
   ix.n = n;
   c->k0.resize(n, 1.25);
@@ -304,46 +313,58 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.row_ptr.resize(n + 1, 1.25);
   H.row_cnt.resize(n + 1, 1.25);
   H.diag.resize(n, 1.25);
-  c->err_word.resize(2);
+  // err_word layout: [0] row work counter, [1] unused, [2..3] candidate counter (u64)
+  c->err_word.resize(4);
   IndexView v{ix.det_aid.p, ix.det_bid.p, ix.a_start.p, ix.b_start.p, ix.am_idx.p, ix.bm_idx.p,
               ix.as_off.p,  ix.as_list.p, ix.am_dn.p,   ix.bm_up.p,   ix.ua.p};
   int dev_sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
-  SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
-  k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                           H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                           nullptr, H.diag.p, work);
-  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaMemsetAsync(work, 0, 4 * sizeof(unsigned), s));
+  {
+    ProfScope ps(c->prof, s, "hbuild_count");
+    k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                             H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
+                                             nullptr, H.diag.p, work);
+    SHCI_LAUNCH_CHECK();
+  }
   // row_ptr = exclusive scan of counts (counts widened to 64 bit)
   widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
   const uint64_t nnz = exclusive_scan_u64(H.row_ptr.p, H.row_ptr.p, n, s, c->sort);
   SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p + n, &nnz, 8, cudaMemcpyHostToDevice, s));
+  unsigned long long cand = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&cand, work + 2, 8, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
   H.nnz = nnz;
+  H.candidates = cand;
   const size_t cap = nnz ? nnz : 1;
   H.col.resize(cap, 1.1);
   if (precision == SHCI_PREC_FP64) {
-    H.val64.resize(cap, 1.1);
     H.val32.release();
     H.res32.release();
+    H.val64.resize(cap, 1.1);
   } else {
+    H.val64.release();
     H.val32.resize(cap, 1.1);
     H.res32.resize(cap, 1.1);
-    H.val64.release();
   }
   SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
-  if (precision == SHCI_PREC_FP64) {
-    k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                             nullptr, H.row_ptr.p, H.col.p, H.val64.p, nullptr,
-                                             nullptr, nullptr, work);
-  } else {
-    k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                             nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
-                                             H.res32.p, nullptr, work);
+  {
+    ProfScope ps(c->prof, s, "hbuild_fill");
+    if (precision == SHCI_PREC_FP64) {
+      k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                               nullptr, H.row_ptr.p, H.col.p, H.val64.p,
+                                               nullptr, nullptr, nullptr, work);
+    } else {
+      k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                               nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
+                                               H.res32.p, nullptr, work);
+    }
+    SHCI_LAUNCH_CHECK();
   }
-  SHCI_LAUNCH_CHECK();
   SHCI_CUDA(cudaStreamSynchronize(s));
+  c->prof.flush();
   H.valid = true;
   c->launches += 5;
   return nnz;

@@ -217,9 +217,12 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
         cu.resize(tot, 1.25);
         cd.resize(tot, 1.25);
         cv.resize(tot, 1.25);
-        k_pt_emit<<<grid, kPtWarps * 32, 0, s>>>(P, eps_pt, n_batches, batch, k0, k1, d_off.p,
-                                                 cu.p, cd.p, cv.p);
-        SHCI_LAUNCH_CHECK();
+        {
+          ProfScope ps(c->prof, s, "pt2_emit");
+          k_pt_emit<<<grid, kPtWarps * 32, 0, s>>>(P, eps_pt, n_batches, batch, k0, k1, d_off.p,
+                                                   cu.p, cd.p, cv.p);
+          SHCI_LAUNCH_CHECK();
+        }
         c->launches += 1;
         compact_valid(c, cu.p, cd.p, cv.p, tot, bu, bd, &bv, &bn);
         // keep the batch buffer bounded: reduce by key when it grows large
@@ -230,12 +233,18 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
       }
       k0 = k1;
     }
-    bn = sort_unique_pairs(c, bu, bd, bn, &bv);
+    {
+      ProfScope ps(c->prof, s, "pt2_reduce");
+      bn = sort_unique_pairs(c, bu, bd, bn, &bv);
+    }
     bu.n = bd.n = bv.n = bn;
     double bs = 0.0, bsq = 0.0;
     if (bn) {
-      k_pt_contrib<<<cgrid, 256, 0, s>>>(c->dI, bu.p, bd.p, bv.p, bn, energy_var, partial.p);
-      SHCI_LAUNCH_CHECK();
+      {
+        ProfScope ps(c->prof, s, "pt2_contrib");
+        k_pt_contrib<<<cgrid, 256, 0, s>>>(c->dI, bu.p, bd.p, bv.p, bn, energy_var, partial.p);
+        SHCI_LAUNCH_CHECK();
+      }
       std::vector<double> hp(2 * cgrid);
       SHCI_CUDA(cudaMemcpyAsync(hp.data(), partial.p, hp.size() * 8, cudaMemcpyDeviceToHost, s));
       SHCI_CUDA(cudaStreamSynchronize(s));
@@ -259,6 +268,7 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
     }
   }
   out.n_pt_dets = n_sum;
+  c->prof.flush();
   return out;
 }
 

@@ -374,8 +374,11 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
           SHCI_CUDA(cudaMemcpyAsync(d_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
           cu.resize(tot, 1.25);
           cd.resize(tot, 1.25);
-          k_sel_emit<<<grid, kSelWarps * 32, 0, s>>>(P, k0, k1, d_off.p, epsm.p + k0, cu.p, cd.p);
-          SHCI_LAUNCH_CHECK();
+          {
+            ProfScope ps(c->prof, s, "select_emit");
+            k_sel_emit<<<grid, kSelWarps * 32, 0, s>>>(P, k0, k1, d_off.p, epsm.p + k0, cu.p, cd.p);
+            SHCI_LAUNCH_CHECK();
+          }
           // compact valid candidates, then sort + unique
           const size_t before = pass_n;
           compact_valid(c, cu.p, cd.p, nullptr, tot, pass_up, pass_dn, nullptr, &pass_n);
@@ -416,6 +419,7 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
   SHCI_CUDA(cudaMemcpyAsync(c->eps_tried.data(), d_eps.p, n_dets * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->eps_tried.resize(c->up.size(), 1.0e100);
+  c->prof.flush();
   return n_new_total;
 }
 

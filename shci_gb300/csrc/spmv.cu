@@ -47,6 +47,7 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   if (!H.valid) throw ArgError("no Hamiltonian built");
   cudaStream_t s = c->stream;
   const uint32_t n = static_cast<uint32_t>(H.n);
+  ProfScope ps(c->prof, s, "spmv");
   SHCI_CUDA(cudaMemsetAsync(y, 0, H.n * sizeof(double), s));
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
