@@ -29,9 +29,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "H-build+Davidson s and PT2 s at ~2e7 dets, mixed vs FP64 on GPU, |dE|<1e-6 Ha"
+# workload -> (eps_vars_schedule iterations, eps_var of the timed iteration)
+WORKLOADS = {
+    3: ([1e-3, 5e-4, 2e-4, 1e-4, 5e-5], 2e-5),   # n=40 10a10b: the metric's configuration
+    2: ([1e-3, 5e-4, 2e-4, 1e-4], 5e-5),         # n=26 7a7b: small case (profiling)
+    1: ([], 2e-4),                               # n=16 5a5b
+}
 WORKLOAD = 3
-SCHEDULE = [1e-3, 5e-4, 2e-4, 1e-4, 5e-5]
-EPS_VAR = 2e-5
+SCHEDULE, EPS_VAR = WORKLOADS[WORKLOAD]
 TARGET_ERROR = 5e-5
 DAVIDSON_MATVECS = 9
 
@@ -166,8 +171,11 @@ def run_reference(args):
 
 
 def workload_name(n):
-    return ("synthetic n=40 10a10b C1, schedule 1e-3..5e-5 then first eps_var=2e-5 iteration "
-            "(%d dets): H-build + Davidson (9 H*v)" % n)
+    from shci_gb300 import synthetic
+    w = synthetic.WORKLOADS[WORKLOAD]
+    return ("synthetic n=%d %da%db C1, schedule %s then first eps_var=%g iteration "
+            "(%d dets): H-build + Davidson (9 H*v)"
+            % (w["n"], w["n_up"], w["n_dn"], SCHEDULE, EPS_VAR, n))
 
 
 def run_ours(args):
@@ -258,12 +266,16 @@ def run_ours(args):
     per = {k: (v[0] / max(1, v[1]), v[1]) for k, v in prof.items()}
     dom = max(prof, key=lambda k: prof[k][0])
     nnz, cand = stats["nnz"], stats["candidates"]
-    # algorithmic bytes per launch (per unit = one stored element / one det row)
+    # Algorithmic HBM bytes per launch.  H build: read the det list (16 B/det), write counts /
+    # read row offsets and the diagonal (8 B/det), write the store (12 B per stored element:
+    # u32 column + FP32 value + FP32 residual).  The index lists scanned per candidate are
+    # L2-resident (~12 B/det in total) and are reported as a scan rate, not as HBM bytes.
+    # H*v: read the store once (col + FP32 value = 8 B/element), row offsets, x (twice), y
+    # read-modify-write and the diagonal.
     alg = {
-        "hbuild_count": 12.0 * cand + 16 * n + 4 * n + 8 * n,
-        "hbuild_fill": 12.0 * cand + 16 * n + 8 * (n + 1) + 12.0 * nnz,
-        "spmv": 8.0 * nnz + 8 * (n + 1) + 8 * n + 16 * n + 8 * n,
-        "det_index": 0.0,
+        "hbuild_count": 16.0 * n + 4 * n + 8 * n,
+        "hbuild_fill": 16.0 * n + 8 * (n + 1) + 12.0 * nnz,
+        "spmv": 8.0 * nnz + 8 * (n + 1) + 16 * n + 16 * n + 8 * n,
     }
     kernels = {}
     for k, (ms_l, cnt) in per.items():
@@ -271,6 +283,8 @@ def run_ours(args):
         g = (b / (ms_l * 1e-3) / 1e9) if b else None
         kernels[k] = {"ms_per_launch": ms_l, "launches": cnt,
                       "gbs": g, "frac": (g / hbm) if g else None}
+        if k.startswith("hbuild"):
+            kernels[k]["candidates_per_s"] = cand / (ms_l * 1e-3)
     dk = kernels[dom]
     roof = {"kernel": dom, "bound": "hbm", "achieved": dk["gbs"], "peak": hbm, "unit": "GB/s",
             "frac": dk["frac"], "traffic": None, "peak_kind": peak_kind,
@@ -286,7 +300,7 @@ def run_ours(args):
         "config": {"workload": workload_name(n), "n_dets": n, "nnz_upper": nnz,
                    "nnz_sym": 2 * (nnz + n) - n, "l2": "inputs larger than L2 (H store %.0f GB)"
                    % (12 * nnz / 1e9), "setup_s": setup_s},
-        "roofline": roof, "kernels": kernels, "cpu_baseline": cpu,
+        "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "hamiltonian": stats,
         "e2e": {"value": e2e / 1e3, "unit": "s", "h2d_bytes_per_step": 24 * n,
                 "d2h_bytes_per_step": 8},
         "gpu_launches": launches // args.steps,
@@ -307,7 +321,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--data", default=os.environ.get("SHCI_BENCH_DATA", "/tmp/shci_bench_data"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", type=int, default=3, choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD, SCHEDULE, EPS_VAR
+    WORKLOAD = args.workload
+    SCHEDULE, EPS_VAR = WORKLOADS[WORKLOAD]
     if args.impl == "reference":
         run_reference(args)
     else:

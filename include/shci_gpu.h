@@ -111,8 +111,9 @@ shci_status shci_hamiltonian_elems(shci_ctx* ctx, const uint64_t* up_i, const ui
  * (2 * (strict + n) - n, sparse_matrix.cc:13-26).  Elements with |H| < 1e-12 are dropped. */
 shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_out);
 
-/* Sizes of the last build: stats[0..5] = {n dets, strict-upper nnz, unique alpha strings,
- * unique beta strings, alpha-single pairs, (row, candidate) pairs scanned}. */
+/* Sizes of the last build: stats[0..8] = {n dets, strict-upper nnz, unique alpha strings,
+ * unique beta strings, alpha-single pairs, (row, candidate) pairs scanned, and those pairs
+ * split into same-beta, same-alpha and alpha-single x beta-single parts}. */
 shci_status shci_hamiltonian_stats(shci_ctx* ctx, uint64_t* stats);
 
 /* Copy the Hamiltonian to the host: row_ptr[n+1] (strict upper), cols[nnz], vals[nnz]

@@ -328,6 +328,7 @@ shci_status shci_hamiltonian_stats(shci_ctx* c, uint64_t* stats) {
     stats[3] = c->idx.n_beta;
     stats[4] = n_as;
     stats[5] = c->H.candidates;
+    for (int k = 0; k < 3; k++) stats[6 + k] = c->H.cand_parts[k];
   });
 }
 

@@ -34,6 +34,7 @@ struct DevHamiltonian {
   size_t n = 0;
   size_t nnz = 0;
   size_t candidates = 0;  // (row, candidate) pairs scanned by the last build
+  size_t cand_parts[3] = {0, 0, 0};  // same beta, same alpha, alpha single x beta single
   int precision = SHCI_PREC_FP64;
   DevBuf<uint64_t> row_ptr;   // [n+1]
   DevBuf<uint32_t> col;       // [nnz]

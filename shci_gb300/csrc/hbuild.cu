@@ -227,10 +227,11 @@ __global__ void __launch_bounds__(kWarps * 32)
     }
     if (MODE == 0 && lane == 0) {
       row_cnt[i] = cnt;
-      // candidates scanned by this row: both groups plus the alpha-single groups
-      const uint64_t nc = (ix.b_start[b + 1] - ix.b_start[b]) + (ix.a_start[a + 1] - ix.a_start[a]) +
-                          n_mixed;
-      atomicAdd(reinterpret_cast<unsigned long long*>(work + 2), (unsigned long long)nc);
+      // candidates scanned by this row: same-beta group, same-alpha group, alpha-single groups
+      unsigned long long* cc = reinterpret_cast<unsigned long long*>(work + 2);
+      atomicAdd(cc + 0, (unsigned long long)(ix.b_start[b + 1] - ix.b_start[b]));
+      atomicAdd(cc + 1, (unsigned long long)(ix.a_start[a + 1] - ix.a_start[a]));
+      atomicAdd(cc + 2, (unsigned long long)n_mixed);
     }
   }
 }
@@ -313,15 +314,15 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.row_ptr.resize(n + 1, 1.25);
   H.row_cnt.resize(n + 1, 1.25);
   H.diag.resize(n, 1.25);
-  // err_word layout: [0] row work counter, [1] unused, [2..3] candidate counter (u64)
-  c->err_word.resize(4);
+  // err_word layout: [0] row work counter, [1] unused, [2..7] three u64 candidate counters
+  c->err_word.resize(8);
   IndexView v{ix.det_aid.p, ix.det_bid.p, ix.a_start.p, ix.b_start.p, ix.am_idx.p, ix.bm_idx.p,
               ix.as_off.p,  ix.as_list.p, ix.am_dn.p,   ix.bm_up.p,   ix.ua.p};
   int dev_sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
-  SHCI_CUDA(cudaMemsetAsync(work, 0, 4 * sizeof(unsigned), s));
+  SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
   {
     ProfScope ps(c->prof, s, "hbuild_count");
     k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
@@ -333,11 +334,12 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
   const uint64_t nnz = exclusive_scan_u64(H.row_ptr.p, H.row_ptr.p, n, s, c->sort);
   SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p + n, &nnz, 8, cudaMemcpyHostToDevice, s));
-  unsigned long long cand = 0;
-  SHCI_CUDA(cudaMemcpyAsync(&cand, work + 2, 8, cudaMemcpyDeviceToHost, s));
+  unsigned long long cand[3] = {0, 0, 0};
+  SHCI_CUDA(cudaMemcpyAsync(cand, work + 2, 24, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
   H.nnz = nnz;
-  H.candidates = cand;
+  H.candidates = cand[0] + cand[1] + cand[2];
+  for (int k = 0; k < 3; k++) H.cand_parts[k] = cand[k];
   const size_t cap = nnz ? nnz : 1;
   H.col.resize(cap, 1.1);
   if (precision == SHCI_PREC_FP64) {
