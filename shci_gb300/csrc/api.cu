@@ -89,10 +89,10 @@ shci_status shci_create(shci_ctx** out, int device, size_t hbm_budget_bytes) {
     c->err_word.mt = &c->mem;
     c->sort.set_tracker(&c->mem);
     auto& ix = c->idx;
-    for (auto* b : {&ix.det_aid, &ix.det_bid, &ix.a_start, &ix.b_start, &ix.am_idx, &ix.bm_idx,
-                    &ix.as_off, &ix.as_list})
+    for (auto* b : {&ix.det_aid, &ix.det_bid, &ix.a_start, &ix.b_start, &ix.am_idx, &ix.ad_idx,
+                    &ix.bd_idx, &ix.as_off, &ix.as_list, &ix.bs_off, &ix.bs_list})
       b->mt = &c->mem;
-    for (auto* b : {&ix.am_dn, &ix.bm_up, &ix.ua}) b->mt = &c->mem;
+    for (auto* b : {&ix.am_dn, &ix.ad_dn, &ix.bd_up, &ix.ua, &ix.ub, &ix.bs_str}) b->mt = &c->mem;
     auto& H = c->H;
     H.row_ptr.mt = H.col.mt = H.row_cnt.mt = &c->mem;
     H.val64.mt = H.diag.mt = &c->mem;

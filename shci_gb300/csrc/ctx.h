@@ -22,11 +22,16 @@ struct DetIndex {
   size_t n_alpha = 0, n_beta = 0;
   DevBuf<uint32_t> det_aid, det_bid;      // [n] unique alpha / beta id of each det
   DevBuf<uint32_t> a_start, b_start;      // [n_alpha+1], [n_beta+1] group offsets
-  DevBuf<uint32_t> am_idx, bm_idx;        // [n] det ids in alpha-major / beta-major order
-  DevBuf<uint64_t> am_dn, bm_up;          // [n] the other spin string in that order
-  DevBuf<uint64_t> ua;                    // [n_alpha] sorted unique alpha strings
+  DevBuf<uint32_t> am_idx;                // [n] det ids, alpha groups, by beta string
+  DevBuf<uint64_t> am_dn;                 // [n] beta strings in that order
+  DevBuf<uint32_t> ad_idx, bd_idx;        // [n] det ids, alpha / beta groups, by det id
+  DevBuf<uint64_t> ad_dn, bd_up;          // [n] the other spin string in that order
+  DevBuf<uint64_t> ua, ub;                // sorted unique alpha / beta strings
   DevBuf<uint32_t> as_off;                // [n_alpha+1] alpha-singles CSR
   DevBuf<uint32_t> as_list;               // alpha ids one single excitation away
+  DevBuf<uint32_t> bs_off;                // [n_beta+1] beta-singles CSR
+  DevBuf<uint32_t> bs_list;               // beta ids one single excitation away
+  DevBuf<uint64_t> bs_str;                // their beta strings
 };
 
 // Upper-triangle Hamiltonian (strict upper part in CSR; FP64 diagonal kept apart).

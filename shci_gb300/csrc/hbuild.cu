@@ -3,20 +3,23 @@
 // Replaces Hamiltonian<S>::update_abdet / update_abm1 / update_absingles / update_matrix
 // (src/solver/hamiltonian.h:157-598).  The reference keeps hash maps from alpha / beta
 // strings to det lists and intersects alpha-single lists with beta-single lists per row.
-// Here the det list is radix-sorted twice on the device:
-//   alpha-major order (by up, then dn): groups of dets sharing an alpha string;
-//   beta-major order  (by dn, then up): groups of dets sharing a beta string;
-// and each unique alpha string gets the list of unique alphas one single excitation away
-// (found by binary search of the n_up * (n - n_up) single excitations in the sorted unique
-// alphas, which replaces the alpha-minus-one hash map).  A warp then builds one row:
-//   (a) same beta string, any alpha: scan the beta group      (hamiltonian.h:430-442)
-//   (b) same alpha string, any beta: scan the alpha group     (hamiltonian.h:456-468)
-//   (c) alpha single x beta single:  scan the alpha groups of the alpha singles and keep the
-//       members whose beta string differs by one electron (popc(xor) == 2)  (:482-532)
-// keeping j > i (strict upper triangle) and |H_ij| >= 1e-12 (:440).  The result is the same
-// element set the reference builds (its incremental update only changes the order in
-// which rows are filled).  A count pass sizes each row, a scan gives row offsets, and a
-// fill pass writes the columns/values in the same deterministic traversal order.
+// Here the det list is radix-sorted on the device into:
+//   alpha groups ordered by beta string (am_*): dets sharing an alpha string;
+//   alpha groups and beta groups ordered by det id (ad_*, bd_*);
+// and each unique alpha (beta) string gets the list of unique alphas (betas) one single
+// excitation away, found by binary search of its n_e * (n - n_e) single excitations in the
+// sorted unique strings (this replaces the alpha-minus-one hash map).  A warp builds a row:
+//   (a) same beta string, any alpha  (hamiltonian.h:430-442): scan the beta group from the
+//       first det id > i (the group is in det-id order, so the lower triangle is skipped);
+//   (b) same alpha string, any beta  (:456-468): the same over the alpha group;
+//   (c) alpha single x beta single   (:482-532): for each alpha single a' of the row, either
+//       scan a''s group keeping members whose beta differs by one electron, or - when the
+//       group is larger than a few times the row's beta-single list - binary-search each
+//       beta single of the row in a''s group (ordered by beta string), whichever is cheaper;
+// keeping j > i (strict upper triangle) and |H_ij| >= 1e-12 (:440).  The result is the
+// element set the reference builds (its incremental update only changes the order in which
+// rows are filled).  A count pass sizes each row, a scan gives row offsets, and a fill pass
+// writes columns / values in the same deterministic traversal order.
 #include "ctx.h"
 #include "kernels.h"
 
@@ -47,11 +50,17 @@ __global__ void k_group_fill(const uint64_t* sorted, const uint32_t* perm, const
     const uint32_t d = perm[k];
     if (flags[k]) {
       start[g] = static_cast<uint32_t>(k);
-      if (uniq) uniq[g] = sorted[k];
+      uniq[g] = sorted[k];
     }
     det_gid[d] = g;
-    other_sorted[k] = other[d];
+    if (other_sorted) other_sorted[k] = other[d];
   }
+}
+
+__global__ void k_widen_ids(const uint32_t* in, uint64_t* out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
 }
 
 __device__ __forceinline__ bool bsearch_u64(const uint64_t* a, uint32_t n, uint64_t key,
@@ -67,14 +76,14 @@ __device__ __forceinline__ bool bsearch_u64(const uint64_t* a, uint32_t n, uint6
   return lo < n && a[lo] == key;
 }
 
-// Alpha singles: for each unique alpha, the unique alphas one single excitation away.
+// Singles of unique strings: for each sorted unique string u[g], the ids of the unique strings
+// one single excitation away (and, if str_out, their strings).
 template <bool FILL>
-__global__ void k_alpha_singles(const uint64_t* ua, uint32_t n_alpha, int n_orbs,
-                                uint32_t* cnt, const uint32_t* off, uint32_t* list) {
+__global__ void k_singles(const uint64_t* u, uint32_t n_u, int n_orbs, uint32_t* cnt,
+                          const uint32_t* off, uint32_t* list, uint64_t* str_out) {
   const uint64_t full = n_orbs == 64 ? ~0ull : ((1ull << n_orbs) - 1ull);
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_alpha;
-       g += gridDim.x * blockDim.x) {
-    const uint64_t a = ua[g];
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_u; g += gridDim.x * blockDim.x) {
+    const uint64_t a = u[g];
     uint32_t c = 0;
     const uint32_t base = FILL ? off[g] : 0;
     for (uint64_t mo = a; mo; mo &= mo - 1) {
@@ -82,8 +91,11 @@ __global__ void k_alpha_singles(const uint64_t* ua, uint32_t n_alpha, int n_orbs
       for (uint64_t mv = full & ~a; mv; mv &= mv - 1) {
         const uint64_t vb = mv & (~mv + 1);
         uint32_t pos;
-        if (bsearch_u64(ua, n_alpha, a ^ ob ^ vb, &pos)) {
-          if (FILL) list[base + c] = pos;
+        if (bsearch_u64(u, n_u, a ^ ob ^ vb, &pos)) {
+          if (FILL) {
+            list[base + c] = pos;
+            if (str_out) str_out[base + c] = a ^ ob ^ vb;
+          }
           c++;
         }
       }
@@ -93,9 +105,35 @@ __global__ void k_alpha_singles(const uint64_t* ua, uint32_t n_alpha, int n_orbs
 }
 
 struct IndexView {
-  const uint32_t *det_aid, *det_bid, *a_start, *b_start, *am_idx, *bm_idx, *as_off, *as_list;
-  const uint64_t *am_dn, *bm_up, *ua;
+  const uint32_t *det_aid, *det_bid, *a_start, *b_start;
+  const uint32_t *am_idx, *ad_idx, *bd_idx;
+  const uint64_t *am_dn, *ad_dn, *bd_up;
+  const uint64_t* ua;
+  const uint32_t *as_off, *as_list, *bs_off;
+  const uint64_t* bs_str;
 };
+
+// first k in [lo, hi) with idx[k] > i (idx ascending)
+__device__ __forceinline__ uint32_t first_after(const uint32_t* idx, uint32_t lo, uint32_t hi,
+                                                uint32_t i) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (idx[mid] <= i) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// first k in [lo, hi) with a[k] >= key (a ascending)
+__device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* a, uint32_t lo, uint32_t hi,
+                                                    uint64_t key) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
 
 // MODE 0: count (and diagonal), MODE 1: fill FP64, MODE 2: fill mixed (FP32 value+residual)
 template <int MODE>
@@ -115,6 +153,7 @@ __global__ void __launch_bounds__(kWarps * 32)
     const uint32_t a = ix.det_aid[i], b = ix.det_bid[i];
     uint64_t base = MODE ? row_ptr[i] : 0;
     uint32_t cnt = 0;
+    uint64_t n_scan_a = 0, n_scan_b = 0, n_mixed = 0;
     auto emit = [&](bool keep, uint32_t j, double H) {
       const unsigned bal = __ballot_sync(kFull, keep);
       if (MODE && keep) {
@@ -130,52 +169,53 @@ __global__ void __launch_bounds__(kWarps * 32)
       }
       cnt += __popc(bal);
     };
-    // (a) same beta string
+    // (a) same beta string: beta group in det-id order, from the first j > i
     {
-      const uint32_t s = ix.b_start[b], e = ix.b_start[b + 1];
+      const uint32_t e = ix.b_start[b + 1];
+      const uint32_t s = first_after(ix.bd_idx, ix.b_start[b], e, i);
+      n_scan_a = e - s;
       for (uint32_t k0 = s; k0 < e; k0 += 32) {
         const uint32_t k = k0 + lane;
         bool keep = false;
         uint32_t j = 0;
         double H = 0.0;
         if (k < e) {
-          j = ix.bm_idx[k];
-          if (j > i) {
-            const uint64_t uj = ix.bm_up[k];
-            if (popc64(uj ^ ui) <= 4) {
-              H = h_offdiag(I, ui, di, uj, di);
-              keep = fabs(H) >= kEps;
-            }
+          j = ix.bd_idx[k];
+          const uint64_t uj = ix.bd_up[k];
+          if (popc64(uj ^ ui) <= 4) {
+            H = h_offdiag(I, ui, di, uj, di);
+            keep = fabs(H) >= kEps;
           }
         }
         emit(keep, j, H);
       }
     }
-    // (b) same alpha string
+    // (b) same alpha string: alpha group in det-id order, from the first j > i
     {
-      const uint32_t s = ix.a_start[a], e = ix.a_start[a + 1];
+      const uint32_t e = ix.a_start[a + 1];
+      const uint32_t s = first_after(ix.ad_idx, ix.a_start[a], e, i);
+      n_scan_b = e - s;
       for (uint32_t k0 = s; k0 < e; k0 += 32) {
         const uint32_t k = k0 + lane;
         bool keep = false;
         uint32_t j = 0;
         double H = 0.0;
         if (k < e) {
-          j = ix.am_idx[k];
-          if (j > i) {
-            const uint64_t dj = ix.am_dn[k];
-            if (popc64(dj ^ di) <= 4) {
-              H = h_offdiag(I, ui, di, ui, dj);
-              keep = fabs(H) >= kEps;
-            }
+          j = ix.ad_idx[k];
+          const uint64_t dj = ix.ad_dn[k];
+          if (popc64(dj ^ di) <= 4) {
+            H = h_offdiag(I, ui, di, ui, dj);
+            keep = fabs(H) >= kEps;
           }
         }
         emit(keep, j, H);
       }
     }
-    // (c) alpha single x beta single: flatten (alpha single, group member) pairs over lanes
-    uint64_t n_mixed = 0;
+    // (c) alpha single x beta single
     {
       const uint32_t s0 = ix.as_off[a], s1 = ix.as_off[a + 1];
+      const uint32_t b0 = ix.bs_off[b], nbs = ix.bs_off[b + 1] - b0;
+      const uint32_t thr = 4u * nbs + 32u;  // probe groups larger than this
       for (uint32_t c0 = s0; c0 < s1; c0 += 32) {
         const uint32_t c = c0 + lane;
         uint32_t g = 0, gs = 0, gn = 0;
@@ -184,8 +224,10 @@ __global__ void __launch_bounds__(kWarps * 32)
           gs = ix.a_start[g];
           gn = ix.a_start[g + 1] - gs;
         }
-        // inclusive scan of group sizes across the chunk
-        uint32_t inc = gn;
+        const bool probe = gn > thr;
+        const uint32_t sn = probe ? 0u : gn;
+        // scan mode: flatten (alpha single, group member) pairs over lanes
+        uint32_t inc = sn;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const uint32_t t = __shfl_up_sync(kFull, inc, o);
@@ -207,11 +249,11 @@ __global__ void __launch_bounds__(kWarps * 32)
             if (v <= t) lo += step;
           }
           const uint32_t o_inc = __shfl_sync(kFull, inc, lo);
-          const uint32_t o_gn = __shfl_sync(kFull, gn, lo);
+          const uint32_t o_n = __shfl_sync(kFull, sn, lo);
           const uint32_t o_gs = __shfl_sync(kFull, gs, lo);
           const uint32_t o_g = __shfl_sync(kFull, g, lo);
           if (t < total) {
-            const uint32_t k = o_gs + (t - (o_inc - o_gn));
+            const uint32_t k = o_gs + (t - (o_inc - o_n));
             j = ix.am_idx[k];
             if (j > i) {
               const uint64_t dj = ix.am_dn[k];
@@ -223,20 +265,87 @@ __global__ void __launch_bounds__(kWarps * 32)
           }
           emit(keep, j, H);
         }
+        // probe mode: binary-search each beta single of the row in the big groups
+        unsigned pmask = __ballot_sync(kFull, probe);
+        while (pmask) {
+          const int l = __ffs(pmask) - 1;
+          pmask &= pmask - 1;
+          const uint32_t p_gs = __shfl_sync(kFull, gs, l);
+          const uint32_t p_gn = __shfl_sync(kFull, gn, l);
+          const uint32_t p_g = __shfl_sync(kFull, g, l);
+          const uint64_t ua2 = ix.ua[p_g];
+          n_mixed += nbs;
+          for (uint32_t k0 = 0; k0 < nbs; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            bool keep = false;
+            uint32_t j = 0;
+            double H = 0.0;
+            if (k < nbs) {
+              const uint64_t bstr = ix.bs_str[b0 + k];
+              const uint32_t pos = lower_bound_u64(ix.am_dn, p_gs, p_gs + p_gn, bstr);
+              if (pos < p_gs + p_gn && ix.am_dn[pos] == bstr) {
+                j = ix.am_idx[pos];
+                if (j > i) {
+                  H = h_offdiag(I, ui, di, ua2, bstr);
+                  keep = fabs(H) >= kEps;
+                }
+              }
+            }
+            emit(keep, j, H);
+          }
+        }
       }
     }
     if (MODE == 0 && lane == 0) {
       row_cnt[i] = cnt;
-      // candidates scanned by this row: same-beta group, same-alpha group, alpha-single groups
+      // candidates examined by this row, per part
       unsigned long long* cc = reinterpret_cast<unsigned long long*>(work + 2);
-      atomicAdd(cc + 0, (unsigned long long)(ix.b_start[b + 1] - ix.b_start[b]));
-      atomicAdd(cc + 1, (unsigned long long)(ix.a_start[a + 1] - ix.a_start[a]));
+      atomicAdd(cc + 0, (unsigned long long)n_scan_a);
+      atomicAdd(cc + 1, (unsigned long long)n_scan_b);
       atomicAdd(cc + 2, (unsigned long long)n_mixed);
     }
   }
 }
 
 }  // namespace
+
+// Sorts det ids by group id (stable: det-id order within each group) and gathers `other`.
+static void group_by_det_id(shci_ctx* c, const uint32_t* gid, size_t n_groups,
+                            const uint64_t* other, DevBuf<uint32_t>& idx_out,
+                            DevBuf<uint64_t>& other_out) {
+  const size_t n = c->up.size();
+  cudaStream_t s = c->stream;
+  int bits = 1;
+  while ((1ull << bits) < n_groups + 1) bits++;
+  k_widen_ids<<<grid_for(n, 256), 256, 0, s>>>(gid, c->k0.p, n);
+  SHCI_LAUNCH_CHECK();
+  iota_u32(c->u0.p, n, s);
+  radix_sort_pairs(c->k0, c->u0, n, 0, bits, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(idx_out.p, c->u0.p, n * 4, cudaMemcpyDeviceToDevice, s));
+  gather_u64(other, c->u0.p, other_out.p, n, s);
+  c->launches += 3;
+}
+
+static void build_singles(shci_ctx* c, const DevBuf<uint64_t>& u, size_t n_u, DevBuf<uint32_t>& off,
+                          DevBuf<uint32_t>& list, DevBuf<uint64_t>* str) {
+  cudaStream_t s = c->stream;
+  const int nb = c->I.n;
+  const uint32_t nu = static_cast<uint32_t>(n_u);
+  off.resize(nu + 1, 1.25);
+  c->u1.reserve(nu + 1, 1.25);
+  k_singles<false><<<grid_for(nu, 128), 128, 0, s>>>(u.p, nu, nb, c->u1.p, nullptr, nullptr,
+                                                     nullptr);
+  SHCI_LAUNCH_CHECK();
+  const uint32_t tot = exclusive_scan_u32(c->u1.p, off.p, nu, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(off.p + nu, &tot, 4, cudaMemcpyHostToDevice, s));
+  list.resize(tot ? tot : 1, 1.25);
+  if (str) str->resize(tot ? tot : 1, 1.25);
+  k_singles<true><<<grid_for(nu, 128), 128, 0, s>>>(u.p, nu, nb, nullptr, off.p, list.p,
+                                                    str ? str->p : nullptr);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 3;
+}
 
 void build_index(shci_ctx* c) {
   auto& ix = c->idx;
@@ -253,11 +362,13 @@ void build_index(shci_ctx* c) {
   ix.det_aid.resize(n, 1.25);
   ix.det_bid.resize(n, 1.25);
   ix.am_idx.resize(n, 1.25);
-  ix.bm_idx.resize(n, 1.25);
   ix.am_dn.resize(n, 1.25);
-  ix.bm_up.resize(n, 1.25);
+  ix.ad_idx.resize(n, 1.25);
+  ix.ad_dn.resize(n, 1.25);
+  ix.bd_idx.resize(n, 1.25);
+  ix.bd_up.resize(n, 1.25);
   for (int major = 0; major < 2; major++) {
-    // major 0: alpha-major (sort by dn, then stably by up); major 1: beta-major.
+    // major 0: by (up, dn) - sort by dn, then stably by up; major 1: by (dn, up).
     const uint64_t* first = major == 0 ? c->d_dn.p : c->d_up.p;
     const uint64_t* second = major == 0 ? c->d_up.p : c->d_dn.p;
     SHCI_CUDA(cudaMemcpyAsync(c->k0.p, first, n * 8, cudaMemcpyDeviceToDevice, s));
@@ -269,37 +380,29 @@ void build_index(shci_ctx* c) {
     SHCI_LAUNCH_CHECK();
     const uint32_t ng = exclusive_scan_u32(c->u1.p, c->u2.p, n, s, c->sort);
     auto& start = major == 0 ? ix.a_start : ix.b_start;
-    auto& perm = major == 0 ? ix.am_idx : ix.bm_idx;
-    auto& other_sorted = major == 0 ? ix.am_dn : ix.bm_up;
+    auto& uniq = major == 0 ? ix.ua : ix.ub;
     auto& gid = major == 0 ? ix.det_aid : ix.det_bid;
     start.resize(ng + 1, 1.25);
-    if (major == 0) ix.ua.resize(ng, 1.25);
-    SHCI_CUDA(cudaMemcpyAsync(perm.p, c->u0.p, n * 4, cudaMemcpyDeviceToDevice, s));
+    uniq.resize(ng, 1.25);
+    if (major == 0)
+      SHCI_CUDA(cudaMemcpyAsync(ix.am_idx.p, c->u0.p, n * 4, cudaMemcpyDeviceToDevice, s));
     k_group_fill<<<grid_for(n, 256), 256, 0, s>>>(c->k1.p, c->u0.p, c->u1.p, c->u2.p, first, n,
-                                                  start.p, major == 0 ? ix.ua.p : nullptr,
-                                                  gid.p, other_sorted.p);
+                                                  start.p, uniq.p, gid.p,
+                                                  major == 0 ? ix.am_dn.p : nullptr);
     SHCI_LAUNCH_CHECK();
     const uint32_t nn = static_cast<uint32_t>(n);
     SHCI_CUDA(cudaMemcpyAsync(start.p + ng, &nn, 4, cudaMemcpyHostToDevice, s));
     if (major == 0) ix.n_alpha = ng;
     else ix.n_beta = ng;
-    SHCI_CUDA(cudaStreamSynchronize(s));  // nn lives on the host stack
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    c->launches += 10;
   }
-  // alpha singles
-  const uint32_t na = static_cast<uint32_t>(ix.n_alpha);
-  ix.as_off.resize(na + 1, 1.25);
-  c->u1.reserve(na + 1, 1.25);
-  k_alpha_singles<false><<<grid_for(na, 128), 128, 0, s>>>(ix.ua.p, na, nb, c->u1.p, nullptr,
-                                                           nullptr);
-  SHCI_LAUNCH_CHECK();
-  const uint32_t tot = exclusive_scan_u32(c->u1.p, ix.as_off.p, na, s, c->sort);
-  SHCI_CUDA(cudaMemcpyAsync(ix.as_off.p + na, &tot, 4, cudaMemcpyHostToDevice, s));
-  ix.as_list.resize(tot ? tot : 1, 1.25);
-  k_alpha_singles<true><<<grid_for(na, 128), 128, 0, s>>>(ix.ua.p, na, nb, nullptr, ix.as_off.p,
-                                                          ix.as_list.p);
-  SHCI_LAUNCH_CHECK();
-  SHCI_CUDA(cudaStreamSynchronize(s));
-  c->launches += 2 * (4 * 2 + 4) + 3;
+  // groups in det-id order (the sort is stable and starts from det-id order)
+  group_by_det_id(c, ix.det_aid.p, ix.n_alpha, c->d_dn.p, ix.ad_idx, ix.ad_dn);
+  group_by_det_id(c, ix.det_bid.p, ix.n_beta, c->d_up.p, ix.bd_idx, ix.bd_up);
+  // single-excitation lists of the unique strings
+  build_singles(c, ix.ua, ix.n_alpha, ix.as_off, ix.as_list, nullptr);
+  build_singles(c, ix.ub, ix.n_beta, ix.bs_off, ix.bs_list, &ix.bs_str);
 }
 
 size_t build_hamiltonian(shci_ctx* c, int precision) {
@@ -316,8 +419,9 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.diag.resize(n, 1.25);
   // err_word layout: [0] row work counter, [1] unused, [2..7] three u64 candidate counters
   c->err_word.resize(8);
-  IndexView v{ix.det_aid.p, ix.det_bid.p, ix.a_start.p, ix.b_start.p, ix.am_idx.p, ix.bm_idx.p,
-              ix.as_off.p,  ix.as_list.p, ix.am_dn.p,   ix.bm_up.p,   ix.ua.p};
+  IndexView v{ix.det_aid.p, ix.det_bid.p, ix.a_start.p, ix.b_start.p, ix.am_idx.p,
+              ix.ad_idx.p,  ix.bd_idx.p,  ix.am_dn.p,   ix.ad_dn.p,   ix.bd_up.p,
+              ix.ua.p,      ix.as_off.p,  ix.as_list.p, ix.bs_off.p,  ix.bs_str.p};
   int dev_sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
