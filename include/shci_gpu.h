@@ -104,6 +104,19 @@ shci_status shci_hamiltonian_elems(shci_ctx* ctx, const uint64_t* up_i, const ui
                                    const uint64_t* up_j, const uint64_t* dn_j, size_t n,
                                    double* out);
 
+/* Same results as shci_hamiltonian_elems for callers that cannot allocate device memory
+ * (for example a process whose device memory is held by another framework's caching
+ * allocator, or one that forbids device allocation after start-up).  It has no counterpart
+ * in the reference: it exists only for such callers.  It allocates nothing: inputs and
+ * results are staged in one fixed 2.5 MiB device array built into the library (resident on
+ * every GPU that loads it until the process exits).  At most 65,536 pairs per call (larger
+ * n: SHCI_ERR_ARG).  All calls share the array, so calls that overlap on the GPU race; the
+ * first call on each device looks up the array's address and should come before any stream
+ * capture. */
+shci_status shci_hamiltonian_elems_noalloc(shci_ctx* ctx, const uint64_t* up_i,
+                                           const uint64_t* dn_i, const uint64_t* up_j,
+                                           const uint64_t* dn_j, size_t n, double* out);
+
 /* ---- Hamiltonian build (Hamiltonian<S>::update, hamiltonian.h:87-112, 415-598) -------- */
 
 /* Build the upper-triangle sparse Hamiltonian of the current dets on the device.

@@ -57,6 +57,7 @@ def load():
         "shci_set_coefs": [vp, _f64p, sz],
         "shci_set_coefs_dev": [vp, vp, sz],
         "shci_hamiltonian_elems": [vp, _u64p, _u64p, _u64p, _u64p, sz, _f64p],
+        "shci_hamiltonian_elems_noalloc": [vp, _u64p, _u64p, _u64p, _u64p, sz, _f64p],
         "shci_update_hamiltonian": [vp, i, P(sz)],
         "shci_get_hamiltonian": [vp, _u64p, _u32p, _f64p, _f64p],
         "shci_hv": [vp, vp, vp, i],
@@ -204,6 +205,14 @@ class Context:
         ui, di, uj, dj = (np.ascontiguousarray(x, np.uint64) for x in (ui, di, uj, dj))
         out = np.zeros(len(ui))
         self._ck(self.L.shci_hamiltonian_elems(self.h, ui, di, uj, dj, len(ui), out))
+        return out
+
+    def h_elems_noalloc(self, ui, di, uj, dj):
+        """shci_hamiltonian_elems_noalloc: same results, staged in the library's fixed device
+        array (no device allocation; at most 65,536 pairs per call)."""
+        ui, di, uj, dj = (np.ascontiguousarray(x, np.uint64) for x in (ui, di, uj, dj))
+        out = np.zeros(len(ui))
+        self._ck(self.L.shci_hamiltonian_elems_noalloc(self.h, ui, di, uj, dj, len(ui), out))
         return out
 
     # ---- Hamiltonian / Davidson --------------------------------------------------------

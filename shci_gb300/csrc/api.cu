@@ -298,6 +298,16 @@ shci_status shci_hamiltonian_elems(shci_ctx* c, const uint64_t* ui, const uint64
   });
 }
 
+shci_status shci_hamiltonian_elems_noalloc(shci_ctx* c, const uint64_t* ui, const uint64_t* di,
+                                           const uint64_t* uj, const uint64_t* dj, size_t n,
+                                           double* out) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    hamiltonian_elems_noalloc(c, ui, di, uj, dj, n, out);
+  });
+}
+
 shci_status shci_update_hamiltonian(shci_ctx* c, int precision, size_t* nnz_out) {
   if (!c) return SHCI_ERR_ARG;
   return guard(c, [&]() {

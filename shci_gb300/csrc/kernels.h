@@ -21,6 +21,10 @@ void sync_dets(shci_ctx* c);          // host det list -> device (if dirty)
 void hamiltonian_elems(shci_ctx* c, const uint64_t* ui, const uint64_t* di, const uint64_t* uj,
                        const uint64_t* dj, size_t n, double* out);
 
+// noalloc.cu: hamiltonian_elems with staging in a fixed device array (no allocation)
+void hamiltonian_elems_noalloc(shci_ctx* c, const uint64_t* ui, const uint64_t* di,
+                               const uint64_t* uj, const uint64_t* dj, size_t n, double* out);
+
 // hbuild.cu
 void build_index(shci_ctx* c);
 size_t build_hamiltonian(shci_ctx* c, int precision);
