@@ -202,6 +202,29 @@ shci_status shci_profile_get(shci_ctx* ctx, char* names, double* total_ms, uint6
 shci_status shci_pt2_dtm(shci_ctx* ctx, double energy_var, double eps_pt_dtm, size_t n_batches,
                          double* correction, double* uncert, size_t* n_pt_dets);
 
+/* Pseudo-stochastic stage (Solver<S>::get_energy_pt_psto, solver.h:766-896): batches of the
+ * PT space between eps_pt_psto and eps_pt_dtm with the reference's batch extrapolation,
+ * uncertainty and early stop (uncert <= target_error / 2, or eps_pt_psto <= eps_pt and
+ * uncert <= target_error).  out: correction (excluding the dtm part), uncertainty, PT dets,
+ * batches computed. */
+shci_status shci_pt2_psto(shci_ctx* ctx, double energy_var, double eps_pt_dtm,
+                          double eps_pt_psto, size_t n_batches, double target_error,
+                          double eps_pt, double* correction, double* uncert, size_t* n_pt_dets,
+                          size_t* n_batches_done);
+
+/* Stochastic stage (Solver<S>::get_energy_pt_sto, solver.h:898-1153) with a given sample
+ * size: |c_i|-weighted samples drawn on the host with the reference's generator
+ * (std::default_random_engine(random_seed)) and alias tables, a random hash batch per
+ * iteration, the reference's estimator and stopping rules (at most max_iterations).
+ * psto_uncert = uncertainty of the preceding psto stage.  semisto must be 0 (see the
+ * message returned otherwise).  loops (may be NULL, cap entries) receives each iteration's
+ * estimate; out: correction, uncertainty, iterations run. */
+shci_status shci_pt2_sto(shci_ctx* ctx, double energy_var, double eps_pt_psto, double eps_pt,
+                         size_t n_batches, size_t n_dets_in_sample, int semisto,
+                         unsigned random_seed, size_t max_iterations, double target_error,
+                         double psto_uncert, double* correction, double* uncert,
+                         size_t* n_iterations, double* loops, size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

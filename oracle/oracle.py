@@ -74,6 +74,8 @@ def lib():
             "orc_run_variation_step": (d, [vp, d, i, d]),
             "orc_hbuild_sample": (None, [vp, sz, sz, _f64p]),
             "orc_threads": (i, []),
+            "orc_pt_psto": (None, [vp, d, d, sz, d, d, _f64p]),
+            "orc_pt_sto": (sz, [vp, d, d, sz, sz, u, sz, d, d, _f64p, _f64p, sz]),
             "orc_rdm1": (None, [vp, _f64p]),
             "orc_rdm2": (None, [vp, _f64p]),
         }
@@ -272,6 +274,19 @@ class Oracle:
         self.L.orc_pt_dtm(self.h, eps_pt_dtm, n_batches, ctypes.byref(v), ctypes.byref(u),
                           ctypes.byref(n))
         return v.value, u.value, n.value
+
+    def pt_psto(self, eps_dtm, eps_psto, n_batches, target_error=5e-5, eps_pt=0.0):
+        out = np.zeros(4)
+        self.L.orc_pt_psto(self.h, eps_dtm, eps_psto, n_batches, target_error, eps_pt, out)
+        return out[0], out[1], int(out[2]), int(out[3])
+
+    def pt_sto(self, eps_psto, eps_pt, n_batches, n_samples, seed=347634253, max_iter=100,
+               target_error=5e-5, psto_uncert=0.0):
+        out = np.zeros(2)
+        loops = np.zeros(max_iter)
+        n = self.L.orc_pt_sto(self.h, eps_psto, eps_pt, n_batches, n_samples, seed, max_iter,
+                              target_error, psto_uncert, out, loops, max_iter)
+        return out[0], out[1], loops[:n]
 
     def rdm1(self):
         out = np.zeros(self.n_orbs * self.n_orbs)

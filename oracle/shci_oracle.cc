@@ -15,6 +15,7 @@
 // Floating point: compiled with -ffp-contract=off so x86 and Arm builds agree bit for bit.
 
 #include <algorithm>
+#include <array>
 #include <cassert>
 #include <cmath>
 #include <cstdint>
@@ -1303,6 +1304,185 @@ struct Solver {
     res.n_pt_dets = n_sum;
     return res;
   }
+
+  // ------------------------------------------------ PT2: pseudo-stochastic stage
+  // src/solver/solver.h:766-896 with a given number of batches.
+  PtResult pt_psto(double eps_dtm, double eps_psto, size_t n_batches, double target_error,
+                   double eps_pt, size_t* batches_done) {
+    std::unordered_set<Det, DetHasher> vset(sys.dets.begin(), sys.dets.end());
+    const size_t n_var = sys.dets.size();
+    double esum = 0.0, esq = 0.0;
+    size_t n_sum = 0;
+    PtResult res;
+    *batches_done = 0;
+    for (size_t batch = 0; batch < n_batches; batch++) {
+      const int nt = omp_get_max_threads();
+      std::vector<std::unordered_map<Det, std::array<double, 2>, DetHasher>> part(nt);
+#pragma omp parallel for schedule(dynamic, 8)
+      for (size_t i = 0; i < n_var; i++) {
+        auto& m = part[omp_get_thread_num()];
+        const Det& det = sys.dets[i];
+        const double coef = sys.coefs[i];
+        auto handler = [&](const Det& a, int n_excite) {
+          if (rehash(det_hash(a)) % n_batches != batch) return;
+          if (vset.count(a)) return;
+          const double hc = sys.hamiltonian_elem(det, a, n_excite) * coef;
+          if (std::abs(hc) < eps_psto) return;
+          auto& v = m[a];
+          v[0] += hc;
+          if (std::abs(hc) >= eps_dtm) v[1] += hc;
+        };
+        sys.find_connected_dets(det, INF / std::abs(coef), eps_psto / std::abs(coef), handler);
+      }
+      std::unordered_map<Det, std::array<double, 2>, DetHasher> hc;
+      for (auto& m : part)
+        for (auto& kv : m) {
+          auto& v = hc[kv.first];
+          v[0] += kv.second[0];
+          v[1] += kv.second[1];
+        }
+      double bs = 0.0, bsq = 0.0;
+      for (auto& kv : hc) {
+        const double d = kv.second[0] * kv.second[0] - kv.second[1] * kv.second[1];
+        const double x = d / (sys.energy_var - sys.hamiltonian_elem(kv.first, kv.first, 0));
+        bs += x;
+        bsq += x * x;
+      }
+      n_sum += hc.size();
+      esum += bs;
+      esq += bsq;
+      res.value = esum / (batch + 1) * n_batches;
+      if (batch == n_batches - 1) {
+        res.uncert = 0.0;
+      } else {
+        const double avg = esum / n_sum;
+        const double sd = std::sqrt(esq / n_sum - avg * avg);
+        res.uncert = sd / std::sqrt((double)n_sum) * n_sum / (batch + 1) * (n_batches - batch - 1);
+      }
+      *batches_done = batch + 1;
+      if (res.uncert <= target_error * 0.5) break;
+      if (eps_psto <= eps_pt && res.uncert <= target_error) break;
+    }
+    res.n_pt_dets = n_sum;
+    return res;
+  }
+
+  // ------------------------------------------------ PT2: stochastic stage
+  // src/solver/solver.h:898-1153 with n_dets_in_sample given and semisto_sto = false.
+  PtResult pt_sto(double eps_psto, double eps_pt, size_t n_batches, size_t n_samples,
+                  unsigned seed, size_t max_iter, double target_error, double psto_uncert,
+                  std::vector<double>* loops) {
+    std::unordered_set<Det, DetHasher> vset(sys.dets.begin(), sys.dets.end());
+    const size_t n_var = sys.dets.size();
+    double sw = 0.0;
+    for (size_t i = 0; i < n_var; i++) sw += std::abs(sys.coefs[i]);
+    std::vector<double> probs(n_var);
+    for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(sys.coefs[i]) / sw;
+    std::default_random_engine gen(seed);
+    std::uniform_real_distribution<double> ur(0., 1.);
+    // Vose alias tables (src/util.cc:128-175)
+    std::vector<double> ap(n_var), tp(n_var);
+    std::vector<size_t> al(n_var, 0);
+    {
+      std::stack<size_t> sm, lg;
+      for (size_t i = 0; i < n_var; i++) {
+        tp[i] = probs[i] * n_var;
+        if (tp[i] < 1.) sm.push(i); else lg.push(i);
+      }
+      while (!sm.empty() && !lg.empty()) {
+        const size_t l = lg.top(), s = sm.top();
+        ap[s] = tp[s];
+        al[s] = l;
+        tp[l] = tp[l] + tp[s] - 1.;
+        if (tp[l] < 1.) {
+          lg.pop();
+          sm.top() = l;
+        } else {
+          sm.pop();
+        }
+      }
+      while (!lg.empty()) { ap[lg.top()] = 1.; lg.pop(); }
+      while (!sm.empty()) { ap[sm.top()] = 1.; sm.pop(); }
+    }
+    std::uniform_int_distribution<size_t> ui_var(0, n_var - 1);
+    std::uniform_int_distribution<size_t> ui_batch(0, n_batches - 1);
+    const double factor = 1. / (n_samples - 1.);
+    PtResult res;
+    std::vector<double> lv;
+    size_t iteration = 0;
+    while (iteration < max_iter) {
+      std::unordered_map<size_t, unsigned> cnt;
+      std::vector<size_t> list;
+      for (size_t k = 0; k < n_samples; k++) {
+        const size_t r1 = ui_var(gen);
+        const double r2 = ur(gen);
+        const size_t id = r2 < ap[r1] ? r1 : al[r1];
+        if (cnt.count(id) == 0) list.push_back(id);
+        cnt[id]++;
+      }
+      const size_t batch_id = ui_batch(gen);
+      const int nt = omp_get_max_threads();
+      std::vector<std::unordered_map<Det, std::array<double, 5>, DetHasher>> part(nt);
+#pragma omp parallel for schedule(dynamic, 8)
+      for (size_t si = 0; si < list.size(); si++) {
+        auto& m = part[omp_get_thread_num()];
+        const size_t i = list[si];
+        const Det& det = sys.dets[i];
+        const double coef = sys.coefs[i];
+        const double count = static_cast<double>(cnt.at(i));
+        const double weight = n_samples * probs[i];
+        auto handler = [&](const Det& a, int n_excite) {
+          if (rehash(det_hash(a)) % n_batches != batch_id) return;
+          if (vset.count(a)) return;
+          const double hc = sys.hamiltonian_elem(det, a, n_excite) * coef;
+          if (std::abs(hc) < eps_pt) return;
+          auto& v = m[a];
+          const double x = count * hc / weight;
+          v[0] += x;
+          if (std::abs(hc) > eps_psto) v[1] += x;
+          const double x2 = count * hc / weight * std::sqrt(factor);
+          if (std::abs(hc) > eps_psto) {
+            v[2] += x2;
+            v[3] += x2;
+          } else {
+            v[2] += x2;
+            v[4] += std::pow(count * hc / weight, 2) * (1. - weight / count + factor);
+          }
+        };
+        sys.find_connected_dets(det, INF / std::abs(coef), eps_pt / std::abs(coef), handler);
+      }
+      std::unordered_map<Det, std::array<double, 5>, DetHasher> hc;
+      for (auto& m : part)
+        for (auto& kv : m) {
+          auto& v = hc[kv.first];
+          for (int k = 0; k < 5; k++) v[k] += kv.second[k];
+        }
+      double loop = 0.0;
+      for (auto& kv : hc) {
+        const auto& s = kv.second;
+        const double f = static_cast<double>(n_batches) /
+                         (sys.energy_var - sys.hamiltonian_elem(kv.first, kv.first, 0));
+        loop += (s[0] * s[0] - s[1] * s[1] + s[2] * s[2] - s[3] * s[3] - s[4]) * f;
+      }
+      res.n_pt_dets += hc.size();
+      lv.push_back(loop);
+      const double n = static_cast<double>(lv.size());
+      double sm = 0.0, sq = 0.0;
+      for (double v : lv) {
+        sm += v;
+        sq += v * v;
+      }
+      res.value = sm / n;
+      res.uncert = std::sqrt((sq - sm * sm / n) / (n - 1)) / std::sqrt(n);
+      iteration++;
+      if (iteration >= 6 && res.uncert <= target_error * 0.7) break;
+      if (iteration >= 10 &&
+          std::sqrt(res.uncert * res.uncert + psto_uncert * psto_uncert) <= target_error)
+        break;
+    }
+    if (loops) *loops = lv;
+    return res;
+  }
 };
 
 // ---------------------------------------------------------------- RDMs (C13), time_sym = false
@@ -1852,6 +2032,28 @@ void orc_pt_dtm(void* h, double eps_pt_dtm, size_t n_batches, double* value, dou
   *value = r.value;
   *uncert = r.uncert;
   *n_pt_dets = r.n_pt_dets;
+}
+
+void orc_pt_psto(void* h, double eps_dtm, double eps_psto, size_t n_batches, double target_error,
+                 double eps_pt, double* out /* value, uncert, n_pt_dets, batches */) {
+  size_t done = 0;
+  auto r = S(h).pt_psto(eps_dtm, eps_psto, n_batches, target_error, eps_pt, &done);
+  out[0] = r.value;
+  out[1] = r.uncert;
+  out[2] = static_cast<double>(r.n_pt_dets);
+  out[3] = static_cast<double>(done);
+}
+
+size_t orc_pt_sto(void* h, double eps_psto, double eps_pt, size_t n_batches, size_t n_samples,
+                  unsigned seed, size_t max_iter, double target_error, double psto_uncert,
+                  double* out /* value, uncert */, double* loops, size_t cap) {
+  std::vector<double> lv;
+  auto r = S(h).pt_sto(eps_psto, eps_pt, n_batches, n_samples, seed, max_iter, target_error,
+                       psto_uncert, &lv);
+  out[0] = r.value;
+  out[1] = r.uncert;
+  for (size_t k = 0; k < lv.size() && k < cap; k++) loops[k] = lv[k];
+  return lv.size();
 }
 
 void orc_rdm1(void* h, double* out) {

@@ -72,6 +72,8 @@ def load():
         "shci_get_launch_count": [vp, P(u64)],
         "shci_pt2_dtm": [vp, d, d, sz, P(d), P(d), P(sz)],
         "shci_hamiltonian_stats": [vp, _u64p],
+        "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
+        "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, P(d), P(d), P(sz), _f64p, sz],
         "shci_profile": [vp, i],
         "shci_profile_get": [vp, vp, _f64p, _u64p, sz, P(sz)],
     }
@@ -313,6 +315,24 @@ class Context:
         self._ck(self.L.shci_pt2_dtm(self.h, energy_var, eps_pt_dtm, n_batches, ctypes.byref(v),
                                      ctypes.byref(u), ctypes.byref(n)))
         return v.value, u.value, n.value
+
+    def pt2_psto(self, energy_var, eps_pt_dtm, eps_pt_psto, n_batches=16, target_error=5e-5,
+                 eps_pt=0.0):
+        v, u, n, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t(), ctypes.c_size_t()
+        self._ck(self.L.shci_pt2_psto(self.h, energy_var, eps_pt_dtm, eps_pt_psto, n_batches,
+                                      target_error, eps_pt, ctypes.byref(v), ctypes.byref(u),
+                                      ctypes.byref(n), ctypes.byref(b)))
+        return v.value, u.value, n.value, b.value
+
+    def pt2_sto(self, energy_var, eps_pt_psto, eps_pt, n_batches, n_samples, seed=347634253,
+                max_iter=100, target_error=5e-5, psto_uncert=0.0, semisto=False):
+        v, u, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
+        loops = np.zeros(max_iter)
+        self._ck(self.L.shci_pt2_sto(self.h, energy_var, eps_pt_psto, eps_pt, n_batches,
+                                     n_samples, int(semisto), seed, max_iter, target_error,
+                                     psto_uncert, ctypes.byref(v), ctypes.byref(u),
+                                     ctypes.byref(n), loops, max_iter))
+        return v.value, u.value, loops[: n.value]
 
     def stream(self):
         return self.L.shci_stream(self.h)

@@ -546,4 +546,40 @@ shci_status shci_pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size
   });
 }
 
+shci_status shci_pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
+                          size_t n_batches, double target_error, double eps_pt,
+                          double* correction, double* uncert, size_t* n_pt_dets,
+                          size_t* n_batches_done) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    auto r = pt2_psto(c, energy_var, eps_pt_dtm, eps_pt_psto, n_batches, target_error, eps_pt);
+    if (correction) *correction = r.value;
+    if (uncert) *uncert = r.uncert;
+    if (n_pt_dets) *n_pt_dets = r.n_pt_dets;
+    if (n_batches_done) *n_batches_done = r.n_batches_done;
+  });
+}
+
+shci_status shci_pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
+                         size_t n_batches, size_t n_dets_in_sample, int semisto,
+                         unsigned random_seed, size_t max_iterations, double target_error,
+                         double psto_uncert, double* correction, double* uncert,
+                         size_t* n_iterations, double* loops, size_t cap) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    std::vector<double> lv;
+    auto r = pt2_sto(c, energy_var, eps_pt_psto, eps_pt, n_batches, n_dets_in_sample,
+                     semisto != 0, random_seed, max_iterations, target_error, psto_uncert, &lv);
+    if (correction) *correction = r.value;
+    if (uncert) *uncert = r.uncert;
+    if (n_iterations) *n_iterations = r.n_batches_done;
+    if (loops)
+      for (size_t k = 0; k < lv.size() && k < cap; k++) loops[k] = lv[k];
+  });
+}
+
 }  // extern "C"

@@ -48,15 +48,23 @@ void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs
 size_t select_dets(shci_ctx* c, double eps_var, bool var_sd);
 void rebuild_det_set(shci_ctx* c);
 size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, size_t m,
-                         DevBuf<double>* vals = nullptr);
-void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const double* v, size_t m,
-                   DevBuf<uint64_t>& oa, DevBuf<uint64_t>& ob, DevBuf<double>* ov, size_t* n_out);
+                         DevBuf<double>* vals = nullptr, int n_vals = 1, int a_bits = 0);
+void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const double* const* v,
+                   int n_vals, size_t m, DevBuf<uint64_t>& oa, DevBuf<uint64_t>& ob,
+                   DevBuf<double>* ov, size_t* n_out);
 
 // pt2.cu
 struct Pt2Out {
   double value = 0.0, uncert = 0.0;
   size_t n_pt_dets = 0;
+  size_t n_batches_done = 0;  // batches (dtm / psto) or iterations (sto) computed
 };
 Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches);
+Pt2Out pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
+                size_t n_batches, double target_error, double eps_pt);
+Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
+               size_t n_batches, size_t n_dets_in_sample, bool semisto, unsigned random_seed,
+               size_t max_iterations, double target_error, double psto_uncert,
+               std::vector<double>* loops);
 
 }  // namespace shci

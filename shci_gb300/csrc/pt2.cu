@@ -1,14 +1,26 @@
-// Deterministic Epstein-Nesbet PT2 (K6 in PT mode + K7).
+// Epstein-Nesbet PT2 on the device: deterministic, pseudo-stochastic and stochastic stages
+// (K6 in PT mode + K7).
 //
-// Reference: Solver<S>::get_energy_pt_dtm (src/solver/solver.h:636-764) and mapreduce_sum
-// (:1155-1177).  For batch b of n_batches, every var det i emits the connected dets a
-// (heat-bath window [eps_pt_dtm / |c_i|, INF)) with rehash(DetHasher(a)) % n_batches == b,
-// a not variational, and |H_ai c_i| >= eps_pt_dtm, as (a, H_ai c_i) pairs.  The reference
-// accumulates them in a distributed hash map; here the pairs are compacted, radix-sorted by
-// det and reduced by key (a fixed-order segmented sum), and a second kernel forms
-// (sum_i H_ai c_i)^2 / (E_var - H_aa) per unique a and reduces the contributions and their
-// squares in a fixed order.
+// Reference: Solver<S>::get_energy_pt_dtm / _psto / _sto (src/solver/solver.h:636-1153) and
+// mapreduce_sum (:1155-1177).  Each stage visits source dets i (all var dets, or a stochastic
+// sample) and emits the connected dets a in the heat-bath window [eps / |c_i|, INF) that fall
+// in the current hash batch (rehash(DetHasher(a)) % n_batches), are not variational and have
+// |H_ai c_i| >= eps.  The reference accumulates (a -> sum) in a distributed hash map; here
+// the (a, values) pairs are compacted, radix-sorted by det and reduced by key in a fixed
+// order, and a second kernel forms each unique a's contribution with its diagonal H_aa.
+//   dtm : value  = H_ai c_i                          contribution S0^2 / (E - H_aa)
+//   psto: values = [hc, hc if |hc| >= eps_dtm]      contribution (S0^2 - S1^2) / (E - H_aa)
+//   sto : values = the five sums of solver.h:1093-1103, contribution of :1117-1124
+// Stochastic iterations are independent: the host draws every iteration's sample with the
+// reference's generator and distributions (std::default_random_engine, alias tables of
+// src/util.cc:128-175), a chunk of iterations is processed in one device pass with the
+// iteration index stored above the orbital bits of the key, and the reference's stopping
+// rules are then applied iteration by iteration.
 #include <cmath>
+#include <numeric>
+#include <random>
+#include <stack>
+#include <unordered_map>
 
 #include "ctx.h"
 #include "heatbath.cuh"
@@ -19,14 +31,41 @@ namespace shci {
 namespace {
 
 constexpr int kPtWarps = 8;
+enum : int { kDtm = 0, kPsto = 1, kSto = 2 };
 
+struct PtParams {
+  double eps;        // emission threshold |H_ai c_i| >= eps (and window eps / |c_i|)
+  double eps_dtm;    // psto: second column threshold
+  double eps_psto;   // sto: column split threshold
+  uint64_t n_batches;
+  uint64_t batch;    // dtm / psto: the batch being computed
+  double factor;     // sto: 1 / (n_samples - n_dtm - 1)
+  int iter_shift;    // sto: bit position of the iteration index in the emitted up key
+};
+
+// Stochastic sources: entry k = (det, iteration, count, weight, batch, deterministic?)
+struct StoSources {
+  const uint32_t* det;
+  const uint32_t* iter;
+  const double* count;
+  const double* weight;
+  const uint32_t* batch;
+  const uint8_t* is_dtm;
+};
+
+__device__ __forceinline__ uint32_t src_det(const StoSources& S, uint32_t k, int mode) {
+  return mode == kSto ? S.det[k] : k;
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32)
-    k_pt_count(SelParams P, double eps_pt, uint32_t n_src, uint64_t* cnt_out) {
+    k_pt_count(SelParams P, PtParams Q, StoSources S, uint32_t n_src, uint64_t* cnt_out) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t wpg = gridDim.x * kPtWarps;
-  for (uint32_t i = blockIdx.x * kPtWarps + (threadIdx.x >> 5); i < n_src; i += wpg) {
+  for (uint32_t k = blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < n_src; k += wpg) {
+    const uint32_t i = src_det(S, k, MODE);
     const double ac = fabs(P.coef[i]);
-    const double eps_min = eps_pt / ac;
+    const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
     const int n_slots = P.n_elecs + P.n_pairs;
@@ -39,23 +78,39 @@ __global__ void __launch_bounds__(kPtWarps * 32)
       for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(kFull, cc, o);
       tot += cc;
     }
-    if (lane == 0) cnt_out[i] = tot;
+    if (lane == 0) cnt_out[k] = tot;
   }
 }
 
+struct OutCols {
+  double* v[5];
+};
+
+template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32)
-    k_pt_emit(SelParams P, double eps_pt, uint64_t n_batches, uint64_t batch, uint32_t k_begin,
-              uint32_t k_end, const uint64_t* off, uint64_t* out_up, uint64_t* out_dn,
-              double* out_v) {
+    k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
+              const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t wpg = gridDim.x * kPtWarps;
-  for (uint32_t i = k_begin + blockIdx.x * kPtWarps + (threadIdx.x >> 5); i < k_end; i += wpg) {
+  for (uint32_t k = k_begin + blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < k_end; k += wpg) {
+    const uint32_t i = src_det(S, k, MODE);
     const double coef = P.coef[i];
     const double ac = fabs(coef);
-    const double eps_min = eps_pt / ac;
+    const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
-    uint64_t base = off[i - k_begin];
+    uint64_t batch = Q.batch;
+    double count = 1.0, weight = 1.0;
+    bool dtm_src = true;
+    uint64_t iter_tag = 0;
+    if (MODE == kSto) {
+      batch = S.batch[k];
+      dtm_src = S.is_dtm[k] != 0;
+      count = dtm_src ? 1.0 : S.count[k];
+      weight = dtm_src ? 1.0 : S.weight[k];
+      iter_tag = static_cast<uint64_t>(S.iter[k]) << Q.iter_shift;
+    }
+    uint64_t base = off[k - k_begin];
     const int n_slots = P.n_elecs + P.n_pairs;
     for (int s0 = 0; s0 < n_slots; s0 += 32) {
       const int slot = s0 + lane;
@@ -86,75 +141,132 @@ __global__ void __launch_bounds__(kPtWarps * 32)
         bool ok = make_candidate(P, up, dn, s0 + (int)ol, e, &cu, &cd, &single);
         double hc = 0.0;
         // handler order of solver.h:703-713: batch, variational set, |H_ai c_i|
-        if (ok && rehash(det_hash(cu, cd)) % n_batches != batch) ok = false;
+        if (ok && rehash(det_hash(cu, cd)) % Q.n_batches != batch) ok = false;
         if (ok && in_set(P, cu, cd)) ok = false;
         if (ok) {
-          const double h = h_offdiag(P.I, up, dn, cu, cd);
-          hc = h * coef;
-          if (fabs(hc) < eps_pt) ok = false;
+          hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
+          if (fabs(hc) < Q.eps) ok = false;
         }
-        out_up[base + t] = ok ? cu : kInvalid;
-        out_dn[base + t] = ok ? cd : kInvalid;
-        out_v[base + t] = hc;
+        const uint64_t pos = base + t;
+        out_up[pos] = ok ? (cu | iter_tag) : kInvalid;
+        out_dn[pos] = ok ? cd : kInvalid;
+        if (MODE == kDtm) {
+          out.v[0][pos] = hc;
+        } else if (MODE == kPsto) {
+          out.v[0][pos] = hc;
+          out.v[1][pos] = fabs(hc) >= Q.eps_dtm ? hc : 0.0;
+        } else {
+          // solver.h:1093-1103
+          const double x = count * hc / weight;
+          const bool above = fabs(hc) > Q.eps_psto;
+          double v2 = 0.0, v3 = 0.0, v4 = 0.0;
+          if (!dtm_src) {
+            v2 = count * hc / weight * sqrt(Q.factor);
+            if (above) v3 = v2;
+            else v4 = x * x * (1. - weight / count + Q.factor);
+          }
+          out.v[0][pos] = x;
+          out.v[1][pos] = above ? x : 0.0;
+          out.v[2][pos] = v2;
+          out.v[3][pos] = v3;
+          out.v[4][pos] = v4;
+        }
       }
       base += total;
     }
   }
 }
 
-// Per unique PT det: x = S^2 / (E_var - H_aa); partial sums of x and x^2 per block.
-__global__ void __launch_bounds__(256)
-    k_pt_contrib(DevIntegrals I, const uint64_t* au, const uint64_t* ad, const double* S,
-                 size_t m, double e_var, double* partial) {
-  double sx = 0.0, sxx = 0.0;
+// x[k] = contribution of unique PT det k (mapper of solver.h:727-732, 856-862, 1117-1124)
+template <int MODE>
+__global__ void k_pt_x(DevIntegrals I, const uint64_t* au, const uint64_t* ad, OutCols S,
+                       size_t m, double e_var, double n_batches, uint64_t orb_mask, double* x) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m;
        k += (size_t)gridDim.x * blockDim.x) {
-    const double haa = h_diag(I, au[k], ad[k]);
-    const double x = S[k] * S[k] / (e_var - haa);
-    sx += x;
-    sxx += x * x;
-  }
-  __shared__ double s1[8], s2[8];
-#pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    sx += __shfl_xor_sync(kFull, sx, o);
-    sxx += __shfl_xor_sync(kFull, sxx, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s1[threadIdx.x >> 5] = sx;
-    s2[threadIdx.x >> 5] = sxx;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < 8; w++) {
-      a += s1[w];
-      b += s2[w];
+    const double haa = h_diag(I, au[k] & orb_mask, ad[k]);
+    double v;
+    if (MODE == kDtm) {
+      v = S.v[0][k] * S.v[0][k] / (e_var - haa);
+    } else if (MODE == kPsto) {
+      const double d = S.v[0][k] * S.v[0][k] - S.v[1][k] * S.v[1][k];
+      v = d / (e_var - haa);
+    } else {
+      const double f = n_batches / (e_var - haa);
+      v = (S.v[0][k] * S.v[0][k] - S.v[1][k] * S.v[1][k] + S.v[2][k] * S.v[2][k] -
+           S.v[3][k] * S.v[3][k] - S.v[4][k]) * f;
     }
-    partial[2 * blockIdx.x] = a;
-    partial[2 * blockIdx.x + 1] = b;
+    x[k] = v;
   }
 }
 
-}  // namespace
+// One block per segment [starts[g], starts[g+1]): out[2g] = sum x, out[2g+1] = sum x^2,
+// reduced in a fixed order.
+__global__ void __launch_bounds__(256)
+    k_seg_reduce2(const double* x, const uint64_t* starts, size_t nseg, double* out) {
+  __shared__ double s1[8], s2[8];
+  for (size_t g = blockIdx.x; g < nseg; g += gridDim.x) {
+    double a = 0.0, b = 0.0;
+    for (uint64_t k = starts[g] + threadIdx.x; k < starts[g + 1]; k += blockDim.x) {
+      a += x[k];
+      b += x[k] * x[k];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      a += __shfl_xor_sync(kFull, a, o);
+      b += __shfl_xor_sync(kFull, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      s1[threadIdx.x >> 5] = a;
+      s2[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int w = 0; w < 8; w++) {
+        ta += s1[w];
+        tb += s2[w];
+      }
+      out[2 * g] = ta;
+      out[2 * g + 1] = tb;
+    }
+    __syncthreads();
+  }
+}
 
-Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) {
+// starts[it] = first k with (au[k] >> shift) >= it, for it = 0..n_it (au sorted ascending)
+__global__ void k_iter_starts(const uint64_t* au, size_t m, int shift, uint32_t n_it,
+                              uint64_t* starts) {
+  const uint32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it > n_it) return;
+  size_t lo = 0, hi = m;
+  while (lo < hi) {
+    const size_t mid = (lo + hi) >> 1;
+    if ((au[mid] >> shift) < it) lo = mid + 1;
+    else hi = mid;
+  }
+  starts[it] = lo;
+}
+
+struct PtSetup {
+  SelParams P{};
+  DevBuf<uint32_t> pairs;
+  unsigned grid = 0;
+};
+
+void pt_setup(shci_ctx* c, PtSetup& st) {
   if (!c->Q.built) throw ArgError("heat-bath queues not built (call shci_build_queues)");
-  if (n_batches == 0) throw ArgError("n_batches must be >= 1");
   sync_dets(c);
   cudaStream_t s = c->stream;
-  const size_t n_var = c->up.size();
   const int n_elecs = static_cast<int>(c->I.n_up + c->I.n_dn);
   rebuild_det_set(c);
   std::vector<uint32_t> pairs;
   for (int a = 0; a < n_elecs; a++)
     for (int b = a + 1; b < n_elecs; b++) pairs.push_back(a | (b << 16));
-  DevBuf<uint32_t> d_pairs;
-  d_pairs.mt = &c->mem;
-  d_pairs.resize(pairs.empty() ? 1 : pairs.size());
+  st.pairs.mt = &c->mem;
+  st.pairs.resize(pairs.empty() ? 1 : pairs.size());
   if (!pairs.empty())
-    SHCI_CUDA(cudaMemcpyAsync(d_pairs.p, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, s));
-  SelParams P{};
+    SHCI_CUDA(cudaMemcpyAsync(st.pairs.p, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, s));
+  SelParams& P = st.P;
   P.I = c->dI;
   P.up = c->d_up.p;
   P.dn = c->d_dn.p;
@@ -165,7 +277,7 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
   P.s_off = c->Q.s_off.p;
   P.s_S = c->Q.s_S.p;
   P.s_r = c->Q.s_r.p;
-  P.pair_tab = d_pairs.p;
+  P.pair_tab = st.pairs.p;
   P.set_up = c->set_up.p;
   P.set_dn = c->set_dn.p;
   P.set_n = static_cast<uint32_t>(c->set_up.n);
@@ -175,86 +287,152 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
   P.n_up = static_cast<int>(c->I.n_up);
   P.n_elecs = n_elecs;
   P.n_pairs = static_cast<int>(pairs.size());
-
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-  const unsigned grid = static_cast<unsigned>(sms) * 8u;
-  DevBuf<uint64_t> cnt, cu, cd, bu, bd;
-  DevBuf<double> cv, bv, partial;
-  cnt.mt = cu.mt = cd.mt = bu.mt = bd.mt = &c->mem;
-  cv.mt = bv.mt = partial.mt = &c->mem;
-  cnt.resize(n_var ? n_var : 1);
-  k_pt_count<<<grid, kPtWarps * 32, 0, s>>>(P, eps_pt, (uint32_t)n_var, cnt.p);
-  SHCI_LAUNCH_CHECK();
-  std::vector<uint64_t> hc(n_var);
-  SHCI_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_var * 8, cudaMemcpyDeviceToHost, s));
-  SHCI_CUDA(cudaStreamSynchronize(s));
-  c->launches += 1;
+  st.grid = static_cast<unsigned>(sms) * 8u;
+}
+
+template <int MODE>
+constexpr int n_cols() {
+  return MODE == kDtm ? 1 : MODE == kPsto ? 2 : 5;
+}
+
+// Emits and reduces the pairs of the sources [0, n_src) for one (batch / set of iterations);
+// returns the unique count, keys in (bu, bd) and value columns in bv[0..n_cols).
+template <int MODE>
+size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
+                      uint32_t n_src, const std::vector<uint64_t>& hc, DevBuf<uint64_t>& bu,
+                      DevBuf<uint64_t>& bd, DevBuf<double>* bv, int a_bits) {
+  constexpr int NV = n_cols<MODE>();
+  cudaStream_t s = c->stream;
   const uint64_t kCap = 1ull << 27;
-  const unsigned cgrid = static_cast<unsigned>(sms) * 4u;
-  partial.resize(2 * cgrid);
+  DevBuf<uint64_t> cu, cd;
+  DevBuf<double> cv[NV];
+  cu.mt = cd.mt = &c->mem;
+  for (int v = 0; v < NV; v++) cv[v].mt = &c->mem;
+  size_t bn = 0;
+  uint32_t k0 = 0;
+  while (k0 < n_src) {
+    uint64_t tot = 0;
+    uint32_t k1 = k0;
+    while (k1 < n_src && (k1 == k0 || tot + hc[k1] <= kCap)) tot += hc[k1++];
+    if (tot > 0) {
+      std::vector<uint64_t> off(k1 - k0);
+      uint64_t acc = 0;
+      for (uint32_t k = k0; k < k1; k++) {
+        off[k - k0] = acc;
+        acc += hc[k];
+      }
+      DevBuf<uint64_t> d_off;
+      d_off.mt = &c->mem;
+      d_off.resize(off.size());
+      SHCI_CUDA(cudaMemcpyAsync(d_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
+      cu.resize(tot, 1.25);
+      cd.resize(tot, 1.25);
+      OutCols oc{};
+      const double* vptr[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+      for (int v = 0; v < NV; v++) {
+        cv[v].resize(tot, 1.25);
+        oc.v[v] = cv[v].p;
+        vptr[v] = cv[v].p;
+      }
+      {
+        ProfScope ps(c->prof, s, "pt2_emit");
+        k_pt_emit<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, k0, k1, d_off.p, cu.p,
+                                                          cd.p, oc);
+        SHCI_LAUNCH_CHECK();
+      }
+      c->launches += 1;
+      compact_valid(c, cu.p, cd.p, vptr, NV, tot, bu, bd, bv, &bn);
+      if (bn > kCap) {  // keep the accumulation buffer bounded
+        bn = sort_unique_pairs(c, bu, bd, bn, bv, NV, a_bits);
+        bu.n = bd.n = bn;
+      }
+    }
+    k0 = k1;
+  }
+  {
+    ProfScope ps(c->prof, s, "pt2_reduce");
+    bn = sort_unique_pairs(c, bu, bd, bn, bv, NV, a_bits);
+  }
+  bu.n = bd.n = bn;
+  return bn;
+}
+
+template <int MODE>
+std::vector<uint64_t> pt_counts(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
+                                uint32_t n_src) {
+  cudaStream_t s = c->stream;
+  DevBuf<uint64_t> cnt;
+  cnt.mt = &c->mem;
+  cnt.resize(n_src ? n_src : 1);
+  std::vector<uint64_t> hc(n_src);
+  if (n_src) {
+    k_pt_count<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, n_src, cnt.p);
+    SHCI_LAUNCH_CHECK();
+    SHCI_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_src * 8, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    c->launches += 1;
+  }
+  return hc;
+}
+
+// Sum and sum of squares of the contributions of one reduced batch (dtm / psto).
+template <int MODE>
+void pt_batch_sums(shci_ctx* c, DevBuf<uint64_t>& bu, DevBuf<uint64_t>& bd, DevBuf<double>* bv,
+                   size_t bn, double e_var, double* sum, double* sumsq) {
+  *sum = *sumsq = 0.0;
+  if (!bn) return;
+  cudaStream_t s = c->stream;
+  DevBuf<double> x, out;
+  DevBuf<uint64_t> starts;
+  x.mt = out.mt = starts.mt = &c->mem;
+  x.resize(bn);
+  out.resize(2);
+  starts.resize(2);
+  OutCols oc{};
+  for (int v = 0; v < n_cols<MODE>(); v++) oc.v[v] = bv[v].p;
+  {
+    ProfScope ps(c->prof, s, "pt2_contrib");
+    k_pt_x<MODE><<<grid_for(bn, 256), 256, 0, s>>>(c->dI, bu.p, bd.p, oc, bn, e_var, 1.0, ~0ull,
+                                                   x.p);
+    SHCI_LAUNCH_CHECK();
+    const uint64_t st2[2] = {0, bn};
+    SHCI_CUDA(cudaMemcpyAsync(starts.p, st2, 16, cudaMemcpyHostToDevice, s));
+    k_seg_reduce2<<<1, 256, 0, s>>>(x.p, starts.p, 1, out.p);
+    SHCI_LAUNCH_CHECK();
+  }
+  double h[2];
+  SHCI_CUDA(cudaMemcpyAsync(h, out.p, 16, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  *sum = h[0];
+  *sumsq = h[1];
+  c->launches += 2;
+}
+
+// Deterministic-style batched stage (dtm: MODE kDtm, psto: kPsto) with the batch accumulation,
+// uncertainty and (psto) early stopping of solver.h:691-764, 818-895.
+template <int MODE>
+Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, double target_error,
+                  double eps_pt) {
+  PtSetup st;
+  pt_setup(c, st);
+  const uint32_t n_var = static_cast<uint32_t>(c->up.size());
+  StoSources S{};
+  Q.n_batches = n_batches;
+  const std::vector<uint64_t> hc = pt_counts<MODE>(c, st, Q, S, n_var);
   Pt2Out out;
   double esum = 0.0, esq = 0.0;
   size_t n_sum = 0;
+  DevBuf<uint64_t> bu, bd;
+  DevBuf<double> bv[2];
+  bu.mt = bd.mt = bv[0].mt = bv[1].mt = &c->mem;
   for (size_t batch = 0; batch < n_batches; batch++) {
-    size_t bn = 0;
-    uint32_t k0 = 0;
-    while (k0 < n_var) {
-      uint64_t tot = 0;
-      uint32_t k1 = k0;
-      while (k1 < n_var && (k1 == k0 || tot + hc[k1] <= kCap)) tot += hc[k1++];
-      if (tot > 0) {
-        std::vector<uint64_t> off(k1 - k0);
-        uint64_t acc = 0;
-        for (uint32_t k = k0; k < k1; k++) {
-          off[k - k0] = acc;
-          acc += hc[k];
-        }
-        DevBuf<uint64_t> d_off;
-        d_off.mt = &c->mem;
-        d_off.resize(off.size());
-        SHCI_CUDA(cudaMemcpyAsync(d_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
-        cu.resize(tot, 1.25);
-        cd.resize(tot, 1.25);
-        cv.resize(tot, 1.25);
-        {
-          ProfScope ps(c->prof, s, "pt2_emit");
-          k_pt_emit<<<grid, kPtWarps * 32, 0, s>>>(P, eps_pt, n_batches, batch, k0, k1, d_off.p,
-                                                   cu.p, cd.p, cv.p);
-          SHCI_LAUNCH_CHECK();
-        }
-        c->launches += 1;
-        compact_valid(c, cu.p, cd.p, cv.p, tot, bu, bd, &bv, &bn);
-        // keep the batch buffer bounded: reduce by key when it grows large
-        if (bn > kCap) {
-          bn = sort_unique_pairs(c, bu, bd, bn, &bv);
-          bu.n = bd.n = bv.n = bn;
-        }
-      }
-      k0 = k1;
-    }
-    {
-      ProfScope ps(c->prof, s, "pt2_reduce");
-      bn = sort_unique_pairs(c, bu, bd, bn, &bv);
-    }
-    bu.n = bd.n = bv.n = bn;
-    double bs = 0.0, bsq = 0.0;
-    if (bn) {
-      {
-        ProfScope ps(c->prof, s, "pt2_contrib");
-        k_pt_contrib<<<cgrid, 256, 0, s>>>(c->dI, bu.p, bd.p, bv.p, bn, energy_var, partial.p);
-        SHCI_LAUNCH_CHECK();
-      }
-      std::vector<double> hp(2 * cgrid);
-      SHCI_CUDA(cudaMemcpyAsync(hp.data(), partial.p, hp.size() * 8, cudaMemcpyDeviceToHost, s));
-      SHCI_CUDA(cudaStreamSynchronize(s));
-      for (unsigned b = 0; b < cgrid; b++) {
-        bs += hp[2 * b];
-        bsq += hp[2 * b + 1];
-      }
-      c->launches += 1;
-    }
-    // batch accumulation and uncertainty as solver.h:733-743
+    Q.batch = batch;
+    bu.n = bd.n = 0;
+    const size_t bn = pt_emit_reduce<MODE>(c, st, Q, S, n_var, hc, bu, bd, bv, 0);
+    double bs, bsq;
+    pt_batch_sums<MODE>(c, bu, bd, bv, bn, e_var, &bs, &bsq);
     n_sum += bn;
     esum += bs;
     esq += bsq;
@@ -264,10 +442,224 @@ Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt, size_t n_batches) 
     } else {
       const double avg = esum / n_sum;
       const double sd = std::sqrt(esq / n_sum - avg * avg);
-      out.uncert = sd * std::sqrt((double)n_sum) / (batch + 1) * (n_batches - batch - 1);
+      if (MODE == kDtm) {
+        out.uncert = sd * std::sqrt((double)n_sum) / (batch + 1) * (n_batches - batch - 1);
+      } else {
+        const double mean_sd = sd / std::sqrt((double)n_sum);
+        out.uncert = mean_sd * n_sum / (batch + 1) * (n_batches - batch - 1);
+      }
+    }
+    out.n_batches_done = batch + 1;
+    if (MODE == kPsto) {
+      if (out.uncert <= target_error * 0.5) break;
+      if (Q.eps <= eps_pt && out.uncert <= target_error) break;
     }
   }
   out.n_pt_dets = n_sum;
+  c->prof.flush();
+  return out;
+}
+
+// Vose alias tables, as src/util.cc:128-175.
+void alias_tables(const std::vector<double>& p, std::vector<double>& np, std::vector<size_t>& al) {
+  const size_t L = p.size();
+  np.assign(L, 0.0);
+  al.assign(L, 0);
+  std::vector<double> t(L);
+  std::stack<size_t> small, large;
+  for (size_t i = 0; i < L; i++) {
+    t[i] = p[i] * L;
+    if (t[i] < 1.) small.push(i);
+    else large.push(i);
+  }
+  while (!small.empty() && !large.empty()) {
+    const size_t l = large.top(), s = small.top();
+    np[s] = t[s];
+    al[s] = l;
+    t[l] = t[l] + t[s] - 1.;
+    if (t[l] < 1.) {
+      large.pop();
+      small.top() = l;
+    } else {
+      small.pop();
+    }
+  }
+  while (!large.empty()) {
+    np[large.top()] = 1.;
+    large.pop();
+  }
+  while (!small.empty()) {
+    np[small.top()] = 1.;
+    small.pop();
+  }
+}
+
+}  // namespace
+
+Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches) {
+  if (n_batches == 0) throw ArgError("n_batches must be >= 1");
+  PtParams Q{};
+  Q.eps = eps_pt_dtm;
+  return pt_batched<kDtm>(c, energy_var, Q, n_batches, 0.0, 0.0);
+}
+
+Pt2Out pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
+                size_t n_batches, double target_error, double eps_pt) {
+  if (n_batches == 0) throw ArgError("n_batches must be >= 1");
+  PtParams Q{};
+  Q.eps = eps_pt_psto;
+  Q.eps_dtm = eps_pt_dtm;
+  return pt_batched<kPsto>(c, energy_var, Q, n_batches, target_error, eps_pt);
+}
+
+// Stochastic stage (solver.h:898-1153) with n_dets_in_sample given.  psto_uncert is the
+// uncertainty of the preceding stage (it enters the second stopping rule).
+Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
+               size_t n_batches, size_t n_dets_in_sample, bool semisto, unsigned random_seed,
+               size_t max_iterations, double target_error, double psto_uncert,
+               std::vector<double>* loops) {
+  if (n_batches == 0) throw ArgError("n_batches must be >= 1");
+  if (n_dets_in_sample < 2) throw ArgError("n_dets_in_sample_pt_sto must be given (>= 2)");
+  if (semisto)
+    throw ArgError("semisto_sto with n_dets_in_sample_pt_sto set has no deterministic dets in "
+                   "the reference (its 25% quantile heap is empty: solver.h:1009-1021); set "
+                   "semisto_sto to false");
+  const size_t n_var = c->up.size();
+  std::vector<double> coefs(n_var);
+  sync_dets(c);
+  cudaStream_t s = c->stream;
+  SHCI_CUDA(cudaMemcpyAsync(coefs.data(), c->d_coef.p, n_var * 8, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  // probabilities (solver.h:921-933)
+  double sum_w = 0.0;
+  for (size_t i = 0; i < n_var; i++) sum_w += std::abs(coefs[i]);
+  std::vector<double> probs(n_var);
+  for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(coefs[i]) / sum_w;
+  std::default_random_engine gen(random_seed);
+  std::uniform_real_distribution<double> ur(0., 1.);
+  const size_t n_dtm = 0;
+  std::vector<double> aprob;
+  std::vector<size_t> alias;
+  alias_tables(probs, aprob, alias);
+  std::uniform_int_distribution<size_t> ui_var(0, n_var - 1);
+  std::uniform_int_distribution<size_t> ui_batch(0, n_batches - 1);
+  const double factor = 1. / (n_dets_in_sample - n_dtm - 1.);
+  const int shift = c->I.n;
+  if (shift > 57) throw ArgError("stochastic PT2 supports n_orbs <= 57");
+  const uint32_t kIterChunk = 16;
+
+  PtSetup st;
+  pt_setup(c, st);
+  Pt2Out out;
+  std::vector<double> loop_vals;
+  bool done = false;
+  size_t iteration = 0;
+  while (!done && iteration < max_iterations) {
+    // draw the samples of the next chunk of iterations (solver.h:1048-1072)
+    const uint32_t n_it = static_cast<uint32_t>(std::min<size_t>(kIterChunk, max_iterations - iteration));
+    std::vector<uint32_t> h_det, h_iter, h_batch;
+    std::vector<double> h_count, h_weight;
+    std::vector<uint8_t> h_dtm;
+    for (uint32_t it = 0; it < n_it; it++) {
+      std::unordered_map<size_t, unsigned> cnt;
+      std::vector<size_t> list;
+      for (size_t k = 0; k < n_dets_in_sample - n_dtm; k++) {
+        const size_t r1 = ui_var(gen);
+        const double r2 = ur(gen);
+        const size_t id = r2 < aprob[r1] ? r1 : alias[r1];
+        if (cnt.count(id) == 0) list.push_back(id);
+        cnt[id]++;
+      }
+      const size_t batch_id = ui_batch(gen);
+      for (size_t k = 0; k < list.size(); k++) {
+        const size_t i = list[k];
+        h_det.push_back(static_cast<uint32_t>(i));
+        h_iter.push_back(it);
+        h_batch.push_back(static_cast<uint32_t>(batch_id));
+        h_count.push_back(static_cast<double>(cnt[i]));
+        h_weight.push_back((n_dets_in_sample - n_dtm) * probs[i]);
+        h_dtm.push_back(k < n_dtm ? 1 : 0);
+      }
+    }
+    const uint32_t n_src = static_cast<uint32_t>(h_det.size());
+    DevBuf<uint32_t> d_det, d_iter, d_batch;
+    DevBuf<double> d_count, d_weight;
+    DevBuf<uint8_t> d_dtm;
+    d_det.mt = d_iter.mt = d_batch.mt = d_count.mt = d_weight.mt = d_dtm.mt = &c->mem;
+    d_det.resize(n_src);
+    d_iter.resize(n_src);
+    d_batch.resize(n_src);
+    d_count.resize(n_src);
+    d_weight.resize(n_src);
+    d_dtm.resize(n_src);
+    SHCI_CUDA(cudaMemcpyAsync(d_det.p, h_det.data(), n_src * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_iter.p, h_iter.data(), n_src * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_batch.p, h_batch.data(), n_src * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_count.p, h_count.data(), n_src * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_weight.p, h_weight.data(), n_src * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_dtm.p, h_dtm.data(), n_src, cudaMemcpyHostToDevice, s));
+    StoSources S{d_det.p, d_iter.p, d_count.p, d_weight.p, d_batch.p, d_dtm.p};
+    PtParams Q{};
+    Q.eps = eps_pt;
+    Q.eps_psto = eps_pt_psto;
+    Q.n_batches = n_batches;
+    Q.factor = factor;
+    Q.iter_shift = shift;
+    const std::vector<uint64_t> hc = pt_counts<kSto>(c, st, Q, S, n_src);
+    DevBuf<uint64_t> bu, bd;
+    DevBuf<double> bv[5];
+    bu.mt = bd.mt = &c->mem;
+    for (auto& b : bv) b.mt = &c->mem;
+    const size_t bn = pt_emit_reduce<kSto>(c, st, Q, S, n_src, hc, bu, bd, bv, shift + 5);
+    // per-iteration sums of the contributions
+    std::vector<double> it_sum(n_it, 0.0);
+    if (bn) {
+      DevBuf<double> x, o;
+      DevBuf<uint64_t> starts;
+      x.mt = o.mt = starts.mt = &c->mem;
+      x.resize(bn);
+      o.resize(2 * n_it);
+      starts.resize(n_it + 1);
+      OutCols oc{};
+      for (int v = 0; v < 5; v++) oc.v[v] = bv[v].p;
+      const uint64_t mask = shift == 64 ? ~0ull : ((1ull << shift) - 1ull);
+      {
+        ProfScope ps(c->prof, s, "pt2_contrib");
+        k_pt_x<kSto><<<grid_for(bn, 256), 256, 0, s>>>(c->dI, bu.p, bd.p, oc, bn, energy_var,
+                                                       static_cast<double>(n_batches), mask, x.p);
+        SHCI_LAUNCH_CHECK();
+        k_iter_starts<<<1, 128, 0, s>>>(bu.p, bn, shift, n_it, starts.p);
+        SHCI_LAUNCH_CHECK();
+        k_seg_reduce2<<<n_it, 256, 0, s>>>(x.p, starts.p, n_it, o.p);
+        SHCI_LAUNCH_CHECK();
+      }
+      std::vector<double> h(2 * n_it);
+      SHCI_CUDA(cudaMemcpyAsync(h.data(), o.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      for (uint32_t it = 0; it < n_it; it++) it_sum[it] = h[2 * it];
+      c->launches += 3;
+    }
+    out.n_pt_dets += bn;
+    // statistics and stopping rules, iteration by iteration (solver.h:1126-1147)
+    for (uint32_t it = 0; it < n_it && !done; it++) {
+      loop_vals.push_back(it_sum[it]);
+      const double n = static_cast<double>(loop_vals.size());
+      double sm = 0.0, sq = 0.0;
+      for (double v : loop_vals) {
+        sm += v;
+        sq += v * v;
+      }
+      out.value = sm / n;
+      out.uncert = std::sqrt((sq - sm * sm / n) / (n - 1)) / std::sqrt(n);
+      iteration++;
+      if (iteration >= 6 && out.uncert <= target_error * 0.7) done = true;
+      if (iteration >= 10 &&
+          std::sqrt(out.uncert * out.uncert + psto_uncert * psto_uncert) <= target_error)
+        done = true;
+    }
+  }
+  out.n_batches_done = iteration;
+  if (loops) *loops = loop_vals;
   c->prof.flush();
   return out;
 }

@@ -179,11 +179,12 @@ __global__ void k_seg_starts(const uint32_t* flags, const uint32_t* pos, size_t 
 
 }  // namespace
 
-// Sorts (up, dn) pairs held in a / b (length m) into ascending Det order and removes
-// duplicates; returns the unique count (left in a / b).  With vals, the values of equal
-// keys are summed (reduce by key) and left in vals.
+// Sorts (up, dn) pairs held in a / b (length m) into ascending (a, b) order and removes
+// duplicates; returns the unique count (left in a / b).  With vals (n_vals columns), the
+// values of equal keys are summed (reduce by key) and left in the columns.  a_bits = bits
+// of the a key (0: n_orbs); b keys always have n_orbs bits.
 size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, size_t m,
-                         DevBuf<double>* vals) {
+                         DevBuf<double>* vals, int n_vals, int a_bits) {
   if (m == 0) return 0;
   cudaStream_t s = c->stream;
   const int nb = c->I.n;
@@ -197,7 +198,7 @@ size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, 
   iota_u32(c->u0.p, m, s);
   radix_sort_pairs(key, c->u0, m, 0, nb, s, c->sort);
   gather_u64(a.p, c->u0.p, key.p, m, s);
-  radix_sort_pairs(key, c->u0, m, 0, nb, s, c->sort);
+  radix_sort_pairs(key, c->u0, m, 0, a_bits > 0 ? a_bits : nb, s, c->sort);
   // key = sorted ups; gather dns
   DevBuf<uint64_t> sd;
   sd.mt = &c->mem;
@@ -206,7 +207,7 @@ size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, 
   k_unique_flags<<<grid_for(m, 256), 256, 0, s>>>(key.p, sd.p, m, c->u1.p);
   SHCI_LAUNCH_CHECK();
   const uint32_t nu = exclusive_scan_u32(c->u1.p, c->u2.p, m, s, c->sort);
-  if (vals) {
+  if (vals && n_vals > 0) {
     DevBuf<uint32_t> starts;
     starts.mt = &c->mem;
     starts.resize(nu ? nu : 1);
@@ -215,11 +216,13 @@ size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, 
     DevBuf<double> sums;
     sums.mt = &c->mem;
     sums.resize(nu ? nu : 1);
-    k_segsum<<<grid_for(nu, 256), 256, 0, s>>>(starts.p, nu, m, c->u0.p, vals->p, sums.p);
-    SHCI_LAUNCH_CHECK();
-    SHCI_CUDA(cudaMemcpyAsync(vals->p, sums.p, nu * 8, cudaMemcpyDeviceToDevice, s));
+    for (int v = 0; v < n_vals; v++) {
+      k_segsum<<<grid_for(nu, 256), 256, 0, s>>>(starts.p, nu, m, c->u0.p, vals[v].p, sums.p);
+      SHCI_LAUNCH_CHECK();
+      SHCI_CUDA(cudaMemcpyAsync(vals[v].p, sums.p, nu * 8, cudaMemcpyDeviceToDevice, s));
+    }
     SHCI_CUDA(cudaStreamSynchronize(s));
-    c->launches += 2;
+    c->launches += 1 + n_vals;
   }
   k_compact2<<<grid_for(m, 256), 256, 0, s>>>(key.p, sd.p, c->u1.p, c->u2.p, m, a.p, b.p);
   SHCI_LAUNCH_CHECK();
@@ -228,23 +231,19 @@ size_t sort_unique_pairs(shci_ctx* c, DevBuf<uint64_t>& a, DevBuf<uint64_t>& b, 
 }
 
 namespace {
-__global__ void k_compact3(const uint64_t* a, const uint64_t* b, const double* v,
-                           const uint32_t* flags, const uint32_t* pos, size_t n, uint64_t* oa,
-                           uint64_t* ob, double* ov) {
+__global__ void k_compact_vals(const double* v, const uint32_t* flags, const uint32_t* pos,
+                               size_t n, double* ov) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
-    if (flags[i]) {
-      oa[pos[i]] = a[i];
-      ob[pos[i]] = b[i];
-      ov[pos[i]] = v[i];
-    }
+    if (flags[i]) ov[pos[i]] = v[i];
 }
 }  // namespace
 
-// Appends the entries of (a, b[, v]) whose a != kInvalid to (oa, ob[, ov]) after *n_out
-// (growing them); *n_out is advanced by the number appended.
-void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const double* v, size_t m,
-                   DevBuf<uint64_t>& oa, DevBuf<uint64_t>& ob, DevBuf<double>* ov, size_t* n_out) {
+// Appends the entries of (a, b[, v columns]) whose a != kInvalid to (oa, ob[, ov columns])
+// after *n_out (growing them); *n_out is advanced by the number appended.
+void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const double* const* v,
+                   int n_vals, size_t m, DevBuf<uint64_t>& oa, DevBuf<uint64_t>& ob,
+                   DevBuf<double>* ov, size_t* n_out) {
   if (m == 0) return;
   cudaStream_t s = c->stream;
   c->u1.reserve(m, 1.25);
@@ -258,15 +257,14 @@ void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const doub
   oa.n = ob.n = at;
   oa.grow_keep(at + nv, s);
   ob.grow_keep(at + nv, s);
-  if (ov) {
-    ov->n = at;
-    ov->grow_keep(at + nv, s);
-    k_compact3<<<grid_for(m, 256), 256, 0, s>>>(a, b, v, c->u1.p, c->u2.p, m, oa.p + at,
-                                                ob.p + at, ov->p + at);
-  } else {
-    k_compact2<<<grid_for(m, 256), 256, 0, s>>>(a, b, c->u1.p, c->u2.p, m, oa.p + at, ob.p + at);
-  }
+  k_compact2<<<grid_for(m, 256), 256, 0, s>>>(a, b, c->u1.p, c->u2.p, m, oa.p + at, ob.p + at);
   SHCI_LAUNCH_CHECK();
+  for (int k = 0; k < n_vals && ov; k++) {
+    ov[k].n = at;
+    ov[k].grow_keep(at + nv, s);
+    k_compact_vals<<<grid_for(m, 256), 256, 0, s>>>(v[k], c->u1.p, c->u2.p, m, ov[k].p + at);
+    SHCI_LAUNCH_CHECK();
+  }
   *n_out = at + nv;
 }
 
@@ -381,7 +379,7 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
           }
           // compact valid candidates, then sort + unique
           const size_t before = pass_n;
-          compact_valid(c, cu.p, cd.p, nullptr, tot, pass_up, pass_dn, nullptr, &pass_n);
+          compact_valid(c, cu.p, cd.p, nullptr, 0, tot, pass_up, pass_dn, nullptr, &pass_n);
           if (pass_n > before) {
             pass_n = sort_unique_pairs(c, pass_up, pass_dn, pass_n);
             pass_up.n = pass_dn.n = pass_n;

@@ -70,6 +70,21 @@ def main(ref):
                         "correction": float(m.group(3)),
                         "n_pt_dets": parse_int(nl[-1].split()[-1]) if nl else None})
     pins["pt_dtm"] = dtm
+    # First pseudo-stochastic batch of each eps_var (the log's batch count is 16).
+    psto = []
+    for i, l in enumerate(out):
+        m = re.match(r"PT psto correction \(eps1= (\S+), eps_pt_psto= (\S+)\): (\S+) \+- (\S+)", l)
+        if m:
+            head = out[max(0, i - 12):i]
+            if not any(x.startswith("BEG OF #1/") for x in head):
+                continue
+            nl = [x for x in head if x.startswith("Number of psto pt dets")]
+            nb = [x for x in out[max(0, i - 30):i] if x.startswith("Number of psto batches")]
+            psto.append({"eps_var": float(m.group(1)), "eps_pt_psto": float(m.group(2)),
+                         "correction": float(m.group(3)), "uncert": float(m.group(4)),
+                         "n_pt_dets": parse_int(nl[-1].split()[-1]),
+                         "n_batches": int(nb[-1].split()[-1])})
+    pins["pt_psto_first_batch"] = psto
     json.dump(pins, open(os.path.join(HERE, "c_atom_pins.json"), "w"), indent=1)
 
     dt = open(os.path.join(ref, "src", "solver", "davidson_test.cc")).read()

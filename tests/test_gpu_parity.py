@@ -197,6 +197,42 @@ def test_pt2_dtm_matches_oracle_and_reference(shci, oracle_mod, c_oracle, c_atom
     assert n3 == n and abs(v3 - v) < 1e-12 and u3 == 0.0
 
 
+def test_pt2_psto_matches_oracle_and_reference(shci, c_oracle, c_atom_pins):
+    up, dn, coefs = c_oracle.dets()
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    ev = c_oracle.energy_var
+    pin = [p for p in c_atom_pins["pt_psto_first_batch"] if p["eps_var"] == 5e-5][0]
+    v, u, n, b = c.pt2_psto(ev, 5e-6, pin["eps_pt_psto"], pin["n_batches"], 5e-5, 5e-8)
+    vo, uo, no, bo = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], pin["n_batches"], 5e-5, 5e-8)
+    assert (n, b) == (no, bo) == (pin["n_pt_dets"], 1)
+    assert abs(v - vo) < 1e-13 and abs(u - uo) < 1e-13
+    assert abs(v - pin["correction"]) < 6e-11
+    # all 16 batches (no early stop): extrapolation ends in the exact psto sum
+    v16, u16, n16, b16 = c.pt2_psto(ev, 5e-6, pin["eps_pt_psto"], 16, 0.0, 0.0)
+    vo16, uo16, no16, bo16 = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], 16, 0.0, 0.0)
+    assert b16 == bo16 == 16 and n16 == no16 and u16 == 0.0
+    assert abs(v16 - vo16) < 1e-13
+
+
+def test_pt2_sto_matches_oracle(shci, oracle_mod, w1_fcidump):
+    """Stochastic stage: the host draws the same samples as the reference's generator, so
+    every iteration's estimate equals the oracle's."""
+    o = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    o.run_all_variations([2e-4], [], 5e-5)
+    up, dn, coefs = o.dets()
+    c = new_ctx(shci, w1_fcidump, 5, 5)
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    ev = o.energy_var
+    v, u, loops = c.pt2_sto(ev, 1e-6, 1e-7, 8, 3000, 347634253, 12, 5e-5, 0.0)
+    vo, uo, loops_o = o.pt_sto(1e-6, 1e-7, 8, 3000, 347634253, 12, 5e-5, 0.0)
+    assert len(loops) == len(loops_o) >= 6
+    assert np.max(np.abs(loops - loops_o)) < 1e-14
+    assert abs(v - vo) < 1e-14 and abs(u - uo) < 1e-13
+
+
 def test_mixed_precision_energy(shci, c_ham):
     c, _, _, _, _, up, dn, coefs = c_ham
     c.set_coefs(coefs)

