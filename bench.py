@@ -178,6 +178,48 @@ def workload_name(n):
             % (w["n"], w["n_up"], w["n_dn"], SCHEDULE, EPS_VAR, n))
 
 
+PT2 = {  # workload -> (eps_pt_dtm, eps_pt_psto, eps_pt, psto batches, sto batches, samples)
+    3: (1e-6, 2e-7, 1e-8, 16, 64, 200000),
+    2: (1e-6, 1e-7, 5e-8, 16, 64, 20000),
+    1: (1e-6, 1e-6, 1e-6, 16, 64, 2000),
+}
+
+
+def run_pt2(ctx, stream, e_var):
+    """Solver<S>::run_perturbation's three stages on the context's wavefunction, each timed
+    with CUDA events on the context stream."""
+    import torch
+    eps_dtm, eps_psto, eps_pt, nb_psto, nb_sto, n_samples = PT2[WORKLOAD]
+    out = {"eps_pt_dtm": eps_dtm, "eps_pt_psto": eps_psto, "eps_pt": eps_pt}
+    try:
+        t = []
+        for _ in range(4):
+            ev = torch.cuda.Event(enable_timing=True)
+            t.append(ev)
+        t[0].record(stream)
+        dtm, _, n_dtm = ctx.pt2_dtm(e_var, eps_dtm, 0)
+        t[1].record(stream)
+        psto = (0.0, 0.0, 0, 0)
+        if eps_psto < eps_dtm:
+            psto = ctx.pt2_psto(e_var, eps_dtm, eps_psto, nb_psto, TARGET_ERROR, eps_pt)
+        t[2].record(stream)
+        sto, sto_u, loops = ctx.pt2_sto(e_var, eps_psto, eps_pt, nb_sto, n_samples, 347634253,
+                                        100, TARGET_ERROR, psto[1])
+        t[3].record(stream)
+        torch.cuda.synchronize()
+        ms = [t[k].elapsed_time(t[k + 1]) for k in range(3)]
+        e2 = dtm + psto[0] + sto
+        out.update({"s": sum(ms) / 1e3, "dtm_s": ms[0] / 1e3, "psto_s": ms[1] / 1e3,
+                    "sto_s": ms[2] / 1e3, "n_pt_dets_dtm": n_dtm, "psto_batches": psto[3],
+                    "n_pt_dets_psto": psto[2], "sto_iterations": len(loops),
+                    "sto_batches": nb_sto, "sto_samples": n_samples,
+                    "correction": e2, "uncert": (psto[1] ** 2 + sto_u ** 2) ** 0.5,
+                    "energy_total": e_var + e2})
+    except Exception as e:  # report, do not lose the H-build / Davidson line
+        out["error"] = str(e)
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -231,6 +273,9 @@ def run_ours(args):
         t = torch.tensor([ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
+
+    # PT2 on the step's wavefunction (the metric's "PT2 s"): dtm, psto, sto stages
+    pt2 = run_pt2(ctx, stream, e_mixed) if args.pt2 else None
 
     # all-FP64 form of the same step
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -305,6 +350,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 8},
         "gpu_launches": launches // args.steps,
         "clocks": clk.summary(),
+        "pt2": pt2,
         "fp64": {"ms_per_step": ms_fp64, "energy": e_fp64},
         "energy_mixed_fp64corrected": e_mixed, "energy_davidson_mixed": e_dav,
         "dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
@@ -322,6 +368,8 @@ def main():
     ap.add_argument("--data", default=os.environ.get("SHCI_BENCH_DATA", "/tmp/shci_bench_data"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", type=int, default=3, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-pt2", dest="pt2", action="store_false",
+                    help="skip the PT2 measurement")
     args = ap.parse_args()
     global WORKLOAD, SCHEDULE, EPS_VAR
     WORKLOAD = args.workload

@@ -197,8 +197,9 @@ shci_status shci_profile_get(shci_ctx* ctx, char* names, double* total_ms, uint6
 /* ---- PT2 (Solver<S>::get_energy_pt_dtm, solver.h:636-764) ---------------------------- */
 
 /* Deterministic Epstein-Nesbet PT2 over n_batches hash batches (rehash(DetHasher(a)) %
- * n_batches).  energy_var = E_var of the context's wavefunction.  out: correction, its
- * uncertainty (0 when all batches ran), number of unique PT dets. */
+ * n_batches); n_batches = 0 picks the count from the candidate total and free HBM (the
+ * result does not depend on it).  energy_var = E_var of the context's wavefunction.  out:
+ * correction, its uncertainty (0 when all batches ran), number of unique PT dets. */
 shci_status shci_pt2_dtm(shci_ctx* ctx, double energy_var, double eps_pt_dtm, size_t n_batches,
                          double* correction, double* uncert, size_t* n_pt_dets);
 

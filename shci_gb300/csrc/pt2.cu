@@ -419,8 +419,20 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   pt_setup(c, st);
   const uint32_t n_var = static_cast<uint32_t>(c->up.size());
   StoSources S{};
-  Q.n_batches = n_batches;
   const std::vector<uint64_t> hc = pt_counts<MODE>(c, st, Q, S, n_var);
+  if (n_batches == 0) {
+    // Automatic batch count: every candidate pair costs ~48 device bytes while a batch is
+    // processed (keys, value columns, compaction, sort ping-pong); keep a batch within 40% of
+    // the free HBM.  (The dtm energy does not depend on the batch count.)
+    uint64_t tot = 0;
+    for (uint64_t v : hc) tot += v;
+    size_t free_b = 0, total_b = 0;
+    SHCI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const double per = 48.0 * (MODE == kDtm ? 1.0 : 1.3);
+    n_batches = static_cast<size_t>(std::ceil(tot * per / (0.4 * free_b)));
+    if (n_batches < 1) n_batches = 1;
+  }
+  Q.n_batches = n_batches;
   Pt2Out out;
   double esum = 0.0, esq = 0.0;
   size_t n_sum = 0;
@@ -497,7 +509,6 @@ void alias_tables(const std::vector<double>& p, std::vector<double>& np, std::ve
 }  // namespace
 
 Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches) {
-  if (n_batches == 0) throw ArgError("n_batches must be >= 1");
   PtParams Q{};
   Q.eps = eps_pt_dtm;
   return pt_batched<kDtm>(c, energy_var, Q, n_batches, 0.0, 0.0);
