@@ -226,6 +226,19 @@ shci_status shci_pt2_sto(shci_ctx* ctx, double energy_var, double eps_pt_psto, d
                          double psto_uncert, double* correction, double* uncert,
                          size_t* n_iterations, double* loops, size_t cap);
 
+/* ---- RDMs: the adjoint of E_var (RDM::get_1rdm / get_2rdm, src/chem/rdm.cc) ---------- */
+
+/* 1-RDM of the context's wavefunction: rdm1[p*n + r] = sum_ij c_i c_j <D_i| a+_r a_p |D_j>
+ * summed over spin (rdm.cc:12-131), in the reordered orbital basis. */
+shci_status shci_rdm1(shci_ctx* ctx, double* rdm1);
+
+/* Spatial 2-RDM over the connections of the current Hamiltonian (rdm.cc:333-642), half
+ * stored as the reference does: Gamma(p,q,r,s) = <a+_p a+_q a_r a_s> at index
+ * A(A+1)/2 + B with A = max(p n + s, q n + r), B = min(...) (rdm.cc:233-241, 644-657);
+ * rdm2_half has n^2 (n^2 + 1) / 2 entries.  E_var = E_core + sum_pq h_pq g1_pq +
+ * 1/2 sum_pqrs Gamma(p,q,r,s) (ps|qr), with g1 the 2-RDM contraction (rdm.cc:707-753). */
+shci_status shci_rdm2(shci_ctx* ctx, double* rdm2_half);
+
 #ifdef __cplusplus
 }
 #endif

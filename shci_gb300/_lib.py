@@ -74,6 +74,8 @@ def load():
         "shci_hamiltonian_stats": [vp, _u64p],
         "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
         "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, P(d), P(d), P(sz), _f64p, sz],
+        "shci_rdm1": [vp, _f64p],
+        "shci_rdm2": [vp, _f64p],
         "shci_profile": [vp, i],
         "shci_profile_get": [vp, vp, _f64p, _u64p, sz, P(sz)],
     }
@@ -333,6 +335,18 @@ class Context:
                                      psto_uncert, ctypes.byref(v), ctypes.byref(u),
                                      ctypes.byref(n), loops, max_iter))
         return v.value, u.value, loops[: n.value]
+
+    def rdm1(self):
+        n = self.n_orbs
+        out = np.zeros(n * n)
+        self._ck(self.L.shci_rdm1(self.h, out))
+        return out.reshape(n, n)
+
+    def rdm2_half(self):
+        n = self.n_orbs
+        out = np.zeros(n * n * (n * n + 1) // 2)
+        self._ck(self.L.shci_rdm2(self.h, out))
+        return out
 
     def stream(self):
         return self.L.shci_stream(self.h)

@@ -546,6 +546,24 @@ shci_status shci_pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size
   });
 }
 
+shci_status shci_rdm1(shci_ctx* c, double* out) {
+  if (!c || !out) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    rdm1(c, out);
+  });
+}
+
+shci_status shci_rdm2(shci_ctx* c, double* out_half) {
+  if (!c || !out_half) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    rdm2(c, out_half);
+  });
+}
+
 shci_status shci_pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
                           size_t n_batches, double target_error, double eps_pt,
                           double* correction, double* uncert, size_t* n_pt_dets,

@@ -67,4 +67,8 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
                size_t max_iterations, double target_error, double psto_uncert,
                std::vector<double>* loops);
 
+// rdm.cu
+void rdm1(shci_ctx* c, double* out);       // host [n*n]
+void rdm2(shci_ctx* c, double* out_half);  // host [n^2 (n^2+1) / 2]
+
 }  // namespace shci

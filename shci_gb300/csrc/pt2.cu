@@ -557,7 +557,9 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   const double factor = 1. / (n_dets_in_sample - n_dtm - 1.);
   const int shift = c->I.n;
   if (shift > 57) throw ArgError("stochastic PT2 supports n_orbs <= 57");
-  const uint32_t kIterChunk = 16;
+  // Iterations per device pass: the first pass runs the 6 iterations before which the
+  // stopping rules cannot fire, later passes 2 (results past the stop are discarded).
+  const uint32_t kFirstChunk = 6, kNextChunk = 2;
 
   PtSetup st;
   pt_setup(c, st);
@@ -567,7 +569,8 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   size_t iteration = 0;
   while (!done && iteration < max_iterations) {
     // draw the samples of the next chunk of iterations (solver.h:1048-1072)
-    const uint32_t n_it = static_cast<uint32_t>(std::min<size_t>(kIterChunk, max_iterations - iteration));
+    const uint32_t chunk = iteration == 0 ? kFirstChunk : kNextChunk;
+    const uint32_t n_it = static_cast<uint32_t>(std::min<size_t>(chunk, max_iterations - iteration));
     std::vector<uint32_t> h_det, h_iter, h_batch;
     std::vector<double> h_count, h_weight;
     std::vector<uint8_t> h_dtm;
