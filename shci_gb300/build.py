@@ -65,7 +65,26 @@ def build(verbose=False, jobs=None):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
+    build_cli()
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "main.cc")
+CLI = os.path.join(HERE, "bin", "shci_gpu")
+
+
+def build_cli():
+    """The drop-in driver: links only the C ABI of libshci_gpu.so."""
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    deps = [CLI_SRC, os.path.join(HERE, "cli", "json.h"), LIB]
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(d) for d in deps):
+        return CLI
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"), CLI_SRC,
+           "-o", CLI, "-L", LIBDIR, "-lshci_gpu", "-Wl,-rpath,$ORIGIN/../lib"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed: %s\n%s" % (" ".join(cmd), r.stderr))
+    return CLI
 
 
 if __name__ == "__main__":

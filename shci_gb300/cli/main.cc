@@ -1,0 +1,355 @@
+// shci_gpu: the drop-in command line driver.
+//
+// Run in a directory that holds config.json and FCIDUMP, like the reference's `shci`
+// executable (src/main.cc:24-37, src/injector.cc:10-24).  It follows Solver<S>::run
+// (src/solver/solver.h:100-160): setup, the variational stages with their eps_vars_schedule
+// (:338-539), optional RDM output (src/chem/chem_system.cc:611-623, src/chem/rdm.cc:202-331) and
+// the three PT2 stages per eps_var (:541-1153), writing result.json with the reference's keys
+// (energy_hf, n_elecs, config, energy_var/<eps>, energy_total/<eps_var>/<eps_pt>/{value,
+// uncert}) and printing the reference's grep-able lines ("Final iteration ... energy=",
+// "Total energy: ...").  All computation goes through the C ABI of include/shci_gpu.h.
+//
+// GPU-specific keys (ignored by the reference): gpu/device (default 0), gpu/precision
+// ("mixed" default, or "fp64").
+#include <shci_gpu.h>
+
+#include <clocale>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "json.h"
+
+using shci_cli::Json;
+
+namespace {
+
+Json g_config, g_result;
+
+std::string fmt(const char* f, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, f);
+  std::vsnprintf(buf, sizeof(buf), f, ap);
+  va_end(ap);
+  return buf;
+}
+
+[[noreturn]] void die(const std::string& m) {
+  std::fprintf(stderr, "shci_gpu: %s\n", m.c_str());
+  std::exit(1);
+}
+
+void ck(shci_ctx* c, shci_status s, const char* what) {
+  if (s != SHCI_OK) die(std::string(what) + ": " + shci_last_error(c));
+}
+
+// Config::get (src/config.h:21-50): slash-separated keys, defaults for optional ones.
+double cfg_d(const std::string& k, double def, bool required = false) {
+  const Json* j = g_config.get(k);
+  if (!j) {
+    if (required) die("Cannot find '" + k + "' in config.json");
+    return def;
+  }
+  if (j->type != Json::Number) die("'" + k + "' must be a number");
+  return j->num;
+}
+bool cfg_b(const std::string& k, bool def) {
+  const Json* j = g_config.get(k);
+  if (!j) return def;
+  if (j->type != Json::Bool) die("'" + k + "' must be true or false");
+  return j->b;
+}
+std::string cfg_s(const std::string& k, const std::string& def, bool required = false) {
+  const Json* j = g_config.get(k);
+  if (!j) {
+    if (required) die("Cannot find '" + k + "' in config.json");
+    return def;
+  }
+  if (j->type != Json::String) die("'" + k + "' must be a string");
+  return j->str;
+}
+std::vector<double> cfg_v(const std::string& k, bool required) {
+  const Json* j = g_config.get(k);
+  std::vector<double> out;
+  if (!j) {
+    if (required) die("Cannot find '" + k + "' in config.json");
+    return out;
+  }
+  if (j->type != Json::Array) die("'" + k + "' must be an array");
+  for (const auto& e : j->arr) out.push_back(e.num);
+  return out;
+}
+
+// Result::put (src/result.h:56-70): rewrites result.json after every put.
+void result_dump() {
+  std::ofstream f("result.json");
+  f << shci_cli::dump(g_result) << std::endl;
+}
+void result_put(const std::string& k, double v) {
+  g_result.put(k) = Json::number(v);
+  result_dump();
+}
+
+std::string key_eps(double e) { return fmt("%#.2e", e); }
+
+struct Wavefunction {
+  double eps_var = 0.0, energy = 0.0;
+  std::vector<uint64_t> up, dn;
+  std::vector<double> coefs;
+};
+
+}  // namespace
+
+int main(int, char* argv[]) {
+  std::setlocale(LC_ALL, "en_US.UTF-8");
+  std::printf("Semistochastic Heat-bath Configuration Interation (SHCI) - GB300 build\n\n");
+  std::printf("Executable: %s\n", argv[0]);
+  {
+    std::ifstream f("config.json");
+    if (!f) die("cannot open config.json");
+    std::stringstream ss;
+    ss << f.rdbuf();
+    g_config = shci_cli::Parser(ss.str()).parse();
+  }
+  {
+    std::ifstream f("result.json");
+    if (f) {
+      std::stringstream ss;
+      ss << f.rdbuf();
+      try {
+        g_result = shci_cli::Parser(ss.str()).parse();
+      } catch (const std::exception&) {
+        g_result = Json();
+      }
+    }
+    if (g_result.type != Json::Object) {
+      g_result = Json();
+      g_result.type = Json::Object;
+    }
+    g_result.put("config") = g_config;
+    result_dump();
+  }
+  std::printf("Configuration:\n%s\n", shci_cli::dump(g_config).c_str());
+  const std::string system = cfg_s("system", "", true);
+  if (system != "chem") die("system '" + system + "' is not supported.");
+  if (cfg_d("n_states", 1) != 1) die("n_states > 1 is not supported by this build");
+  if (cfg_b("time_sym", false)) die("time_sym is not supported by this build");
+  const unsigned n_up = static_cast<unsigned>(cfg_d("n_up", 0, true));
+  const unsigned n_dn = static_cast<unsigned>(cfg_d("n_dn", 0, true));
+  const std::string pg = cfg_s("chem/point_group", "", true);
+  const int device = static_cast<int>(cfg_d("gpu/device", 0));
+  const std::string prec_s = cfg_s("gpu/precision", "mixed");
+  const int prec = prec_s == "fp64" ? SHCI_PREC_FP64 : SHCI_PREC_MIXED;
+  const double target_error = cfg_d("target_error", 5.0e-5);
+  std::vector<double> occ_u = cfg_v("occs_up", false), occ_d = cfg_v("occs_dn", false);
+  int reorder = -1;
+  if (g_config.get("reorder_orbs")) reorder = cfg_b("reorder_orbs", true) ? 1 : 0;
+
+  shci_ctx* c = nullptr;
+  if (shci_create(&c, device, 0) != SHCI_OK) die("cannot create a context on the GPU");
+  std::vector<unsigned> ou(occ_u.begin(), occ_u.end()), od(occ_d.begin(), occ_d.end());
+  ck(c, shci_load_fcidump(c, "FCIDUMP", n_up, n_dn, pg.c_str(), reorder,
+                          ou.empty() ? nullptr : ou.data(), od.empty() ? nullptr : od.data()),
+     "load FCIDUMP");
+  double e_hf = 0.0;
+  uint64_t hf_up = 0, hf_dn = 0;
+  ck(c, shci_get_hf(c, &hf_up, &hf_dn, &e_hf), "HF det");
+  int n_orbs = 0;
+  ck(c, shci_get_integrals(c, &n_orbs, nullptr, nullptr, nullptr, nullptr, nullptr), "integrals");
+  double qinfo[4];
+  ck(c, shci_build_queues(c, qinfo), "heat-bath queues");
+  std::printf("Max hci queue elem: %.10f Ha\nNumber of entries in hci queue: %'zu\n", qinfo[0],
+              (size_t)qinfo[1]);
+  std::printf("Max singles_queue elem: %.10f Ha\nNumber of entries in singles_queue: %'zu\n",
+              qinfo[2], (size_t)qinfo[3]);
+  std::printf("HF energy: %.10f Ha\n", e_hf);
+  {
+    Json ne = Json::number(n_up + n_dn);
+    ne.is_int = true;
+    g_result.put("n_elecs") = ne;
+  }
+  result_put("energy_hf", e_hf);
+
+  const std::vector<double> eps_vars = cfg_v("eps_vars", true);
+  const std::vector<double> schedule = cfg_v("eps_vars_schedule", true);
+  std::vector<Wavefunction> wfs;
+  if (!cfg_b("skip_var", false)) {
+    std::printf("Final iteration 0 HF ndets= 1 energy= %.8f\n", e_hf);
+    double eps_prev = 1e100;
+    size_t it_s = 0;
+    size_t it_global = 0;
+    for (double eps_var : eps_vars) {
+      std::vector<double> sched;
+      while (it_s < schedule.size() && schedule[it_s] >= eps_prev) it_s++;
+      while (it_s < schedule.size() && schedule[it_s] > eps_var) sched.push_back(schedule[it_s++]);
+      double e = 0.0;
+      ck(c, shci_run_variation(c, &eps_var, 1, sched.empty() ? nullptr : sched.data(),
+                               sched.size(), target_error, prec, &e),
+         "variation");
+      size_t n_it = 0;
+      ck(c, shci_get_var_trace(c, nullptr, nullptr, nullptr, 0, &n_it), "trace");
+      std::vector<uint64_t> nd(n_it), nz(n_it);
+      std::vector<double> en(n_it);
+      ck(c, shci_get_var_trace(c, nd.data(), nz.data(), en.data(), n_it, &n_it), "trace");
+      for (size_t k = 0; k < n_it; k++) {
+        const double eps_k = k < sched.size() ? sched[k] : eps_var;
+        std::printf("Number of nonzero elems: %'zu\n", (size_t)nz[k]);
+        std::printf("Iteration %zu eps1= %#.2e ndets= %'zu energy= %.8f\n", ++it_global, eps_k,
+                    (size_t)nd[k], en[k]);
+      }
+      Wavefunction wf;
+      wf.eps_var = eps_var;
+      wf.energy = e;
+      size_t n = 0;
+      ck(c, shci_get_n_dets(c, &n), "dets");
+      wf.up.resize(n);
+      wf.dn.resize(n);
+      wf.coefs.resize(n);
+      ck(c, shci_get_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), n), "dets");
+      std::printf("Final iteration %zu eps1= %#.2e ndets= %'zu energy=  %.8f\n", it_global, eps_var,
+                  n, e);
+      result_put("energy_var/" + key_eps(eps_var), e);
+      wfs.push_back(std::move(wf));
+      eps_prev = eps_var;
+    }
+  }
+
+  const bool want_1rdm = cfg_b("get_1rdm_csv", false);
+  const bool want_2rdm = cfg_b("2rdm", false) || cfg_b("get_2rdm_csv", false);
+  if ((want_1rdm || want_2rdm) && !wfs.empty()) {
+    const Wavefunction& wf = wfs.back();
+    ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), wf.up.size()), "dets");
+    std::vector<unsigned> order(n_orbs), inv(n_orbs);
+    ck(c, shci_get_integrals(c, nullptr, nullptr, nullptr, nullptr, nullptr, order.data()), "order");
+    for (int i = 0; i < n_orbs; i++) inv[order[i]] = i;
+    const size_t n = n_orbs;
+    if (want_1rdm) {  // rdm.cc:202-221
+      std::vector<double> g1(n * n);
+      ck(c, shci_rdm1(c, g1.data()), "1-RDM");
+      FILE* f = std::fopen("1rdm.csv", "w");
+      std::fprintf(f, "p,r,1rdm\n");
+      for (size_t p = 0; p < n; p++)
+        for (size_t r = p; r < n; r++) {
+          const double v = g1[p * n + r];
+          if (std::fabs(v) < 1e-9) continue;
+          std::fprintf(f, "%d,%d,%#.15g\n", order[p], order[r], v);
+        }
+      std::fclose(f);
+    }
+    if (want_2rdm) {  // rdm.cc:271-331
+      size_t nnz[2];
+      ck(c, shci_update_hamiltonian(c, SHCI_PREC_FP64, nnz), "Hamiltonian");
+      const size_t nn = n * n;
+      std::vector<double> half(nn * (nn + 1) / 2);
+      ck(c, shci_rdm2(c, half.data()), "2-RDM");
+      auto elem = [&](size_t p, size_t q, size_t r, size_t s) {
+        size_t a = p * n + s, b = q * n + r;
+        if (a < b) std::swap(a, b);
+        return half[a * (a + 1) / 2 + b];
+      };
+      std::printf("writing out 2RDM\n");
+      if (cfg_b("get_2rdm_csv", false)) {
+        FILE* f = std::fopen("2rdm.csv", "w");
+        std::fprintf(f, "p,q,r,s,2rdm\n");
+        for (size_t p = 0; p < n; p++)
+          for (size_t q = p; q < n; q++)
+            for (size_t s = 0; s < n; s++)
+              for (size_t r = 0; r < n; r++) {
+                if (p == q && s > r) continue;
+                const double v = elem(p, q, r, s);
+                if (std::fabs(v) < 1.0e-9) continue;
+                std::fprintf(f, "%d,%d,%d,%d,%#.15g\n", order[p], order[q], order[r], order[s], v);
+              }
+        std::fclose(f);
+      } else {
+        FILE* f = std::fopen("spatialRDM.txt", "w");
+        std::fprintf(f, "%d\n", n_orbs);
+        for (size_t p = 0; p < n; p++)
+          for (size_t q = 0; q < n; q++)
+            for (size_t s = 0; s < n; s++)
+              for (size_t r = 0; r < n; r++) {
+                const double v = elem(inv[p], inv[q], inv[r], inv[s]);
+                if (std::fabs(v) > 1.e-6)
+                  std::fprintf(f, "%3zu   %3zu   %3zu   %3zu   %10.8g\n", p, q, s, r, v);
+              }
+        std::fclose(f);
+      }
+    }
+  }
+  if (cfg_b("var_only", false)) {
+    shci_destroy(c);
+    return 0;
+  }
+
+  // Perturbation for each eps_var (solver.h:399-411, 541-634)
+  for (const Wavefunction& wf : wfs) {
+    const double eps_var = wf.eps_var;
+    double eps_pt_dtm = std::max(2.0e-6, cfg_d("eps_pt_dtm_ratio", 0.1) * eps_var);
+    double eps_pt_psto = std::max(1.0e-7, cfg_d("eps_pt_psto_ratio", 0.01) * eps_var);
+    double eps_pt = cfg_d("eps_pt_ratio", 1.0e-3) * eps_var;
+    eps_pt_dtm = cfg_d("eps_pt_dtm", eps_pt_dtm);
+    eps_pt_psto = cfg_d("eps_pt_psto", eps_pt_psto);
+    eps_pt = cfg_d("eps_pt", eps_pt);
+    if (eps_pt_psto < eps_pt) eps_pt_psto = eps_pt;
+    if (eps_pt_dtm < eps_pt_psto) eps_pt_dtm = eps_pt_psto;
+    const std::string base = "energy_total/" + key_eps(eps_var) + "/" + key_eps(eps_pt);
+    const Json* have = g_result.get(base + "/value");
+    if (have && have->type == Json::Number && have->num != 0.0 && !cfg_b("force_pt", false)) {
+      const Json* hu = g_result.get(base + "/uncert");
+      std::printf("Total energy: %.10f +- %.10f (state 0, loaded from result file)\n", have->num,
+                  hu ? hu->num : 0.0);
+      continue;
+    }
+    ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), wf.up.size()), "dets");
+    double dtm = 0.0, u_dtm = 0.0;
+    size_t n_dtm = 0;
+    ck(c, shci_pt2_dtm(c, wf.energy, eps_pt_dtm, (size_t)cfg_d("n_batches_pt_dtm", 0), &dtm,
+                       &u_dtm, &n_dtm),
+       "PT2 dtm");
+    std::printf("Number of dtm pt dets: %'zu\n", n_dtm);
+    std::printf("PT dtm correction (eps1= %.2e, eps_pt_dtm= %.2e): %.10f +- %.10f Ha\n", eps_var,
+                eps_pt_dtm, dtm, u_dtm);
+    double value = wf.energy + dtm, uncert = 0.0;
+    double psto = 0.0, u_psto = 0.0;
+    if (eps_pt_psto < eps_pt_dtm) {
+      size_t n_psto = 0, nb = 0;
+      const size_t nb_psto = std::max<size_t>(16, (size_t)cfg_d("n_batches_pt_psto", 16));
+      ck(c, shci_pt2_psto(c, wf.energy, eps_pt_dtm, eps_pt_psto, nb_psto, target_error, eps_pt,
+                          &psto, &u_psto, &n_psto, &nb),
+         "PT2 psto");
+      std::printf("PT psto correction (eps1= %.2e, eps_pt_psto= %.2e): %.10f +- %.10f Ha\n",
+                  eps_var, eps_pt_psto, psto, u_psto);
+      value += psto;
+      uncert = u_psto;
+    }
+    if (eps_pt < eps_pt_psto) {
+      const size_t n_samples = (size_t)cfg_d("n_dets_in_sample_pt_sto", 0);
+      if (n_samples == 0 || cfg_b("semisto_sto", true))
+        std::printf("Note: this build runs the stochastic stage with an explicit sample size "
+                    "and semisto_sto = false (using %zu samples)\n",
+                    n_samples ? n_samples : (size_t)200000);
+      double sto = 0.0, u_sto = 0.0;
+      size_t iters = 0;
+      ck(c, shci_pt2_sto(c, wf.energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),
+                         n_samples ? n_samples : 200000, 0,
+                         (unsigned)cfg_d("random_seed", 347634253),
+                         (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, &sto,
+                         &u_sto, &iters, nullptr, 0),
+         "PT2 sto");
+      std::printf("PT sto correction (eps1= %.2e, eps_pt= %.2e): %.10f +- %.10f Ha\n", eps_var,
+                  eps_pt, sto, u_sto);
+      value += sto;
+      uncert = std::sqrt(uncert * uncert + u_sto * u_sto);
+    }
+    std::printf("Total energy: %.10f +- %.10f Ha (state 0)\n", value, uncert);
+    result_put(base + "/value", value);
+    result_put(base + "/uncert", uncert);
+  }
+  shci_destroy(c);
+  return 0;
+}

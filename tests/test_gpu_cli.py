@@ -1,0 +1,44 @@
+"""The drop-in driver: run in a directory with config.json + FCIDUMP like the reference's
+`shci`, it writes result.json with the reference's keys and prints its grep-able lines."""
+import json
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import C_ATOM, GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cli_c_atom_matches_reference_result(tmp_path):
+    from shci_gb300 import build
+    exe = build.build_cli()
+    shutil.copyfile(C_ATOM, tmp_path / "FCIDUMP")
+    cfg = {"system": "chem", "n_up": 4, "n_dn": 2, "eps_vars": [5e-5],
+           "eps_vars_schedule": [2e-3, 1e-3, 5e-4, 2e-4, 1e-4], "chem": {"point_group": "d2h"},
+           "eps_pt_dtm": 5e-6, "eps_pt_psto": 1e-7, "eps_pt": 5e-8,
+           "n_dets_in_sample_pt_sto": 10000, "semisto_sto": False,
+           "get_1rdm_csv": True, "2rdm": True}
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    assert "Final iteration" in out and "Total energy:" in out
+    res = json.load(open(tmp_path / "result.json"))
+    ref = json.load(open(os.path.join(GOLDEN, "c_atom_pins.json")))
+    assert res["n_elecs"] == 6
+    assert abs(res["energy_hf"] - ref["energy_hf"]) < 1e-10
+    assert abs(res["energy_var"]["5.00e-05"] - ref["energy_var"]["5.00e-05"]) < 1e-8
+    tot = res["energy_total"]["5.00e-05"]["5.00e-08"]
+    ref_tot = ref["energy_total"]["5.00e-05"]["5.00e-08"]
+    # different stochastic samples (the reference used semistochastic sampling sized from
+    # machine memory): agreement within the combined error bars
+    assert abs(tot["value"] - ref_tot["value"]) < 5 * (tot["uncert"] + ref_tot["uncert"])
+    assert res["config"]["n_up"] == 4
+    lines = open(tmp_path / "1rdm.csv").read().splitlines()
+    assert lines[0] == "p,r,1rdm"
+    diag = sum(float(l.split(",")[2]) for l in lines[1:] if l.split(",")[0] == l.split(",")[1])
+    assert abs(diag - 6.0) < 1e-8
+    assert (tmp_path / "spatialRDM.txt").read_text().splitlines()[0].strip() == "22"
