@@ -220,6 +220,39 @@ def run_pt2(ctx, stream, e_var):
     return out
 
 
+def run_batched(data_dir, n_instances=256, cpu_sample=8):
+    """Workload 5: n_instances synthetic FCIDUMPs (n ~ U[12,20], electrons per spin ~
+    U[3, n/2-1], seeds 20261203 + 1000 + i), eps_var 1e-4, deterministic PT2 at 1e-6, solved
+    by the concurrent batch runner; CPU baseline = the oracle on the first cpu_sample
+    instances, scaled."""
+    import shci_gb300
+    from shci_gb300 import synthetic
+    inst = []
+    for i in range(n_instances):
+        path, n, ne = synthetic.batch_instance(i, os.path.join(data_dir, "batch"))
+        inst.append((path, ne, ne))
+    t0 = time.perf_counter()
+    res, used = shci_gb300._lib.batch_solve(inst, [1e-4], [], (1e-6, 1e-6, 1e-6), n_workers=0)
+    t = time.perf_counter() - t0
+    out = {"instances": n_instances, "s": t, "instances_per_s": n_instances / t,
+           "workers": used, "total_dets": int(sum(r["n_dets"] for r in res)),
+           "max_dets": int(max(r["n_dets"] for r in res))}
+    if cpu_sample:
+        from oracle.oracle import Oracle
+        tc = time.perf_counter()
+        for path, nu, nd in inst[:cpu_sample]:
+            o = Oracle(path, nu, nd)
+            o.run_all_variations([1e-4], [], TARGET_ERROR)
+            o.pt_dtm(1e-6, 1)
+        tc = time.perf_counter() - tc
+        share = sum(r["seconds"] for r in res[:cpu_sample]) / max(1e-9, sum(r["seconds"] for r in res))
+        out["cpu_baseline"] = {"value": tc / max(share, 1e-9), "unit": "s",
+                               "cores": Oracle.threads(), "kind": "port",
+                               "sample": "oracle solves of the first %d instances scaled by their "
+                                         "share of the GPU per-instance solve time" % cpu_sample}
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -276,6 +309,7 @@ def run_ours(args):
 
     # PT2 on the step's wavefunction (the metric's "PT2 s"): dtm, psto, sto stages
     pt2 = run_pt2(ctx, stream, e_mixed) if args.pt2 else None
+    batched = run_batched(args.data) if args.batched else None
 
     # all-FP64 form of the same step
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -351,6 +385,7 @@ def run_ours(args):
         "gpu_launches": launches // args.steps,
         "clocks": clk.summary(),
         "pt2": pt2,
+        "batched": batched,
         "fp64": {"ms_per_step": ms_fp64, "energy": e_fp64},
         "energy_mixed_fp64corrected": e_mixed, "energy_davidson_mixed": e_dav,
         "dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
@@ -370,6 +405,8 @@ def main():
     ap.add_argument("--workload", type=int, default=3, choices=sorted(WORKLOADS))
     ap.add_argument("--no-pt2", dest="pt2", action="store_false",
                     help="skip the PT2 measurement")
+    ap.add_argument("--batched", action="store_true",
+                    help="also time workload 5 (256 small instances, concurrent batch runner)")
     args = ap.parse_args()
     global WORKLOAD, SCHEDULE, EPS_VAR
     WORKLOAD = args.workload

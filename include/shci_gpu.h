@@ -226,6 +226,40 @@ shci_status shci_pt2_sto(shci_ctx* ctx, double energy_var, double eps_pt_psto, d
                          double psto_uncert, double* correction, double* uncert,
                          size_t* n_iterations, double* loops, size_t cap);
 
+/* ---- batched small instances ------------------------------------------------------------ */
+
+/* One instance of a batch: the reference's whole run (setup, variation with its schedule,
+ * PT2) for one FCIDUMP.  eps_pt_dtm <= 0 skips PT2; the psto stage runs (16 batches) when
+ * 0 < eps_pt_psto < eps_pt_dtm. */
+typedef struct {
+  const char* fcidump;
+  unsigned n_up, n_dn;
+  const char* point_group;
+  const double* eps_vars;
+  size_t n_eps;
+  const double* schedule;
+  size_t n_sched;
+  double target_error;
+  double eps_pt_dtm, eps_pt_psto, eps_pt;
+  int precision;
+} shci_batch_item;
+
+typedef struct {
+  int status;             /* shci_status of this instance */
+  double energy_hf, energy_var;
+  double correction_pt;   /* PT2 correction (E_total = energy_var + correction_pt) */
+  double uncert_pt;
+  uint64_t n_dets, n_pt_dets;
+  double seconds;         /* wall time of this instance's solve */
+} shci_batch_result;
+
+/* Solves n instances on `device` concurrently (n_workers contexts and streams, largest
+ * instances first); n_workers <= 0 lets the autotuner choose from measured throughput
+ * (*workers_used reports the choice).  No counterpart object in the reference, which runs
+ * one instance per process; each instance follows Solver<S>::run (solver.h:100-160). */
+shci_status shci_batch_solve(int device, const shci_batch_item* items, size_t n, int n_workers,
+                             shci_batch_result* results, int* workers_used);
+
 /* ---- RDMs: the adjoint of E_var (RDM::get_1rdm / get_2rdm, src/chem/rdm.cc) ---------- */
 
 /* 1-RDM of the context's wavefunction: rdm1[p*n + r] = sum_ij c_i c_j <D_i| a+_r a_p |D_j>

@@ -91,6 +91,55 @@ def load():
     return L
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("fcidump", ctypes.c_char_p), ("n_up", ctypes.c_uint), ("n_dn", ctypes.c_uint),
+                ("point_group", ctypes.c_char_p), ("eps_vars", ctypes.POINTER(ctypes.c_double)),
+                ("n_eps", ctypes.c_size_t), ("schedule", ctypes.POINTER(ctypes.c_double)),
+                ("n_sched", ctypes.c_size_t), ("target_error", ctypes.c_double),
+                ("eps_pt_dtm", ctypes.c_double), ("eps_pt_psto", ctypes.c_double),
+                ("eps_pt", ctypes.c_double), ("precision", ctypes.c_int)]
+
+
+class BatchResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("energy_hf", ctypes.c_double),
+                ("energy_var", ctypes.c_double), ("correction_pt", ctypes.c_double),
+                ("uncert_pt", ctypes.c_double), ("n_dets", ctypes.c_uint64),
+                ("n_pt_dets", ctypes.c_uint64), ("seconds", ctypes.c_double)]
+
+
+def batch_solve(instances, eps_vars, schedule=(), eps_pt=(0.0, 0.0, 0.0), target_error=5e-5,
+                precision=PREC_FP64, n_workers=0, device=0):
+    """Solves many small instances concurrently (shci_batch_solve).  instances: list of
+    (fcidump_path, n_up, n_dn[, point_group]).  eps_pt = (eps_pt_dtm, eps_pt_psto, eps_pt).
+    Returns (list of result dicts, workers used)."""
+    L = load()
+    L.shci_batch_solve.restype = ctypes.c_int
+    L.shci_batch_solve.argtypes = [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_size_t,
+                                   ctypes.c_int, ctypes.POINTER(BatchResult),
+                                   ctypes.POINTER(ctypes.c_int)]
+    n = len(instances)
+    ev = (ctypes.c_double * len(eps_vars))(*eps_vars)
+    sc = (ctypes.c_double * max(1, len(schedule)))(*schedule)
+    items = (BatchItem * n)()
+    keep = []
+    for k, inst in enumerate(instances):
+        path, nu, nd = inst[0], inst[1], inst[2]
+        pg = inst[3] if len(inst) > 3 else "C1"
+        p, g = str(path).encode(), pg.encode()
+        keep += [p, g]
+        items[k] = BatchItem(p, nu, nd, g, ev, len(eps_vars), sc, len(schedule), target_error,
+                             eps_pt[0], eps_pt[1], eps_pt[2], precision)
+    res = (BatchResult * n)()
+    used = ctypes.c_int()
+    st = L.shci_batch_solve(device, items, n, n_workers, res, ctypes.byref(used))
+    out = [dict(status=r.status, energy_hf=r.energy_hf, energy_var=r.energy_var,
+                correction_pt=r.correction_pt, uncert_pt=r.uncert_pt, n_dets=r.n_dets,
+                n_pt_dets=r.n_pt_dets, seconds=r.seconds) for r in res]
+    if st != 0:
+        raise ShciError(st, "batch solve failed (per-instance status in the results)")
+    return out, used.value
+
+
 def header_symbols():
     """Names of the functions declared in include/shci_gpu.h."""
     import re

@@ -86,12 +86,30 @@ __device__ __forceinline__ double h_diag(const DevIntegrals& I, uint64_t up, uin
   return ob + (direct + exch) + I.e_core;
 }
 
+// x * (-1)^odd.  Multiplying by +-1 only sets the sign bit, so the flip is done on the bits:
+// the same value as the multiplication, without an FP64 instruction (GB300's FP64 pipe runs a
+// warp instruction in 16 SM cycles, so every FP64 op saved in an element matters).
+__device__ __forceinline__ double flip_sign(double x, int odd) {
+  return __longlong_as_double(__double_as_longlong(x) ^
+                              (static_cast<long long>(odd & 1) << 63));
+}
+
+// |h| >= 1e-12 (src/util.h:50) decided on the bit pattern (IEEE order of non-negative doubles
+// is the integer order of their bits); equal to the FP64 comparison for every non-NaN h.
+constexpr unsigned long long kEpsBits = 0x3d719799812dea11ull;  // bits of 1.0e-12
+__device__ __forceinline__ bool keep_elem(double h) {
+  return (static_cast<unsigned long long>(__double_as_longlong(h)) & 0x7fffffffffffffffull) >=
+         kEpsBits;
+}
+
 // Single excitation oi -> oj within the spin string `same` (the other string is `oppo`);
-// `same` is the spin string of the ket-side det i.  perm = +-1.  chem_system.cc:544-577.
+// `same` is the spin string of the ket-side det i; the permutation sign is (-1)^odd.
+// chem_system.cc:544-577, same terms in the same order; 2 * direct is exact, so
+// fma(2, direct, e) rounds exactly like e + 2 * direct.
 __device__ __forceinline__ double h_single(const DevIntegrals& I, uint64_t same, uint64_t oppo,
-                                           int oi, int oj, int perm) {
+                                           int oi, int oj, int odd) {
   const int n = I.n;
-  const double ob = perm * I.h1[oi * n + oj];
+  const double ob = flip_sign(I.h1[oi * n + oj], odd);
   const double* D = I.dtab + (size_t)(oi * n + oj) * n;
   const double* X = I.xtab + (size_t)(oi * n + oj) * n;
   double e = 0.0;
@@ -101,57 +119,59 @@ __device__ __forceinline__ double h_single(const DevIntegrals& I, uint64_t same,
     const double direct = D[o];
     if (oppo >> o & 1) {
       oppo &= ~(1ull << o);
-      e += 2 * direct;
+      e = fma(2.0, direct, e);
     } else {
       e += direct;
     }
   }
   for (uint64_t m = oppo; m; m &= m - 1) e += D[ctz64(m)];
-  e *= perm;
-  return ob + e;
+  return ob + flip_sign(e, odd);
 }
 
 // Parity helper of src/det/half_det.cc:120-206 for one moved orbital: electrons of `s` below b.
 __device__ __forceinline__ int below_count(uint64_t s, int b) { return popc64(s & below(b)); }
 
-// H_ij for dets whose excitation degree is known to be 1 or 2 (or 0: diagonal).  up/dn
-// differences are given; returns 0 for degree > 2.  Equivalent to get_hamiltonian_elem(i,j,-1).
-__device__ __forceinline__ double h_offdiag(const DevIntegrals& I, uint64_t ui, uint64_t di,
-                                            uint64_t uj, uint64_t dj) {
+// H_ij for a single excitation: exactly one of ui^uj, di^dj is non-zero, with two bits set.
+__device__ __forceinline__ double h_one(const DevIntegrals& I, uint64_t ui, uint64_t di,
+                                        uint64_t uj, uint64_t dj) {
+  const uint64_t xu = ui ^ uj;
+  const bool alpha = xu != 0;
+  const uint64_t si = alpha ? ui : di, sj = alpha ? uj : dj, oi_str = alpha ? di : ui;
+  const uint64_t x = si ^ sj;
+  const int oi = ctz64(si & x), oj = ctz64(sj & x);
+  const int par = below_count(si, oi) + below_count(sj, oj);
+  return h_single(I, si, oi_str, oi, oj, par);
+}
+
+// H_ij for a double excitation (one alpha + one beta electron, or two of the same spin).
+__device__ __forceinline__ double h_two(const DevIntegrals& I, uint64_t ui, uint64_t di,
+                                        uint64_t uj, uint64_t dj) {
   const uint64_t xu = ui ^ uj, xd = di ^ dj;
-  const int nu = popc64(xu) >> 1, nd = popc64(xd) >> 1;
-  if (nu + nd > 2 || nu + nd == 0) return 0.0;
-  if (nu == 1 && nd == 0) {
-    const int oi = ctz64(ui & xu), oj = ctz64(uj & xu);
-    const int par = below_count(ui, oi) + below_count(uj, oj);
-    return h_single(I, ui, di, oi, oj, (par & 1) ? -1 : 1);
-  }
-  if (nd == 1 && nu == 0) {
-    const int oi = ctz64(di & xd), oj = ctz64(dj & xd);
-    const int par = below_count(di, oi) + below_count(dj, oj);
-    return h_single(I, di, ui, oi, oj, (par & 1) ? -1 : 1);
-  }
-  if (nu == 1 && nd == 1) {
+  if (xu && xd) {
     const int ai = ctz64(ui & xu), aj = ctz64(uj & xu);
     const int bi = ctz64(di & xd), bj = ctz64(dj & xd);
     const int par = below_count(ui, ai) + below_count(uj, aj) + below_count(di, bi) +
                     below_count(dj, bj);
-    const double e = g2at(I, ai, aj, bi, bj);
-    const int pu = ((below_count(ui, ai) + below_count(uj, aj)) & 1) ? -1 : 1;
-    const int pd = ((below_count(di, bi) + below_count(dj, bj)) & 1) ? -1 : 1;
-    (void)par;
-    return e * (pu * pd);
+    return flip_sign(g2at(I, ai, aj, bi, bj), par);
   }
   // same-spin double
-  const uint64_t si = nu == 2 ? ui : di, sj = nu == 2 ? uj : dj, x = nu == 2 ? xu : xd;
+  const bool alpha = xu != 0;
+  const uint64_t si = alpha ? ui : di, sj = alpha ? uj : dj, x = alpha ? xu : xd;
   const uint64_t li = si & x, rj = sj & x;
   const int l0 = ctz64(li), l1 = ctz64(li & (li - 1));
   const int r0 = ctz64(rj), r1 = ctz64(rj & (rj - 1));
   const int par = below_count(si, l0) + below_count(si, l1) + below_count(sj, r0) +
                   below_count(sj, r1);
-  double e = g2at(I, l0, r0, l1, r1) - g2at(I, l0, r1, l1, r0);
-  e *= (par & 1) ? -1 : 1;
-  return e;
+  return flip_sign(g2at(I, l0, r0, l1, r1) - g2at(I, l0, r1, l1, r0), par);
+}
+
+// H_ij for dets whose excitation degree is known to be 1 or 2 (or 0: diagonal).  up/dn
+// differences are given; returns 0 for degree > 2.  Equivalent to get_hamiltonian_elem(i,j,-1).
+__device__ __forceinline__ double h_offdiag(const DevIntegrals& I, uint64_t ui, uint64_t di,
+                                            uint64_t uj, uint64_t dj) {
+  const int deg = (popc64(ui ^ uj) + popc64(di ^ dj)) >> 1;
+  if (deg > 2 || deg == 0) return 0.0;
+  return deg == 1 ? h_one(I, ui, di, uj, dj) : h_two(I, ui, di, uj, dj);
 }
 
 // ---------------------------------------------------------------- hashing (C21, a16)

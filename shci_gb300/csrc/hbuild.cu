@@ -135,29 +135,68 @@ __device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* a, uint32_t 
   return lo;
 }
 
-// MODE 0: count (and diagonal), MODE 1: fill FP64, MODE 2: fill mixed (FP32 value+residual)
+// Diagonal elements, a thread per det (chem_system.cc:426-432 via h_diag).
+__global__ void k_hdiag(DevIntegrals I, const uint64_t* __restrict__ up,
+                        const uint64_t* __restrict__ dn, uint32_t n, double* diag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    diag[i] = h_diag(I, up[i], dn[i]);
+}
+
+// Candidate columns that pass the excitation-degree test wait in two per-warp ring buffers,
+// one for single and one for double excitations, and are evaluated 32 at a time.  A scan
+// finds a connected column for about one lane in thirty, and GB300 issues an FP64 warp
+// instruction at 1/16 per SM cycle however many lanes are active, so evaluating in place
+// would run the matrix-element arithmetic with one useful lane; separate queues keep the
+// long single-excitation sums apart from the short double-excitation ones.
+constexpr uint32_t kQ = 64;  // ring size: < 32 waiting + 32 pushed always fit
+struct RowQueues {
+  uint32_t j[2][kQ];
+  uint64_t u[2][kQ];
+  uint64_t d[2][kQ];
+};
+
+// MODE 0: count, MODE 1: fill FP64, MODE 2: fill mixed (FP32 value + FP32 residual).
+// Count and fill run the same traversal and drain the queues at the same points, so a row's
+// columns land in the same deterministic order in every build.
 template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
     k_hbuild(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
              uint32_t n, IndexView ix, uint32_t* row_cnt, const uint64_t* row_ptr,
-             uint32_t* col, double* v64, float* v32, float* r32, double* diag,
-             unsigned* work) {
+             uint32_t* col, double* v64, float* v32, float* r32, unsigned* work) {
+  __shared__ RowQueues qs[kWarps];
+  RowQueues& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
+  const unsigned lt = lanemask_lt();
   while (true) {
     uint32_t i = 0;
     if (lane == 0) i = atomicAdd(work, 1u);
     i = __shfl_sync(kFull, i, 0);
     if (i >= n) break;
     const uint64_t ui = up[i], di = dn[i];
-    if (MODE == 0 && lane == 0) diag[i] = h_diag(I, ui, di);
     const uint32_t a = ix.det_aid[i], b = ix.det_bid[i];
-    uint64_t base = MODE ? row_ptr[i] : 0;
+    const uint64_t base = MODE ? row_ptr[i] : 0;
     uint32_t cnt = 0;
     uint64_t n_scan_a = 0, n_scan_b = 0, n_mixed = 0;
-    auto emit = [&](bool keep, uint32_t j, double H) {
+    uint32_t qh[2] = {0u, 0u}, qn[2] = {0u, 0u};  // ring heads and lengths (warp-uniform)
+    // evaluate the m <= 32 oldest entries of queue t, keep |H| >= 1e-12, write kept ones
+    auto drain = [&](int t, uint32_t m) {
+      __syncwarp();
+      bool keep = false;
+      uint32_t j = 0;
+      double H = 0.0;
+      if (lane < m) {
+        const uint32_t s = (qh[t] + lane) & (kQ - 1);
+        j = q.j[t][s];
+        const uint64_t uj = q.u[t][s], dj = q.d[t][s];
+        H = t == 0 ? h_one(I, ui, di, uj, dj) : h_two(I, ui, di, uj, dj);
+        keep = keep_elem(H);
+      }
+      __syncwarp();
+      qh[t] += m;
+      qn[t] -= m;
       const unsigned bal = __ballot_sync(kFull, keep);
       if (MODE && keep) {
-        const uint64_t pos = base + cnt + __popc(bal & lanemask_lt());
+        const uint64_t pos = base + cnt + __popc(bal & lt);
         col[pos] = j;
         if (MODE == 1) {
           v64[pos] = H;
@@ -169,6 +208,23 @@ __global__ void __launch_bounds__(kWarps * 32)
       }
       cnt += __popc(bal);
     };
+    // queue the lanes' candidates (cand), as singles or doubles, draining full queues
+    auto push = [&](bool cand, bool single, uint32_t j, uint64_t uj, uint64_t dj) {
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        const bool mine = cand && (single == (t == 0));
+        const unsigned bal = __ballot_sync(kFull, mine);
+        if (!bal) continue;
+        if (mine) {
+          const uint32_t s = (qh[t] + qn[t] + __popc(bal & lt)) & (kQ - 1);
+          q.j[t][s] = j;
+          q.u[t][s] = uj;
+          q.d[t][s] = dj;
+        }
+        qn[t] += __popc(bal);
+        if (qn[t] >= 32u) drain(t, 32u);
+      }
+    };
     // (a) same beta string: beta group in det-id order, from the first j > i
     {
       const uint32_t e = ix.b_start[b + 1];
@@ -176,18 +232,17 @@ __global__ void __launch_bounds__(kWarps * 32)
       n_scan_a = e - s;
       for (uint32_t k0 = s; k0 < e; k0 += 32) {
         const uint32_t k = k0 + lane;
-        bool keep = false;
+        bool cand = false;
         uint32_t j = 0;
-        double H = 0.0;
+        uint64_t uj = 0;
+        int x = 0;
         if (k < e) {
           j = ix.bd_idx[k];
-          const uint64_t uj = ix.bd_up[k];
-          if (popc64(uj ^ ui) <= 4) {
-            H = h_offdiag(I, ui, di, uj, di);
-            keep = fabs(H) >= kEps;
-          }
+          uj = ix.bd_up[k];
+          x = popc64(uj ^ ui);
+          cand = x <= 4;
         }
-        emit(keep, j, H);
+        push(cand, x == 2, j, uj, di);
       }
     }
     // (b) same alpha string: alpha group in det-id order, from the first j > i
@@ -197,18 +252,17 @@ __global__ void __launch_bounds__(kWarps * 32)
       n_scan_b = e - s;
       for (uint32_t k0 = s; k0 < e; k0 += 32) {
         const uint32_t k = k0 + lane;
-        bool keep = false;
+        bool cand = false;
         uint32_t j = 0;
-        double H = 0.0;
+        uint64_t dj = 0;
+        int x = 0;
         if (k < e) {
           j = ix.ad_idx[k];
-          const uint64_t dj = ix.ad_dn[k];
-          if (popc64(dj ^ di) <= 4) {
-            H = h_offdiag(I, ui, di, ui, dj);
-            keep = fabs(H) >= kEps;
-          }
+          dj = ix.ad_dn[k];
+          x = popc64(dj ^ di);
+          cand = x <= 4;
         }
-        emit(keep, j, H);
+        push(cand, x == 2, j, ui, dj);
       }
     }
     // (c) alpha single x beta single
@@ -237,9 +291,9 @@ __global__ void __launch_bounds__(kWarps * 32)
         n_mixed += total;
         for (uint32_t t0 = 0; t0 < total; t0 += 32) {
           const uint32_t t = t0 + lane;
-          bool keep = false;
+          bool cand = false;
           uint32_t j = 0;
-          double H = 0.0;
+          uint64_t uj = 0, dj = 0;
           // owner lane = number of lanes whose inclusive prefix is <= t (prefixes are
           // non-decreasing); a fixed 5-step search so every lane runs the same shuffles
           uint32_t lo = 0;
@@ -256,14 +310,14 @@ __global__ void __launch_bounds__(kWarps * 32)
             const uint32_t k = o_gs + (t - (o_inc - o_n));
             j = ix.am_idx[k];
             if (j > i) {
-              const uint64_t dj = ix.am_dn[k];
+              dj = ix.am_dn[k];
               if (popc64(dj ^ di) == 2) {
-                H = h_offdiag(I, ui, di, ix.ua[o_g], dj);
-                keep = fabs(H) >= kEps;
+                uj = ix.ua[o_g];
+                cand = true;
               }
             }
           }
-          emit(keep, j, H);
+          push(cand, false, j, uj, dj);
         }
         // probe mode: binary-search each beta single of the row in the big groups
         unsigned pmask = __ballot_sync(kFull, probe);
@@ -277,25 +331,24 @@ __global__ void __launch_bounds__(kWarps * 32)
           n_mixed += nbs;
           for (uint32_t k0 = 0; k0 < nbs; k0 += 32) {
             const uint32_t k = k0 + lane;
-            bool keep = false;
+            bool cand = false;
             uint32_t j = 0;
-            double H = 0.0;
+            uint64_t bstr = 0;
             if (k < nbs) {
-              const uint64_t bstr = ix.bs_str[b0 + k];
+              bstr = ix.bs_str[b0 + k];
               const uint32_t pos = lower_bound_u64(ix.am_dn, p_gs, p_gs + p_gn, bstr);
               if (pos < p_gs + p_gn && ix.am_dn[pos] == bstr) {
                 j = ix.am_idx[pos];
-                if (j > i) {
-                  H = h_offdiag(I, ui, di, ua2, bstr);
-                  keep = fabs(H) >= kEps;
-                }
+                cand = j > i;
               }
             }
-            emit(keep, j, H);
+            push(cand, false, j, ua2, bstr);
           }
         }
       }
     }
+    if (qn[0]) drain(0, qn[0]);
+    if (qn[1]) drain(1, qn[1]);
     if (MODE == 0 && lane == 0) {
       row_cnt[i] = cnt;
       // candidates examined by this row, per part
@@ -304,6 +357,7 @@ __global__ void __launch_bounds__(kWarps * 32)
       atomicAdd(cc + 1, (unsigned long long)n_scan_b);
       atomicAdd(cc + 2, (unsigned long long)n_mixed);
     }
+    __syncwarp();
   }
 }
 
@@ -429,9 +483,12 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
   {
     ProfScope ps(c->prof, s, "hbuild_count");
+    k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n,
+                                             H.diag.p);
+    SHCI_LAUNCH_CHECK();
     k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                              H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                             nullptr, H.diag.p, work);
+                                             nullptr, work);
     SHCI_LAUNCH_CHECK();
   }
   // row_ptr = exclusive scan of counts (counts widened to 64 bit)
@@ -461,11 +518,11 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
     if (precision == SHCI_PREC_FP64) {
       k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                nullptr, H.row_ptr.p, H.col.p, H.val64.p,
-                                               nullptr, nullptr, nullptr, work);
+                                               nullptr, nullptr, work);
     } else {
       k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
-                                               H.res32.p, nullptr, work);
+                                               H.res32.p, work);
     }
     SHCI_LAUNCH_CHECK();
   }

@@ -1,0 +1,28 @@
+"""Batched small instances (workload 5 generator): every instance solved by the concurrent
+batch runner equals the oracle's standalone solve (det count, E_var, deterministic PT2), and
+the result does not depend on the number of workers."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_oracle(oracle_mod, data_dir):
+    import shci_gb300
+    from shci_gb300 import synthetic
+    inst = []
+    for i in range(6):
+        path, n, ne = synthetic.batch_instance(i, data_dir)
+        inst.append((path, ne, ne))
+    res, used = shci_gb300._lib.batch_solve(inst, [1e-4], [], (1e-6, 1e-6, 1e-6), n_workers=3)
+    res2, _ = shci_gb300._lib.batch_solve(inst, [1e-4], [], (1e-6, 1e-6, 1e-6), n_workers=0)
+    for (path, nu, nd), r, r2 in zip(inst, res, res2):
+        o = oracle_mod.Oracle(path, nu, nd)
+        e = o.run_all_variations([1e-4], [], 5e-5)[0]
+        v, _, n_pt = o.pt_dtm(1e-6, 1)
+        assert r["status"] == 0
+        assert r["n_dets"] == len(o.dets()[0])
+        assert abs(r["energy_var"] - e) < 1e-9
+        assert r["n_pt_dets"] == n_pt
+        assert abs(r["correction_pt"] - v) < 1e-11
+        assert r2["n_dets"] == r["n_dets"] and abs(r2["energy_var"] - r["energy_var"]) < 1e-12
