@@ -345,15 +345,19 @@ def run_ours(args):
     per = {k: (v[0] / max(1, v[1]), v[1]) for k, v in prof.items()}
     dom = max(prof, key=lambda k: prof[k][0])
     nnz, cand = stats["nnz"], stats["candidates"]
+    m = stats.get("core_entries", 0)
     # Algorithmic HBM bytes per launch.  H build: read the det list (16 B/det), write counts /
     # read row offsets and the diagonal (8 B/det), write the store (12 B per stored element:
-    # u32 column + FP32 value + FP32 residual).  The index lists scanned per candidate are
-    # L2-resident (~12 B/det in total) and are reported as a scan rate, not as HBM bytes.
-    # H*v: read the store once (col + FP32 value = 8 B/element), row offsets, x (twice), y
-    # read-modify-write and the diagonal.
+    # u32 column + FP32 value + FP32 residual).  Core join: each row reads its entries' bucket
+    # spans (8 B per entry) and the det id of each candidate (4 B); the candidates' spin
+    # strings are gathered from the L2-resident det list.  Building the join writes keys and
+    # entry ids (12 B/entry), sorts them (4 passes x 24 B/entry) and writes spans and det ids
+    # (read 12 B, write 12 B per entry).  H*v: read the store once (col + FP32 value = 8
+    # B/element), row offsets, x (twice), y read-modify-write and the diagonal.
     alg = {
-        "hbuild_count": 16.0 * n + 4 * n + 8 * n,
-        "hbuild_fill": 16.0 * n + 8 * (n + 1) + 12.0 * nnz,
+        "hbuild_count": 16.0 * n + 4 * n + 8 * n + 8.0 * m + 4.0 * cand * (m > 0),
+        "hbuild_fill": 16.0 * n + 8 * (n + 1) + 12.0 * nnz + (8.0 * m + 4.0 * cand) * (m > 0),
+        "core_join": 132.0 * m,
         "spmv": 8.0 * nnz + 8 * (n + 1) + 16 * n + 16 * n + 8 * n,
     }
     kernels = {}

@@ -124,9 +124,12 @@ shci_status shci_hamiltonian_elems_noalloc(shci_ctx* ctx, const uint64_t* up_i,
  * (2 * (strict + n) - n, sparse_matrix.cc:13-26).  Elements with |H| < 1e-12 are dropped. */
 shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_out);
 
-/* Sizes of the last build: stats[0..8] = {n dets, strict-upper nnz, unique alpha strings,
- * unique beta strings, alpha-single pairs, (row, candidate) pairs scanned, and those pairs
- * split into same-beta, same-alpha and alpha-single x beta-single parts}. */
+/* Sizes of the last build: stats[0..9] = {n dets, strict-upper nnz, unique alpha strings,
+ * unique beta strings, alpha-single pairs, (row, candidate) pairs examined, three counts,
+ * path}.  path (stats[9]) is 1 when the two-hole core join built the matrix: then
+ * stats[2..4] are 0 and stats[6] is the number of core entries (dets x electron pairs).
+ * path 0 is the group scan: stats[6..8] split the candidates into same-beta, same-alpha and
+ * alpha-single x beta-single parts. */
 shci_status shci_hamiltonian_stats(shci_ctx* ctx, uint64_t* stats);
 
 /* Copy the Hamiltonian to the host: row_ptr[n+1] (strict upper), cols[nnz], vals[nnz]

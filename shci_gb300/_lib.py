@@ -275,10 +275,13 @@ class Context:
         return nnz[0], nnz[1]
 
     def hamiltonian_stats(self):
-        s = np.zeros(9, np.uint64)
+        s = np.zeros(10, np.uint64)
         self._ck(self.L.shci_hamiltonian_stats(self.h, s))
-        return dict(n=int(s[0]), nnz=int(s[1]), n_alpha=int(s[2]), n_beta=int(s[3]),
-                    alpha_singles=int(s[4]), candidates=int(s[5]),
+        if int(s[9]) == 1:
+            return dict(path="core_join", n=int(s[0]), nnz=int(s[1]), candidates=int(s[5]),
+                        core_entries=int(s[6]))
+        return dict(path="group_scan", n=int(s[0]), nnz=int(s[1]), n_alpha=int(s[2]),
+                    n_beta=int(s[3]), alpha_singles=int(s[4]), candidates=int(s[5]),
                     cand_same_beta=int(s[6]), cand_same_alpha=int(s[7]), cand_mixed=int(s[8]))
 
     def hamiltonian(self, nnz):

@@ -93,6 +93,8 @@ shci_status shci_create(shci_ctx** out, int device, size_t hbm_budget_bytes) {
                     &ix.bd_idx, &ix.as_off, &ix.as_list, &ix.bs_off, &ix.bs_list})
       b->mt = &c->mem;
     for (auto* b : {&ix.am_dn, &ix.ad_dn, &ix.bd_up, &ix.ua, &ix.ub, &ix.bs_str}) b->mt = &c->mem;
+    c->join.pairs.mt = c->join.jdet.mt = &c->mem;
+    c->join.keys.mt = c->join.span.mt = &c->mem;
     auto& H = c->H;
     H.row_ptr.mt = H.col.mt = H.row_cnt.mt = &c->mem;
     H.val64.mt = H.diag.mt = &c->mem;
@@ -316,7 +318,6 @@ shci_status shci_update_hamiltonian(shci_ctx* c, int precision, size_t* nnz_out)
     if (precision != SHCI_PREC_FP64 && precision != SHCI_PREC_MIXED)
       throw ArgError("unknown precision");
     sync_dets(c);
-    build_index(c);
     const size_t nnz = build_hamiltonian(c, precision);
     if (nnz_out) {
       nnz_out[0] = nnz;
@@ -329,16 +330,18 @@ shci_status shci_hamiltonian_stats(shci_ctx* c, uint64_t* stats) {
   if (!c || !stats) return SHCI_ERR_ARG;
   return guard(c, [&]() {
     if (!c->H.valid) throw ArgError("no Hamiltonian built");
+    const bool scan = !c->H.join;
     uint32_t n_as = 0;
-    if (c->idx.n_alpha)
+    if (scan && c->idx.n_alpha)
       SHCI_CUDA(cudaMemcpy(&n_as, c->idx.as_off.p + c->idx.n_alpha, 4, cudaMemcpyDeviceToHost));
     stats[0] = c->H.n;
     stats[1] = c->H.nnz;
-    stats[2] = c->idx.n_alpha;
-    stats[3] = c->idx.n_beta;
+    stats[2] = scan ? c->idx.n_alpha : 0;
+    stats[3] = scan ? c->idx.n_beta : 0;
     stats[4] = n_as;
     stats[5] = c->H.candidates;
     for (int k = 0; k < 3; k++) stats[6 + k] = c->H.cand_parts[k];
+    stats[9] = c->H.join ? 1 : 0;
   });
 }
 

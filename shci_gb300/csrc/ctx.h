@@ -34,12 +34,26 @@ struct DetIndex {
   DevBuf<uint64_t> bs_str;                // their beta strings
 };
 
+// Two-hole core join of the det list (hjoin.cu): every det contributes one entry per pair of
+// its electrons; entries are sorted by a hash of the det minus that pair.
+struct JoinIndex {
+  uint32_t K = 0;               // entries per det = C(n_up + n_dn, 2)
+  int n_up = 0, n_dn = 0;
+  size_t m = 0;                 // n * K entries
+  DevBuf<uint32_t> pairs;       // [K] electron ranks r1 | r2 << 16 (r1 < r2)
+  DevBuf<uint64_t> keys;        // [m] core hashes (sort keys; released after bucketing)
+  DevBuf<uint32_t> jdet;        // [m] det id of each sorted entry
+  DevBuf<uint64_t> span;        // [m] per entry (in det order): sorted position | bucket end << 32
+};
+
 // Upper-triangle Hamiltonian (strict upper part in CSR; FP64 diagonal kept apart).
 struct DevHamiltonian {
   size_t n = 0;
   size_t nnz = 0;
-  size_t candidates = 0;  // (row, candidate) pairs scanned by the last build
-  size_t cand_parts[3] = {0, 0, 0};  // same beta, same alpha, alpha single x beta single
+  bool join = false;      // built by the core join (else by the group scan)
+  size_t candidates = 0;  // (row, candidate) pairs examined by the last build
+  size_t cand_parts[3] = {0, 0, 0};  // scan: same beta, same alpha, alpha single x beta single;
+                                     // join: core entries, 0, 0
   int precision = SHCI_PREC_FP64;
   DevBuf<uint64_t> row_ptr;   // [n+1]
   DevBuf<uint32_t> col;       // [nnz]
@@ -99,6 +113,7 @@ struct shci_ctx {
   std::vector<double> eps_tried;
 
   shci::DetIndex idx;
+  shci::JoinIndex join;
   shci::DevHamiltonian H;
   shci::Davidson dav;
   shci::SortScratch sort;

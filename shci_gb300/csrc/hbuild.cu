@@ -20,7 +20,11 @@
 // element set the reference builds (its incremental update only changes the order in which
 // rows are filled).  A count pass sizes each row, a scan gives row offsets, and a fill pass
 // writes columns / values in the same deterministic traversal order.
+#include <cstdlib>
+#include <cstring>
+
 #include "ctx.h"
+#include "hrow.cuh"
 #include "kernels.h"
 
 namespace shci {
@@ -28,10 +32,6 @@ namespace shci {
 namespace {
 
 constexpr int kWarps = 8;  // warps per block in the row kernels
-
-__device__ __forceinline__ unsigned lanemask_lt() {
-  return (1u << (threadIdx.x & 31)) - 1u;
-}
 
 __global__ void k_group_flags(const uint64_t* sorted, size_t n, uint32_t* flags) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
@@ -142,22 +142,7 @@ __global__ void k_hdiag(DevIntegrals I, const uint64_t* __restrict__ up,
     diag[i] = h_diag(I, up[i], dn[i]);
 }
 
-// Candidate columns that pass the excitation-degree test wait in two per-warp ring buffers,
-// one for single and one for double excitations, and are evaluated 32 at a time.  A scan
-// finds a connected column for about one lane in thirty, and GB300 issues an FP64 warp
-// instruction at 1/16 per SM cycle however many lanes are active, so evaluating in place
-// would run the matrix-element arithmetic with one useful lane; separate queues keep the
-// long single-excitation sums apart from the short double-excitation ones.
-constexpr uint32_t kQ = 64;  // ring size: < 32 waiting + 32 pushed always fit
-struct RowQueues {
-  uint32_t j[2][kQ];
-  uint64_t u[2][kQ];
-  uint64_t d[2][kQ];
-};
-
-// MODE 0: count, MODE 1: fill FP64, MODE 2: fill mixed (FP32 value + FP32 residual).
-// Count and fill run the same traversal and drain the queues at the same points, so a row's
-// columns land in the same deterministic order in every build.
+// Scan traversal.  MODE 0: count, MODE 1: fill FP64, MODE 2: fill mixed (RowSink).
 template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
     k_hbuild(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
@@ -166,7 +151,6 @@ __global__ void __launch_bounds__(kWarps * 32)
   __shared__ RowQueues qs[kWarps];
   RowQueues& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
-  const unsigned lt = lanemask_lt();
   while (true) {
     uint32_t i = 0;
     if (lane == 0) i = atomicAdd(work, 1u);
@@ -174,56 +158,10 @@ __global__ void __launch_bounds__(kWarps * 32)
     if (i >= n) break;
     const uint64_t ui = up[i], di = dn[i];
     const uint32_t a = ix.det_aid[i], b = ix.det_bid[i];
-    const uint64_t base = MODE ? row_ptr[i] : 0;
-    uint32_t cnt = 0;
+    RowSink<MODE> sink(q, I, ui, di, MODE ? row_ptr[i] : 0, col, v64, v32, r32);
     uint64_t n_scan_a = 0, n_scan_b = 0, n_mixed = 0;
-    uint32_t qh[2] = {0u, 0u}, qn[2] = {0u, 0u};  // ring heads and lengths (warp-uniform)
-    // evaluate the m <= 32 oldest entries of queue t, keep |H| >= 1e-12, write kept ones
-    auto drain = [&](int t, uint32_t m) {
-      __syncwarp();
-      bool keep = false;
-      uint32_t j = 0;
-      double H = 0.0;
-      if (lane < m) {
-        const uint32_t s = (qh[t] + lane) & (kQ - 1);
-        j = q.j[t][s];
-        const uint64_t uj = q.u[t][s], dj = q.d[t][s];
-        H = t == 0 ? h_one(I, ui, di, uj, dj) : h_two(I, ui, di, uj, dj);
-        keep = keep_elem(H);
-      }
-      __syncwarp();
-      qh[t] += m;
-      qn[t] -= m;
-      const unsigned bal = __ballot_sync(kFull, keep);
-      if (MODE && keep) {
-        const uint64_t pos = base + cnt + __popc(bal & lt);
-        col[pos] = j;
-        if (MODE == 1) {
-          v64[pos] = H;
-        } else {
-          const float hi = static_cast<float>(H);
-          v32[pos] = hi;
-          r32[pos] = static_cast<float>(H - static_cast<double>(hi));
-        }
-      }
-      cnt += __popc(bal);
-    };
-    // queue the lanes' candidates (cand), as singles or doubles, draining full queues
     auto push = [&](bool cand, bool single, uint32_t j, uint64_t uj, uint64_t dj) {
-#pragma unroll
-      for (int t = 0; t < 2; t++) {
-        const bool mine = cand && (single == (t == 0));
-        const unsigned bal = __ballot_sync(kFull, mine);
-        if (!bal) continue;
-        if (mine) {
-          const uint32_t s = (qh[t] + qn[t] + __popc(bal & lt)) & (kQ - 1);
-          q.j[t][s] = j;
-          q.u[t][s] = uj;
-          q.d[t][s] = dj;
-        }
-        qn[t] += __popc(bal);
-        if (qn[t] >= 32u) drain(t, 32u);
-      }
+      sink.push(cand, single, j, uj, dj);
     };
     // (a) same beta string: beta group in det-id order, from the first j > i
     {
@@ -347,8 +285,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         }
       }
     }
-    if (qn[0]) drain(0, qn[0]);
-    if (qn[1]) drain(1, qn[1]);
+    const uint32_t cnt = sink.finish();
     if (MODE == 0 && lane == 0) {
       row_cnt[i] = cnt;
       // candidates examined by this row, per part
@@ -468,6 +405,10 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.n = n;
   H.precision = precision;
   H.valid = false;
+  const char* force = std::getenv("SHCI_HBUILD");
+  const bool scan_only = force && std::strcmp(force, "scan") == 0;
+  H.join = !scan_only && join_prepare(c);
+  if (!H.join) build_index(c);
   H.row_ptr.resize(n + 1, 1.25);
   H.row_cnt.resize(n + 1, 1.25);
   H.diag.resize(n, 1.25);
@@ -486,10 +427,14 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
     k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n,
                                              H.diag.p);
     SHCI_LAUNCH_CHECK();
-    k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                             H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                             nullptr, work);
-    SHCI_LAUNCH_CHECK();
+    if (H.join) {
+      join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid);
+    } else {
+      k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                               H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
+                                               nullptr, work);
+      SHCI_LAUNCH_CHECK();
+    }
   }
   // row_ptr = exclusive scan of counts (counts widened to 64 bit)
   widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
@@ -501,6 +446,10 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.nnz = nnz;
   H.candidates = cand[0] + cand[1] + cand[2];
   for (int k = 0; k < 3; k++) H.cand_parts[k] = cand[k];
+  if (H.join) {
+    H.cand_parts[0] = c->join.m;
+    H.cand_parts[1] = H.cand_parts[2] = 0;
+  }
   const size_t cap = nnz ? nnz : 1;
   H.col.resize(cap, 1.1);
   if (precision == SHCI_PREC_FP64) {
@@ -515,7 +464,10 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
   {
     ProfScope ps(c->prof, s, "hbuild_fill");
-    if (precision == SHCI_PREC_FP64) {
+    if (H.join) {
+      join_rows(c, precision == SHCI_PREC_FP64 ? 1 : 2, nullptr, H.row_ptr.p, H.col.p,
+                H.val64.p, H.val32.p, H.res32.p, work, grid);
+    } else if (precision == SHCI_PREC_FP64) {
       k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                nullptr, H.row_ptr.p, H.col.p, H.val64.p,
                                                nullptr, nullptr, work);
@@ -527,6 +479,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
     SHCI_LAUNCH_CHECK();
   }
   SHCI_CUDA(cudaStreamSynchronize(s));
+  if (H.join) join_release(c);
   c->prof.flush();
   H.valid = true;
   c->launches += 5;

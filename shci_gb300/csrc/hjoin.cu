@@ -1,0 +1,286 @@
+// Hamiltonian build by a two-hole core join.
+//
+// Two determinants with the same electron counts are connected by at most a double
+// excitation exactly when they share an (n_e - 2)-electron "core": the det with some pair of
+// its electrons removed.  Every det contributes K = C(n_e, 2) entries, one per electron pair
+// (alpha-alpha, beta-beta or alpha-beta), keyed by a hash of its core.  After a stable sort by
+// key, each bucket of equal keys holds, in det-id order, dets that share a core (plus, rarely,
+// dets whose different cores hash alike).  Row i then examines, for each of its K entries,
+// only the members after its own entry in that bucket: exactly the dets j > i sharing that
+// core.  This finds the same element set as the group scan of the reference's
+// Hamiltonian<S>::update_matrix (src/solver/hamiltonian.h:415-598: same-alpha, same-beta and
+// alpha-single x beta-single partners) while examining about 1.4 candidates per stored
+// element instead of tens.
+//
+// A pair (i, j) shares one core if it is a double excitation and n_e - 1 cores if it is a
+// single; it is taken only from its canonical core: the two electrons of i absent from j
+// (double), or the electron of i absent from j plus the lowest electron the two share, alpha
+// orbitals before beta ones (single).  The test uses the actual spin strings, so a hash
+// collision can only add candidates that fail it; the one collision that could repeat a
+// column (two cores of j in one bucket, adjacent by construction) is skipped explicitly.
+//
+// Used when n_e >= 2, n * K < 2^32 and the index fits in memory; otherwise the scan path
+// (hbuild.cu) builds the matrix.
+#include <algorithm>
+#include <cstdlib>
+#include <vector>
+
+#include "ctx.h"
+#include "heatbath.cuh"
+#include "hrow.cuh"
+#include "kernels.h"
+
+namespace shci {
+
+namespace {
+
+constexpr int kJoinWarps = 8;
+
+__device__ __forceinline__ uint64_t core_hash(uint64_t cu, uint64_t cd) {
+  uint64_t h = cu * 0x9E3779B97F4A7C15ull ^ (cd + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full;
+  h ^= h >> 29;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 32;
+  return h;
+}
+
+// Removed-electron masks (alpha, beta) of pair entry k of det (u, d).
+__device__ __forceinline__ void pair_masks(uint32_t pr, uint64_t u, uint64_t d, int n_up,
+                                           uint64_t* ru, uint64_t* rd) {
+  const int r1 = static_cast<int>(pr & 0xffffu), r2 = static_cast<int>(pr >> 16);
+  uint64_t a = 0, b = 0;
+  if (r1 < n_up) a |= 1ull << nth_bit(u, r1);
+  else b |= 1ull << nth_bit(d, r1 - n_up);
+  if (r2 < n_up) a |= 1ull << nth_bit(u, r2);
+  else b |= 1ull << nth_bit(d, r2 - n_up);
+  *ru = a;
+  *rd = b;
+}
+
+// Entries in det order: key = top `bits` bits of the core hash, value = entry index.
+__global__ void k_core_keys(const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
+                            uint32_t n, const uint32_t* __restrict__ pairs, uint32_t K, int n_up,
+                            int n_dn, int bits, uint64_t* keys, uint32_t* vals, unsigned* err) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = warp0; i < n; i += n_warps) {
+    const uint64_t u = up[i], d = dn[i];
+    if (popc64(u) != n_up || popc64(d) != n_dn) {
+      if (lane == 0) atomicOr(err, (unsigned)kDevCheck);
+      continue;
+    }
+    for (uint32_t k = lane; k < K; k += 32) {
+      uint64_t ru, rd;
+      pair_masks(pairs[k], u, d, n_up, &ru, &rd);
+      const size_t t = (size_t)i * K + k;
+      keys[t] = core_hash(u & ~ru, d & ~rd) >> (64 - bits);
+      vals[t] = static_cast<uint32_t>(t);
+    }
+  }
+}
+
+// After the sort: for every bucket [p, e), span[entry] = position | e << 32 for each member,
+// and jdet[position] = det id of the entry there (written over the entry index in place).
+__global__ void k_core_buckets(const uint64_t* __restrict__ keys, uint32_t* vals, size_t m,
+                               uint32_t K, uint64_t* span) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < m;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t key = keys[p];
+    if (p > 0 && keys[p - 1] == key) continue;
+    size_t e = p + 1;
+    while (e < m && keys[e] == key) e++;
+    for (size_t q = p; q < e; q++) {
+      const uint32_t v = vals[q];
+      span[v] = static_cast<uint64_t>(q) | (static_cast<uint64_t>(e) << 32);
+      vals[q] = v / K;
+    }
+  }
+}
+
+}  // namespace
+
+namespace {
+
+struct JoinView {
+  uint32_t K;
+  int n_up;
+  const uint32_t* pairs;
+  const uint64_t* span;
+  const uint32_t* jdet;
+};
+
+// Row kernel of the join (MODE as in RowSink).  A warp per row: lanes take the row's entries
+// 32 at a time, the members after each entry are flattened over the lanes, and every member
+// that passes the canonical-core test goes to the row's queues.
+template <int MODE>
+__global__ void __launch_bounds__(kJoinWarps * 32)
+    k_hjoin(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
+            uint32_t n, JoinView jv, uint32_t* row_cnt, const uint64_t* row_ptr, uint32_t* col,
+            double* v64, float* v32, float* r32, unsigned* work) {
+  __shared__ RowQueues qs[kJoinWarps];
+  RowQueues& q = qs[threadIdx.x >> 5];
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t K = jv.K;
+  while (true) {
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(work, 1u);
+    i = __shfl_sync(kFull, i, 0);
+    if (i >= n) break;
+    const uint64_t ui = up[i], di = dn[i];
+    RowSink<MODE> sink(q, I, ui, di, MODE ? row_ptr[i] : 0, col, v64, v32, r32);
+    uint64_t n_cand = 0;
+    for (uint32_t k0 = 0; k0 < K; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      uint32_t p = 0, len = 0;
+      uint64_t ru = 0, rd = 0;
+      if (k < K) {
+        const uint64_t sp = jv.span[(size_t)i * K + k];
+        p = static_cast<uint32_t>(sp);
+        len = static_cast<uint32_t>(sp >> 32) - p - 1u;
+        pair_masks(jv.pairs[k], ui, di, jv.n_up, &ru, &rd);
+      }
+      const uint32_t inc = warp_inclusive_u32(len);
+      const uint32_t total = __shfl_sync(kFull, inc, 31);
+      n_cand += total;
+      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        const uint32_t o = owner_lane(inc, t);
+        const uint32_t o_inc = __shfl_sync(kFull, inc, o);
+        const uint32_t o_len = __shfl_sync(kFull, len, o);
+        const uint32_t o_p = __shfl_sync(kFull, p, o);
+        const uint64_t o_ru = __shfl_sync(kFull, ru, o);
+        const uint64_t o_rd = __shfl_sync(kFull, rd, o);
+        bool cand = false, single = false;
+        uint32_t j = 0;
+        uint64_t uj = 0, dj = 0;
+        if (t < total) {
+          const uint32_t pos = o_p + 1u + (t - (o_inc - o_len));
+          j = jv.jdet[pos];
+          // a second entry of j in this bucket (its two cores hashed alike) sits right after
+          // the first; take j once
+          const bool repeat = pos > o_p + 1u && jv.jdet[pos - 1u] == j;
+          if (!repeat) {
+            uj = up[j];
+            dj = dn[j];
+            const uint64_t xu = ui ^ uj, xd = di ^ dj;
+            const int x2 = popc64(xu) + popc64(xd);
+            const uint64_t iu = ui & xu, id = di & xd;  // electrons of i absent from j
+            if (x2 == 4) {
+              cand = o_ru == iu && o_rd == id;
+            } else if (x2 == 2) {
+              const uint64_t cu = ui & uj, cd = di & dj;
+              const uint64_t lu = cu & (~cu + 1ull);
+              const uint64_t ld = cu ? 0ull : (cd & (~cd + 1ull));
+              cand = o_ru == (iu | lu) && o_rd == (id | ld);
+              single = true;
+            }
+          }
+        }
+        sink.push(cand, single, j, uj, dj);
+      }
+    }
+    const uint32_t cnt = sink.finish();
+    if (MODE == 0 && lane == 0) {
+      row_cnt[i] = cnt;
+      atomicAdd(reinterpret_cast<unsigned long long*>(work + 2), (unsigned long long)n_cand);
+    }
+  }
+}
+
+}  // namespace
+
+bool join_prepare(shci_ctx* c) {
+  auto& J = c->join;
+  const size_t n = c->up.size();
+  cudaStream_t s = c->stream;
+  if (n == 0) return false;
+  const int n_up = __builtin_popcountll(c->up[0]), n_dn = __builtin_popcountll(c->dn[0]);
+  const int ne = n_up + n_dn;
+  if (ne < 2 || ne > 128) return false;
+  const uint64_t K = static_cast<uint64_t>(ne) * (ne - 1) / 2;
+  const uint64_t m = n * K;
+  if (m >= 0xffffffffull) return false;
+  // memory: keys + sort ping-pong (16 B), entry values + ping-pong (8 B), then span (8 B)
+  size_t free_b = 0, total_b = 0;
+  SHCI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  size_t avail = free_b;
+  if (c->mem.budget) avail = std::min(avail, c->mem.budget > c->mem.used ? c->mem.budget - c->mem.used : 0);
+  if (static_cast<double>(m) * 26.0 > 0.85 * static_cast<double>(avail)) return false;
+  J.K = static_cast<uint32_t>(K);
+  J.n_up = n_up;
+  J.n_dn = n_dn;
+  J.m = m;
+  ProfScope ps(c->prof, s, "core_join");
+  try {
+    std::vector<uint32_t> pr;
+    pr.reserve(K);
+    for (int r1 = 0; r1 < ne; r1++)
+      for (int r2 = r1 + 1; r2 < ne; r2++) pr.push_back(static_cast<uint32_t>(r1 | (r2 << 16)));
+    J.pairs.resize(K);
+    SHCI_CUDA(cudaMemcpyAsync(J.pairs.p, pr.data(), K * 4, cudaMemcpyHostToDevice, s));
+    // hash bits: 32 while the entries are few enough that merged buckets stay rare.
+    // SHCI_JOIN_BITS (4..40) narrows it, so tests can force colliding buckets.
+    int bits = m <= (1ull << 30) ? 32 : 40;
+    if (const char* e = std::getenv("SHCI_JOIN_BITS")) bits = std::min(40, std::max(4, std::atoi(e)));
+    J.keys.resize(m);
+    J.jdet.resize(m);
+    c->err_word.resize(8);
+    SHCI_CUDA(cudaMemsetAsync(c->err_word.p, 0, 4, s));
+    k_core_keys<<<grid_for((size_t)n * 32, 256), 256, 0, s>>>(
+        c->d_up.p, c->d_dn.p, static_cast<uint32_t>(n), J.pairs.p, J.K, n_up, n_dn, bits,
+        J.keys.p, J.jdet.p, c->err_word.p);
+    SHCI_LAUNCH_CHECK();
+    unsigned err = 0;
+    SHCI_CUDA(cudaMemcpyAsync(&err, c->err_word.p, 4, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    if (err) throw ArgError("dets do not all have the electron counts of the first det");
+    radix_sort_pairs(J.keys, J.jdet, m, 0, bits, s, c->sort);
+    // the sort's ping-pong storage is not needed again for this build
+    c->sort.kalt.release();
+    c->sort.valt32.release();
+    J.span.resize(m);
+    k_core_buckets<<<grid_for(m, 256), 256, 0, s>>>(J.keys.p, J.jdet.p, m, J.K, J.span.p);
+    SHCI_LAUNCH_CHECK();
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    J.keys.release();
+    c->launches += 12;
+  } catch (const OomError&) {
+    join_release(c);
+    c->sort.kalt.release();
+    c->sort.valt32.release();
+    return false;
+  }
+  return true;
+}
+
+void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
+               uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
+               unsigned grid) {
+  const auto& J = c->join;
+  const uint32_t n = static_cast<uint32_t>(c->up.size());
+  JoinView v{J.K, J.n_up, J.pairs.p, J.span.p, J.jdet.p};
+  cudaStream_t s = c->stream;
+  if (mode == 0)
+    k_hjoin<0><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, row_cnt,
+                                                 nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                 work);
+  else if (mode == 1)
+    k_hjoin<1><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
+                                                 row_ptr, col, v64, nullptr, nullptr, work);
+  else
+    k_hjoin<2><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
+                                                 row_ptr, col, nullptr, v32, r32, work);
+  SHCI_LAUNCH_CHECK();
+  c->launches += 1;
+}
+
+void join_release(shci_ctx* c) {
+  auto& J = c->join;
+  J.keys.release();
+  J.jdet.release();
+  J.span.release();
+  J.m = 0;
+}
+
+}  // namespace shci

@@ -25,9 +25,18 @@ void hamiltonian_elems(shci_ctx* c, const uint64_t* ui, const uint64_t* di, cons
 void hamiltonian_elems_noalloc(shci_ctx* c, const uint64_t* ui, const uint64_t* di,
                                const uint64_t* uj, const uint64_t* dj, size_t n, double* out);
 
-// hbuild.cu
+// hbuild.cu: group index + scan traversal, and the build driver (join when possible, else
+// scan; the SHCI_HBUILD environment variable set to "scan" forces the scan)
 void build_index(shci_ctx* c);
 size_t build_hamiltonian(shci_ctx* c, int precision);
+
+// hjoin.cu: two-hole core join.  join_prepare returns false (nothing held) when the join
+// cannot be used for the current dets; join_rows runs one pass (mode as the row kernels).
+bool join_prepare(shci_ctx* c);
+void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
+               uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
+               unsigned grid);
+void join_release(shci_ctx* c);
 
 // spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
 void spmv(shci_ctx* c, const double* x, double* y, bool residual);

@@ -19,7 +19,6 @@ static double run_variation(shci_ctx* c, double eps_var, bool until_converged, d
   while (!converged) {
     if (!dets_converged) {
       n_dets_new = n_dets + select_dets(c, eps_var, var_sd);
-      build_index(c);
       build_hamiltonian(c, precision);
     }
     const double tol = until_converged ? target_error / 500000 : target_error / 50;
