@@ -351,13 +351,16 @@ def run_ours(args):
     # u32 column + FP32 value + FP32 residual).  Core join: each row reads its entries' bucket
     # spans (8 B per entry) and the det id of each candidate (4 B); the candidates' spin
     # strings are gathered from the L2-resident det list.  Building the join writes keys and
-    # entry ids (12 B/entry), sorts them (4 passes x 24 B/entry) and writes spans and det ids
-    # (read 12 B, write 12 B per entry).  H*v: read the store once (col + FP32 value = 8
+    # entry ids (4 B keys + 4 B ids per entry), sorts them (4 passes; each reads the keys for
+    # the histogram, then reads and writes keys and ids: 20 B/entry) and writes spans and det
+    # ids (read 8 B, write 12 B per entry).  H*v: read the store once (col + FP32 value = 8
     # B/element), row offsets, x (twice), y read-modify-write and the diagonal.
     alg = {
         "hbuild_count": 16.0 * n + 4 * n + 8 * n + 8.0 * m + 4.0 * cand * (m > 0),
         "hbuild_fill": 16.0 * n + 8 * (n + 1) + 12.0 * nnz + (8.0 * m + 4.0 * cand) * (m > 0),
-        "core_join": 132.0 * m,
+        "join_keys": 16.0 * n + 8.0 * m,
+        "join_sort": 4 * 20.0 * m,
+        "join_buckets": 20.0 * m,
         "spmv": 8.0 * nnz + 8 * (n + 1) + 16 * n + 16 * n + 8 * n,
     }
     kernels = {}

@@ -94,11 +94,13 @@ shci_status shci_create(shci_ctx** out, int device, size_t hbm_budget_bytes) {
       b->mt = &c->mem;
     for (auto* b : {&ix.am_dn, &ix.ad_dn, &ix.bd_up, &ix.ua, &ix.ub, &ix.bs_str}) b->mt = &c->mem;
     c->join.pairs.mt = c->join.jdet.mt = &c->mem;
-    c->join.keys.mt = c->join.span.mt = &c->mem;
+    c->join.keys.mt = c->join.span.mt = c->join.keys32.mt = &c->mem;
+    c->join.scan.mt = c->join.bstart.mt = &c->mem;
     auto& H = c->H;
     H.row_ptr.mt = H.col.mt = H.row_cnt.mt = &c->mem;
     H.val64.mt = H.diag.mt = &c->mem;
     H.val32.mt = H.res32.mt = &c->mem;
+    H.scal.mt = H.xs.mt = H.yfix.mt = H.rowabs.mt = &c->mem;
     c->dav.scal.mt = c->dav.partial.mt = &c->mem;
   });
   if (st != SHCI_OK) {

@@ -131,7 +131,22 @@ __device__ __forceinline__ double h_single(const DevIntegrals& I, uint64_t same,
 // Parity helper of src/det/half_det.cc:120-206 for one moved orbital: electrons of `s` below b.
 __device__ __forceinline__ int below_count(uint64_t s, int b) { return popc64(s & below(b)); }
 
+// Bits strictly between orbitals a != b.
+__device__ __forceinline__ uint64_t between(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return ((1ull << hi) - 1ull) & ~((2ull << lo) - 1ull);
+}
+
+// Parity of moving one electron from orbital a of string s to orbital b (b not in s):
+// below_count(s, a) + below_count(s ^ a ^ b, b) has the parity of the electrons strictly
+// between a and b (the electrons below min(a, b) are counted twice).
+__device__ __forceinline__ int move_parity(uint64_t s, int a, int b) {
+  return popc64(s & between(a, b));
+}
+
 // H_ij for a single excitation: exactly one of ui^uj, di^dj is non-zero, with two bits set.
+// SIGNED = false returns the value up to its sign (enough for the |H| >= 1e-12 test).
+template <bool SIGNED = true>
 __device__ __forceinline__ double h_one(const DevIntegrals& I, uint64_t ui, uint64_t di,
                                         uint64_t uj, uint64_t dj) {
   const uint64_t xu = ui ^ uj;
@@ -139,20 +154,20 @@ __device__ __forceinline__ double h_one(const DevIntegrals& I, uint64_t ui, uint
   const uint64_t si = alpha ? ui : di, sj = alpha ? uj : dj, oi_str = alpha ? di : ui;
   const uint64_t x = si ^ sj;
   const int oi = ctz64(si & x), oj = ctz64(sj & x);
-  const int par = below_count(si, oi) + below_count(sj, oj);
-  return h_single(I, si, oi_str, oi, oj, par);
+  return h_single(I, si, oi_str, oi, oj, SIGNED ? move_parity(si, oi, oj) : 0);
 }
 
 // H_ij for a double excitation (one alpha + one beta electron, or two of the same spin).
+template <bool SIGNED = true>
 __device__ __forceinline__ double h_two(const DevIntegrals& I, uint64_t ui, uint64_t di,
                                         uint64_t uj, uint64_t dj) {
   const uint64_t xu = ui ^ uj, xd = di ^ dj;
   if (xu && xd) {
     const int ai = ctz64(ui & xu), aj = ctz64(uj & xu);
     const int bi = ctz64(di & xd), bj = ctz64(dj & xd);
-    const int par = below_count(ui, ai) + below_count(uj, aj) + below_count(di, bi) +
-                    below_count(dj, bj);
-    return flip_sign(g2at(I, ai, aj, bi, bj), par);
+    const double g = g2at(I, ai, aj, bi, bj);
+    if (!SIGNED) return g;
+    return flip_sign(g, move_parity(ui, ai, aj) + move_parity(di, bi, bj));
   }
   // same-spin double
   const bool alpha = xu != 0;
@@ -160,9 +175,11 @@ __device__ __forceinline__ double h_two(const DevIntegrals& I, uint64_t ui, uint
   const uint64_t li = si & x, rj = sj & x;
   const int l0 = ctz64(li), l1 = ctz64(li & (li - 1));
   const int r0 = ctz64(rj), r1 = ctz64(rj & (rj - 1));
+  const double e = g2at(I, l0, r0, l1, r1) - g2at(I, l0, r1, l1, r0);
+  if (!SIGNED) return e;
   const int par = below_count(si, l0) + below_count(si, l1) + below_count(sj, r0) +
                   below_count(sj, r1);
-  return flip_sign(g2at(I, l0, r0, l1, r1) - g2at(I, l0, r1, l1, r0), par);
+  return flip_sign(e, par);
 }
 
 // H_ij for dets whose excitation degree is known to be 1 or 2 (or 0: diagonal).  up/dn

@@ -41,7 +41,11 @@ struct JoinIndex {
   int n_up = 0, n_dn = 0;
   size_t m = 0;                 // n * K entries
   DevBuf<uint32_t> pairs;       // [K] electron ranks r1 | r2 << 16 (r1 < r2)
+  int bits = 0, key_bytes = 0;  // hash bits kept; key width used by the last index
   DevBuf<uint64_t> keys;        // [m] core hashes (sort keys; released after bucketing)
+  DevBuf<uint32_t> keys32;      //     the same when at most 32 hash bits are kept
+  DevBuf<uint32_t> scan;        // [m] bucket index of each sorted position (while bucketing)
+  DevBuf<uint32_t> bstart;      // [buckets + 1] bucket start positions (while bucketing)
   DevBuf<uint32_t> jdet;        // [m] det id of each sorted entry
   DevBuf<uint64_t> span;        // [m] per entry (in det order): sorted position | bucket end << 32
 };
@@ -63,6 +67,12 @@ struct DevHamiltonian {
   DevBuf<double> diag;        // [n]
   DevBuf<uint32_t> row_cnt;   // [n] scratch
   bool valid = false;
+  // mixed-storage H*v (spmv.cu): row abs-sum bound and fixed-point scratch
+  bool bound_valid = false;
+  DevBuf<double> scal;        // [0] max row abs sum, [1] max |x| (bits), [2] spare
+  DevBuf<float> xs;           // [2n] x split into float pairs
+  DevBuf<unsigned long long> yfix;  // [n] y in 64-bit fixed point
+  DevBuf<float> rowabs;       // [n] scratch for the bound
 };
 
 struct DevQueues {

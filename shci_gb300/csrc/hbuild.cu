@@ -147,7 +147,8 @@ template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
     k_hbuild(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
              uint32_t n, IndexView ix, uint32_t* row_cnt, const uint64_t* row_ptr,
-             uint32_t* col, double* v64, float* v32, float* r32, unsigned* work) {
+             uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
+             float* absacc) {
   __shared__ RowQueues qs[kWarps];
   RowQueues& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
@@ -159,6 +160,7 @@ __global__ void __launch_bounds__(kWarps * 32)
     const uint64_t ui = up[i], di = dn[i];
     const uint32_t a = ix.det_aid[i], b = ix.det_bid[i];
     RowSink<MODE> sink(q, I, ui, di, MODE ? row_ptr[i] : 0, col, v64, v32, r32);
+    if (MODE == 0 && absacc) sink.track_abs(absacc, i);
     uint64_t n_scan_a = 0, n_scan_b = 0, n_mixed = 0;
     auto push = [&](bool cand, bool single, uint32_t j, uint64_t uj, uint64_t dj) {
       sink.push(cand, single, j, uj, dj);
@@ -405,6 +407,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.n = n;
   H.precision = precision;
   H.valid = false;
+  H.bound_valid = false;
   const char* force = std::getenv("SHCI_HBUILD");
   const bool scan_only = force && std::strcmp(force, "scan") == 0;
   H.join = !scan_only && join_prepare(c);
@@ -422,17 +425,25 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
   SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
+  // a mixed build also sums |H_ij| per det during the count (the H*v fixed-point bound)
+  float* absacc = nullptr;
+  if (precision == SHCI_PREC_MIXED) {
+    H.rowabs.resize(n, 1.1);
+    SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
+    absacc = H.rowabs.p;
+  }
   {
     ProfScope ps(c->prof, s, "hbuild_count");
     k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n,
                                              H.diag.p);
     SHCI_LAUNCH_CHECK();
     if (H.join) {
-      join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid);
+      join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid,
+                absacc);
     } else {
       k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                               nullptr, work);
+                                               nullptr, work, absacc);
       SHCI_LAUNCH_CHECK();
     }
   }
@@ -443,6 +454,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   unsigned long long cand[3] = {0, 0, 0};
   SHCI_CUDA(cudaMemcpyAsync(cand, work + 2, 24, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
+  if (absacc) finish_mixed_bound(c);
   H.nnz = nnz;
   H.candidates = cand[0] + cand[1] + cand[2];
   for (int k = 0; k < 3; k++) H.cand_parts[k] = cand[k];
@@ -466,15 +478,15 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
     ProfScope ps(c->prof, s, "hbuild_fill");
     if (H.join) {
       join_rows(c, precision == SHCI_PREC_FP64 ? 1 : 2, nullptr, H.row_ptr.p, H.col.p,
-                H.val64.p, H.val32.p, H.res32.p, work, grid);
+                H.val64.p, H.val32.p, H.res32.p, work, grid, nullptr);
     } else if (precision == SHCI_PREC_FP64) {
       k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                nullptr, H.row_ptr.p, H.col.p, H.val64.p,
-                                               nullptr, nullptr, work);
+                                               nullptr, nullptr, work, nullptr);
     } else {
       k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
-                                               H.res32.p, work);
+                                               H.res32.p, work, nullptr);
     }
     SHCI_LAUNCH_CHECK();
   }

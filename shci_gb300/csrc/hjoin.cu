@@ -58,9 +58,10 @@ __device__ __forceinline__ void pair_masks(uint32_t pr, uint64_t u, uint64_t d, 
 }
 
 // Entries in det order: key = top `bits` bits of the core hash, value = entry index.
+template <class KT>
 __global__ void k_core_keys(const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
                             uint32_t n, const uint32_t* __restrict__ pairs, uint32_t K, int n_up,
-                            int n_dn, int bits, uint64_t* keys, uint32_t* vals, unsigned* err) {
+                            int n_dn, int bits, KT* keys, uint32_t* vals, unsigned* err) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -74,27 +75,46 @@ __global__ void k_core_keys(const uint64_t* __restrict__ up, const uint64_t* __r
       uint64_t ru, rd;
       pair_masks(pairs[k], u, d, n_up, &ru, &rd);
       const size_t t = (size_t)i * K + k;
-      keys[t] = core_hash(u & ~ru, d & ~rd) >> (64 - bits);
+      keys[t] = static_cast<KT>(core_hash(u & ~ru, d & ~rd) >> (64 - bits));
       vals[t] = static_cast<uint32_t>(t);
     }
   }
 }
 
-// After the sort: for every bucket [p, e), span[entry] = position | e << 32 for each member,
-// and jdet[position] = det id of the entry there (written over the entry index in place).
-__global__ void k_core_buckets(const uint64_t* __restrict__ keys, uint32_t* vals, size_t m,
+// After the sort, buckets in three parallel steps: flag bucket starts, scan the flags
+// (bucket index of every position), record each bucket's start; then every position p of
+// bucket b writes span[entry] = p | end(b) << 32 and jdet[p] = det id (over the entry index).
+template <class KT>
+__device__ __forceinline__ uint32_t bucket_head(const KT* keys, size_t p) {
+  return (p == 0 || keys[p] != keys[p - 1]) ? 1u : 0u;
+}
+
+template <class KT>
+__global__ void k_bucket_flags(const KT* __restrict__ keys, size_t m, uint32_t* flags) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < m;
+       p += (size_t)gridDim.x * blockDim.x)
+    flags[p] = bucket_head(keys, p);
+}
+
+template <class KT>
+__global__ void k_bucket_starts(const KT* __restrict__ keys, const uint32_t* __restrict__ scan,
+                                size_t m, uint32_t n_buckets, uint32_t* bstart) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < m;
+       p += (size_t)gridDim.x * blockDim.x)
+    if (bucket_head(keys, p)) bstart[scan[p]] = static_cast<uint32_t>(p);
+  if (blockIdx.x == 0 && threadIdx.x == 0) bstart[n_buckets] = static_cast<uint32_t>(m);
+}
+
+template <class KT>
+__global__ void k_bucket_spans(const KT* __restrict__ keys, const uint32_t* __restrict__ scan,
+                               const uint32_t* __restrict__ bstart, uint32_t* vals, size_t m,
                                uint32_t K, uint64_t* span) {
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < m;
        p += (size_t)gridDim.x * blockDim.x) {
-    const uint64_t key = keys[p];
-    if (p > 0 && keys[p - 1] == key) continue;
-    size_t e = p + 1;
-    while (e < m && keys[e] == key) e++;
-    for (size_t q = p; q < e; q++) {
-      const uint32_t v = vals[q];
-      span[v] = static_cast<uint64_t>(q) | (static_cast<uint64_t>(e) << 32);
-      vals[q] = v / K;
-    }
+    const uint32_t b = scan[p] + bucket_head(keys, p) - 1u;
+    const uint32_t v = vals[p];
+    span[v] = static_cast<uint64_t>(p) | (static_cast<uint64_t>(bstart[b + 1]) << 32);
+    vals[p] = v / K;
   }
 }
 
@@ -117,7 +137,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kJoinWarps * 32)
     k_hjoin(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
             uint32_t n, JoinView jv, uint32_t* row_cnt, const uint64_t* row_ptr, uint32_t* col,
-            double* v64, float* v32, float* r32, unsigned* work) {
+            double* v64, float* v32, float* r32, unsigned* work, float* absacc) {
   __shared__ RowQueues qs[kJoinWarps];
   RowQueues& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
@@ -129,6 +149,7 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
     if (i >= n) break;
     const uint64_t ui = up[i], di = dn[i];
     RowSink<MODE> sink(q, I, ui, di, MODE ? row_ptr[i] : 0, col, v64, v32, r32);
+    if (MODE == 0 && absacc) sink.track_abs(absacc, i);
     uint64_t n_cand = 0;
     for (uint32_t k0 = 0; k0 < K; k0 += 32) {
       const uint32_t k = k0 + lane;
@@ -188,6 +209,69 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
   }
 }
 
+void release_sort_pingpong(shci_ctx* c) {
+  c->sort.kalt.release();
+  c->sort.kalt32.release();
+  c->sort.valt32.release();
+}
+
+void sort_keys(DevBuf<uint32_t>& k, DevBuf<uint32_t>& v, size_t m, int bits, shci_ctx* c) {
+  radix_sort_pairs32(k, v, m, 0, bits, c->stream, c->sort);
+}
+void sort_keys(DevBuf<uint64_t>& k, DevBuf<uint32_t>& v, size_t m, int bits, shci_ctx* c) {
+  radix_sort_pairs(k, v, m, 0, bits, c->stream, c->sort);
+}
+
+// Entries -> sorted buckets -> spans; keys of type KT hold `bits` hash bits.
+template <class KT>
+void join_index(shci_ctx* c, DevBuf<KT>& keys, int bits, size_t n, int n_up, int n_dn) {
+  auto& J = c->join;
+  cudaStream_t s = c->stream;
+  const size_t m = J.m;
+  keys.resize(m);
+  J.jdet.resize(m);
+  c->err_word.resize(8);
+  {
+    ProfScope ps(c->prof, s, "join_keys");
+    SHCI_CUDA(cudaMemsetAsync(c->err_word.p, 0, 4, s));
+    k_core_keys<KT><<<grid_for(n * 32, 256), 256, 0, s>>>(
+        c->d_up.p, c->d_dn.p, static_cast<uint32_t>(n), J.pairs.p, J.K, n_up, n_dn, bits,
+        keys.p, J.jdet.p, c->err_word.p);
+    SHCI_LAUNCH_CHECK();
+  }
+  unsigned err = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&err, c->err_word.p, 4, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  if (err) throw ArgError("dets do not all have the electron counts of the first det");
+  {
+    ProfScope ps(c->prof, s, "join_sort");
+    sort_keys(keys, J.jdet, m, bits, c);
+  }
+  // the sort's ping-pong storage is not needed again for this build
+  release_sort_pingpong(c);
+  J.span.resize(m);
+  J.scan.resize(m + 1);
+  {
+    ProfScope ps(c->prof, s, "join_buckets");
+    k_bucket_flags<KT><<<grid_for(m, 256), 256, 0, s>>>(keys.p, m, J.scan.p);
+    SHCI_LAUNCH_CHECK();
+    const uint32_t nb = exclusive_scan_u32(J.scan.p, J.scan.p, m, s, c->sort);
+    J.bstart.resize((size_t)nb + 1);
+    k_bucket_starts<KT><<<grid_for(m, 256), 256, 0, s>>>(keys.p, J.scan.p, m, nb, J.bstart.p);
+    SHCI_LAUNCH_CHECK();
+    k_bucket_spans<KT><<<grid_for(m, 256), 256, 0, s>>>(keys.p, J.scan.p, J.bstart.p, J.jdet.p,
+                                                          m, J.K, J.span.p);
+    SHCI_LAUNCH_CHECK();
+  }
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  keys.release();
+  J.scan.release();
+  J.bstart.release();
+  J.key_bytes = sizeof(KT);
+  J.bits = bits;
+  c->launches += 12;
+}
+
 }  // namespace
 
 bool join_prepare(shci_ctx* c) {
@@ -211,7 +295,6 @@ bool join_prepare(shci_ctx* c) {
   J.n_up = n_up;
   J.n_dn = n_dn;
   J.m = m;
-  ProfScope ps(c->prof, s, "core_join");
   try {
     std::vector<uint32_t> pr;
     pr.reserve(K);
@@ -223,32 +306,11 @@ bool join_prepare(shci_ctx* c) {
     // SHCI_JOIN_BITS (4..40) narrows it, so tests can force colliding buckets.
     int bits = m <= (1ull << 30) ? 32 : 40;
     if (const char* e = std::getenv("SHCI_JOIN_BITS")) bits = std::min(40, std::max(4, std::atoi(e)));
-    J.keys.resize(m);
-    J.jdet.resize(m);
-    c->err_word.resize(8);
-    SHCI_CUDA(cudaMemsetAsync(c->err_word.p, 0, 4, s));
-    k_core_keys<<<grid_for((size_t)n * 32, 256), 256, 0, s>>>(
-        c->d_up.p, c->d_dn.p, static_cast<uint32_t>(n), J.pairs.p, J.K, n_up, n_dn, bits,
-        J.keys.p, J.jdet.p, c->err_word.p);
-    SHCI_LAUNCH_CHECK();
-    unsigned err = 0;
-    SHCI_CUDA(cudaMemcpyAsync(&err, c->err_word.p, 4, cudaMemcpyDeviceToHost, s));
-    SHCI_CUDA(cudaStreamSynchronize(s));
-    if (err) throw ArgError("dets do not all have the electron counts of the first det");
-    radix_sort_pairs(J.keys, J.jdet, m, 0, bits, s, c->sort);
-    // the sort's ping-pong storage is not needed again for this build
-    c->sort.kalt.release();
-    c->sort.valt32.release();
-    J.span.resize(m);
-    k_core_buckets<<<grid_for(m, 256), 256, 0, s>>>(J.keys.p, J.jdet.p, m, J.K, J.span.p);
-    SHCI_LAUNCH_CHECK();
-    SHCI_CUDA(cudaStreamSynchronize(s));
-    J.keys.release();
-    c->launches += 12;
+    if (bits <= 32) join_index(c, J.keys32, bits, n, n_up, n_dn);
+    else join_index(c, J.keys, bits, n, n_up, n_dn);
   } catch (const OomError&) {
     join_release(c);
-    c->sort.kalt.release();
-    c->sort.valt32.release();
+    release_sort_pingpong(c);
     return false;
   }
   return true;
@@ -256,7 +318,7 @@ bool join_prepare(shci_ctx* c) {
 
 void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
                uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
-               unsigned grid) {
+               unsigned grid, float* absacc) {
   const auto& J = c->join;
   const uint32_t n = static_cast<uint32_t>(c->up.size());
   JoinView v{J.K, J.n_up, J.pairs.p, J.span.p, J.jdet.p};
@@ -264,13 +326,15 @@ void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr
   if (mode == 0)
     k_hjoin<0><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, row_cnt,
                                                  nullptr, nullptr, nullptr, nullptr, nullptr,
-                                                 work);
+                                                 work, absacc);
   else if (mode == 1)
     k_hjoin<1><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
-                                                 row_ptr, col, v64, nullptr, nullptr, work);
+                                                 row_ptr, col, v64, nullptr, nullptr, work,
+                                                 nullptr);
   else
     k_hjoin<2><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
-                                                 row_ptr, col, nullptr, v32, r32, work);
+                                                 row_ptr, col, nullptr, v32, r32, work,
+                                                 nullptr);
   SHCI_LAUNCH_CHECK();
   c->launches += 1;
 }
@@ -278,6 +342,9 @@ void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr
 void join_release(shci_ctx* c) {
   auto& J = c->join;
   J.keys.release();
+  J.keys32.release();
+  J.scan.release();
+  J.bstart.release();
   J.jdet.release();
   J.span.release();
   J.m = 0;

@@ -39,6 +39,9 @@ struct RowSink {
   float* r32;
   const unsigned lane, lt;
   uint32_t cnt = 0;                            // elements kept so far in this row
+  float* absacc = nullptr;                     // MODE 0: optional sums of |H| per det
+  uint32_t row = 0;
+  float rowabs = 0.0f;
   uint32_t qh[2] = {0u, 0u}, qn[2] = {0u, 0u};  // ring heads and lengths (warp-uniform)
 
   __device__ __forceinline__ RowSink(RowQueues& q_, const DevIntegrals& I_, uint64_t ui_,
@@ -57,8 +60,15 @@ struct RowSink {
       const uint32_t s = (qh[t] + lane) & (kRowQ - 1);
       j = q.j[t][s];
       const uint64_t uj = q.u[t][s], dj = q.d[t][s];
-      H = t == 0 ? h_one(I, ui, di, uj, dj) : h_two(I, ui, di, uj, dj);
+      // counting needs |H| only: skip the permutation sign (a sign flip is exact)
+      H = t == 0 ? h_one<MODE != 0>(I, ui, di, uj, dj) : h_two<MODE != 0>(I, ui, di, uj, dj);
       keep = keep_elem(H);
+      if (MODE == 0 && absacc && keep) {
+        // |H| rounded up, summed into both dets' totals (the row abs-sum bound of H*v)
+        const float a = __double2float_ru(fabs(H));
+        atomicAdd(&absacc[j], a);
+        rowabs += a;
+      }
     }
     __syncwarp();
     qh[t] += m;
@@ -101,8 +111,19 @@ struct RowSink {
   __device__ __forceinline__ uint32_t finish() {
     if (qn[0]) drain(0, qn[0]);
     if (qn[1]) drain(1, qn[1]);
+    if (MODE == 0 && absacc) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) rowabs += __shfl_xor_sync(kFull, rowabs, o);
+      if (lane == 0) atomicAdd(&absacc[row], rowabs);
+    }
     __syncwarp();
     return cnt;
+  }
+
+  // MODE 0: also accumulate sum_j |H_ij| of row i and of each column j into acc.
+  __device__ __forceinline__ void track_abs(float* acc, uint32_t i) {
+    absacc = acc;
+    row = i;
   }
 };
 

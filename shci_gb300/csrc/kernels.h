@@ -35,11 +35,14 @@ size_t build_hamiltonian(shci_ctx* c, int precision);
 bool join_prepare(shci_ctx* c);
 void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
                uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
-               unsigned grid);
+               unsigned grid, float* absacc);
 void join_release(shci_ctx* c);
 
 // spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
 void spmv(shci_ctx* c, const double* x, double* y, bool residual);
+// Mixed H*v needs a bound on the row abs sums: the count pass of a mixed build sums |H_ij|
+// into H.rowabs (off-diagonal), and this turns the sums into the bound.
+void finish_mixed_bound(shci_ctx* c);
 
 // davidson.cu
 struct DavidsonOut {

@@ -5,8 +5,11 @@
 //   (2) an exclusive scan of the digit-major [256 x tiles] histogram -> scatter bases,
 //   (3) a stable scatter: each 4096-item tile is walked in 16 rounds of 256 consecutive items;
 //       within a round an item's rank among equal digits comes from __match_any_sync (inside
-//       its warp) plus the per-warp counts of lower warps, so input order is preserved.
-// Passes whose digit is constant over all keys are skipped (detected from the histogram).
+//       its warp) plus the per-warp counts of lower warps, so input order is preserved.  The
+//       tile is first placed digit-sorted in shared memory and then written out run by run,
+//       so global writes are coalesced.
+// Passes whose digit is constant over all keys are skipped (a pre-pass ORs key differences).
+// Keys are 32 or 64 bit, values 32 or 64 bit.
 #include "sort.cuh"
 
 namespace shci {
@@ -113,7 +116,8 @@ constexpr int kSortThreads = 256;
 constexpr int kSortRounds = 16;
 constexpr int kSortTile = kSortThreads * kSortRounds;
 
-__global__ void k_radix_hist(const uint64_t* keys, size_t n, int shift, uint32_t* hist,
+template <class K>
+__global__ void k_radix_hist(const K* keys, size_t n, int shift, uint32_t* hist,
                              unsigned n_tiles) {
   __shared__ uint32_t s_h[256];
   s_h[threadIdx.x] = 0;
@@ -131,21 +135,52 @@ __global__ void k_radix_hist(const uint64_t* keys, size_t n, int shift, uint32_t
   hist[(size_t)threadIdx.x * n_tiles + blockIdx.x] = s_h[threadIdx.x];
 }
 
-template <class V>
-__global__ void k_radix_scatter(const uint64_t* kin, const V* vin, uint64_t* kout, V* vout,
-                                size_t n, int shift, const uint32_t* offs, unsigned n_tiles) {
-  __shared__ uint32_t s_base[256];
+// Stable scatter of one tile.  Items are ranked round by round (256 consecutive items per
+// round: rank among equal digits from __match_any_sync inside the warp plus the counts of
+// lower warps and earlier rounds), placed at their digit-sorted position in shared memory,
+// and then written out in that order, so each digit's run of the tile goes to global memory
+// as consecutive addresses (coalesced) instead of one scattered write per item.  offs is the
+// exclusively scanned digit-major histogram with the total appended, so the tile's count of
+// digit d is offs[d * n_tiles + tile + 1] - offs[d * n_tiles + tile].
+template <class K, class V>
+__global__ void __launch_bounds__(kSortThreads)
+    k_radix_scatter(const K* __restrict__ kin, const V* __restrict__ vin, K* __restrict__ kout,
+                    V* __restrict__ vout, size_t n, int shift, const uint32_t* __restrict__ offs,
+                    unsigned n_tiles) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  K* s_k = reinterpret_cast<K*>(s_raw);
+  V* s_v = reinterpret_cast<V*>(s_raw + sizeof(K) * kSortTile);
+  __shared__ uint32_t s_gbase[256], s_lstart[256], s_run[256];
   __shared__ uint32_t s_wcnt[kSortThreads / 32][256];
+  __shared__ uint32_t s_scan[kSortThreads / 32];
   const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const size_t t0 = (size_t)blockIdx.x * kSortTile;
-  s_base[tid] = offs[(size_t)tid * n_tiles + blockIdx.x];
+  {
+    const size_t hi = (size_t)tid * n_tiles + blockIdx.x;
+    const uint32_t g = offs[hi];
+    const uint32_t cnt = offs[hi + 1] - g;
+    s_gbase[tid] = g;
+    s_run[tid] = 0;
+    // block exclusive scan of the tile's digit counts -> local digit starts
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (unsigned)o) inc += t;
+    }
+    if (lane == 31) s_scan[warp] = inc;
+    __syncthreads();
+    uint32_t before = 0;
+    for (unsigned w = 0; w < warp; w++) before += s_scan[w];
+    s_lstart[tid] = before + inc - cnt;
+  }
   for (int r = 0; r < kSortRounds; r++) {
 #pragma unroll
     for (int w = 0; w < kSortThreads / 32; w++) s_wcnt[w][tid] = 0;
     __syncthreads();
     const size_t idx = t0 + (size_t)r * kSortThreads + tid;
     const bool valid = idx < n;
-    const uint64_t k = valid ? kin[idx] : 0ull;
+    const K k = valid ? kin[idx] : K(0);
     const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned rank = __popc(peers & ((1u << lane) - 1u));
@@ -154,22 +189,31 @@ __global__ void k_radix_scatter(const uint64_t* kin, const V* vin, uint64_t* kou
     if (valid) {
       unsigned pre = 0;
       for (unsigned w = 0; w < warp; w++) pre += s_wcnt[w][d];
-      const unsigned pos = s_base[d] + pre + rank;
-      kout[pos] = k;
-      vout[pos] = vin[idx];
+      const unsigned lp = s_lstart[d] + s_run[d] + pre + rank;
+      s_k[lp] = k;
+      s_v[lp] = vin[idx];
     }
     __syncthreads();
     unsigned tot = 0;
 #pragma unroll
     for (int w = 0; w < kSortThreads / 32; w++) tot += s_wcnt[w][tid];
-    s_base[tid] += tot;
-    __syncthreads();
+    s_run[tid] += tot;
+  }
+  __syncthreads();
+  const unsigned tile_n = static_cast<unsigned>(n - t0 < (size_t)kSortTile ? n - t0 : kSortTile);
+  for (unsigned p = tid; p < tile_n; p += kSortThreads) {
+    const K k = s_k[p];
+    const unsigned d = (unsigned)((k >> shift) & 255u);
+    const size_t g = (size_t)s_gbase[d] + (p - s_lstart[d]);
+    kout[g] = k;
+    vout[g] = s_v[p];
   }
 }
 
 // Bits set in the OR of (k xor k0) over all keys: digits where every key agrees are skipped.
-__global__ void k_key_spread(const uint64_t* keys, size_t n, unsigned long long* spread) {
-  const uint64_t k0 = keys[0];
+template <class K>
+__global__ void k_key_spread(const K* keys, size_t n, unsigned long long* spread) {
+  const K k0 = keys[0];
   uint64_t acc = 0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
@@ -178,39 +222,44 @@ __global__ void k_key_spread(const uint64_t* keys, size_t n, unsigned long long*
   if ((threadIdx.x & 31) == 0 && acc) atomicOr(spread, (unsigned long long)acc);
 }
 
-template <class V>
-void radix_sort_impl(DevBuf<uint64_t>& keys, DevBuf<V>& vals, size_t n, int begin_bit,
-                     int end_bit, cudaStream_t s, SortScratch& sc, DevBuf<V>& valt) {
+template <class K, class V>
+void radix_sort_impl(DevBuf<K>& keys, DevBuf<V>& vals, size_t n, int begin_bit, int end_bit,
+                     cudaStream_t s, SortScratch& sc, DevBuf<K>& kalt, DevBuf<V>& valt) {
   if (n <= 1 || begin_bit >= end_bit) return;
-  if (n > 0xffffffffull) throw ArgError("radix sort: more than 2^32 items");
+  if (n >= 0xffffffffull) throw ArgError("radix sort: 2^32 or more items");
+  end_bit = end_bit > (int)(8 * sizeof(K)) ? (int)(8 * sizeof(K)) : end_bit;
   // Which digits vary at all?
   sc.part64.reserve(scan_part_size(1));
   unsigned long long* spread = reinterpret_cast<unsigned long long*>(sc.part64.p);
   SHCI_CUDA(cudaMemsetAsync(spread, 0, sizeof(unsigned long long), s));
-  k_key_spread<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(keys.p, n, spread);
+  k_key_spread<K><<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(keys.p, n, spread);
   SHCI_LAUNCH_CHECK();
   unsigned long long sp = 0;
   SHCI_CUDA(cudaMemcpyAsync(&sp, spread, sizeof(sp), cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
 
   const unsigned n_tiles = static_cast<unsigned>((n + kSortTile - 1) / kSortTile);
-  sc.kalt.reserve(n, 1.25);
+  const size_t n_hist = (size_t)256 * n_tiles;
+  kalt.reserve(n, 1.25);
   valt.reserve(n, 1.25);
-  sc.hist.reserve((size_t)256 * n_tiles, 1.25);
-  sc.part32.reserve(scan_part_size((size_t)256 * n_tiles), 1.25);
-  uint64_t* kin = keys.p;
+  sc.hist.reserve(n_hist + 1, 1.25);
+  sc.part32.reserve(scan_part_size(n_hist), 1.25);
+  const int smem = static_cast<int>((sizeof(K) + sizeof(V)) * kSortTile);
+  SHCI_CUDA(cudaFuncSetAttribute(k_radix_scatter<K, V>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  K* kin = keys.p;
   V* vin = vals.p;
-  uint64_t* kout = sc.kalt.p;
+  K* kout = kalt.p;
   V* vout = valt.p;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
     const uint64_t mask = (shift + 8 >= 64 ? ~0ull : ((1ull << (shift + 8)) - 1ull)) &
                           ~((1ull << shift) - 1ull);
     if ((sp & mask) == 0) continue;
-    k_radix_hist<<<n_tiles, kSortThreads, 0, s>>>(kin, n, shift, sc.hist.p, n_tiles);
+    k_radix_hist<K><<<n_tiles, kSortThreads, 0, s>>>(kin, n, shift, sc.hist.p, n_tiles);
     SHCI_LAUNCH_CHECK();
-    scan_rec<uint32_t>(sc.hist.p, sc.hist.p, (size_t)256 * n_tiles, s, sc.part32.p, nullptr);
-    k_radix_scatter<V><<<n_tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift,
-                                                        sc.hist.p, n_tiles);
+    scan_rec<uint32_t>(sc.hist.p, sc.hist.p, n_hist, s, sc.part32.p, sc.hist.p + n_hist);
+    k_radix_scatter<K, V><<<n_tiles, kSortThreads, smem, s>>>(kin, vin, kout, vout, n, shift,
+                                                               sc.hist.p, n_tiles);
     SHCI_LAUNCH_CHECK();
     std::swap(kin, kout);
     std::swap(vin, vout);
@@ -218,7 +267,7 @@ void radix_sort_impl(DevBuf<uint64_t>& keys, DevBuf<V>& vals, size_t n, int begi
   if (kin != keys.p) {
     // the result lives in the ping-pong buffers: hand their storage to the caller
     const size_t kn = keys.n, vn = vals.n;
-    swap_storage(keys, sc.kalt);
+    swap_storage(keys, kalt);
     swap_storage(vals, valt);
     keys.n = kn;
     vals.n = vn;
@@ -272,12 +321,20 @@ uint32_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStr
 
 void radix_sort_pairs(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, size_t n, int begin_bit,
                       int end_bit, cudaStream_t s, SortScratch& sc) {
-  radix_sort_impl<uint32_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.valt32);
+  radix_sort_impl<uint64_t, uint32_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.kalt,
+                                      sc.valt32);
 }
 
 void radix_sort_pairs64(DevBuf<uint64_t>& keys, DevBuf<uint64_t>& vals, size_t n,
                         int begin_bit, int end_bit, cudaStream_t s, SortScratch& sc) {
-  radix_sort_impl<uint64_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.valt64);
+  radix_sort_impl<uint64_t, uint64_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.kalt,
+                                      sc.valt64);
+}
+
+void radix_sort_pairs32(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, size_t n,
+                        int begin_bit, int end_bit, cudaStream_t s, SortScratch& sc) {
+  radix_sort_impl<uint32_t, uint32_t>(keys, vals, n, begin_bit, end_bit, s, sc, sc.kalt32,
+                                      sc.valt32);
 }
 
 void iota_u32(uint32_t* v, size_t n, cudaStream_t s) {

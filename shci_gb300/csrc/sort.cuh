@@ -16,11 +16,12 @@ struct SortScratch {
   DevBuf<uint32_t> part32;   // scan partials
   DevBuf<uint64_t> part64;
   DevBuf<uint64_t> kalt;     // ping-pong keys
+  DevBuf<uint32_t> kalt32;
   DevBuf<uint32_t> valt32;   // ping-pong values
   DevBuf<uint64_t> valt64;
   void set_tracker(MemTracker* m) {
     hist.mt = part32.mt = kalt.mt = valt32.mt = valt64.mt = m;
-    part64.mt = m;
+    part64.mt = kalt32.mt = m;
   }
 };
 
@@ -39,6 +40,8 @@ void exclusive_scan_u64_async(const uint64_t* in, uint64_t* out, size_t n, cudaS
 void radix_sort_pairs(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, size_t n, int begin_bit,
                       int end_bit, cudaStream_t s, SortScratch& sc);
 void radix_sort_pairs64(DevBuf<uint64_t>& keys, DevBuf<uint64_t>& vals, size_t n,
+                        int begin_bit, int end_bit, cudaStream_t s, SortScratch& sc);
+void radix_sort_pairs32(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, size_t n,
                         int begin_bit, int end_bit, cudaStream_t s, SortScratch& sc);
 
 template <class T>

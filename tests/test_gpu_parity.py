@@ -104,6 +104,27 @@ def test_spmv_matches_oracle(c_ham):
     assert np.max(np.abs(y - yo)) <= 1e-12 * np.max(np.abs(yo))
 
 
+def test_mixed_spmv_fixed_point(shci, c_ham):
+    """Mixed store: float-pair products with 64-bit fixed-point accumulation.  With the FP32
+    residual the product matches the FP64 oracle to 1e-12 of max|y|; without it, to the FP32
+    rounding of the stored values; and the result is bit-reproducible (integer sums do not
+    depend on the order of the atomics)."""
+    _, o, _, _, _, up, dn, coefs = c_ham
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.set_dets(up, dn, coefs)
+    c.update_hamiltonian(shci.PREC_MIXED)
+    rng = np.random.default_rng(7)
+    for x in (rng.standard_normal(len(up)), coefs, 1e-9 * rng.standard_normal(len(up))):
+        yo = o.hv(x)
+        scale = np.max(np.abs(yo))
+        y_res = c.hv(x, True)
+        assert np.max(np.abs(y_res - yo)) <= 1e-12 * scale
+        assert np.array_equal(c.hv(x, True), y_res)
+        y32 = c.hv(x, False)
+        assert np.max(np.abs(y32 - yo)) <= 1e-6 * scale
+        assert np.array_equal(c.hv(x, False), y32)
+
+
 def test_davidson_matches_oracle(c_ham):
     c, o, _, _, _, up, dn, coefs = c_ham
     e_o, vec_o, conv_o, tr_o = o.davidson(coefs, 5e-5 / 500000)
