@@ -57,6 +57,61 @@ __device__ __forceinline__ uint32_t src_det(const StoSources& S, uint32_t k, int
   return mode == kSto ? S.det[k] : k;
 }
 
+// Walks the candidates of one source det (a warp): the heat-bath slots' index ranges in the
+// window [eps_min, eps_max) are flattened over the lanes 32 at a time, and f(slot, ok, cu,
+// cd) is called by all lanes for each group of 32 (slot = the lane holds an index entry of
+// the window, ok = that entry makes a valid candidate (cu, cd)).
+template <class F>
+__device__ __forceinline__ void pt_walk(const SelParams& P, uint64_t up, uint64_t dn,
+                                        double eps_min, double eps_max, F&& f) {
+  const unsigned lane = threadIdx.x & 31;
+  const int n_slots = P.n_elecs + P.n_pairs;
+  for (int s0 = 0; s0 < n_slots; s0 += 32) {
+    const int slot = s0 + lane;
+    uint32_t lo = 0, c = 0;
+    if (slot < n_slots) slot_range(P, up, dn, slot, eps_min, eps_max, &lo, &c);
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, inc, o);
+      if (lane >= (unsigned)o) inc += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, inc, 31);
+    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+      const uint32_t t = t0 + lane;
+      uint32_t ol = 0;
+#pragma unroll
+      for (uint32_t step = 16; step; step >>= 1) {
+        const uint32_t v = __shfl_sync(kFull, inc, ol + step - 1);
+        if (v <= t) ol += step;
+      }
+      const uint32_t o_inc = __shfl_sync(kFull, inc, ol);
+      const uint32_t o_c = __shfl_sync(kFull, c, ol);
+      const uint32_t o_lo = __shfl_sync(kFull, lo, ol);
+      uint64_t cu = 0, cd = 0;
+      bool single = false, ok = false;
+      if (t < total) {
+        const uint32_t e = o_lo + (t - (o_inc - o_c));
+        ok = make_candidate(P, up, dn, s0 + (int)ol, e, &cu, &cd, &single);
+      }
+      f(t < total, ok, cu, cd);
+    }
+  }
+}
+
+// Candidate a of source i belongs to the batch being computed (the first test of the
+// handler, solver.h:703-705).  One batch: every candidate.
+__device__ __forceinline__ bool in_batch(const PtParams& Q, uint64_t batch, uint64_t cu,
+                                         uint64_t cd) {
+  return Q.n_batches <= 1 || rehash(det_hash(cu, cd)) % Q.n_batches == batch;
+}
+
+__device__ __forceinline__ uint64_t src_batch(const PtParams& Q, const StoSources& S, uint32_t k,
+                                              int mode) {
+  return mode == kSto ? S.batch[k] : Q.batch;
+}
+
+// Output slots of each source: its candidates in the current batch.
 template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32)
     k_pt_count(SelParams P, PtParams Q, StoSources S, uint32_t n_src, uint64_t* cnt_out) {
@@ -68,15 +123,23 @@ __global__ void __launch_bounds__(kPtWarps * 32)
     const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
-    const int n_slots = P.n_elecs + P.n_pairs;
     uint64_t tot = 0;
-    for (int s0 = 0; s0 < n_slots; s0 += 32) {
-      uint32_t lo = 0, c = 0;
-      if (s0 + (int)lane < n_slots) slot_range(P, up, dn, s0 + lane, eps_min, eps_max, &lo, &c);
-      uint64_t cc = c;
+    if (Q.n_batches <= 1) {
+      // every candidate counts: the slot ranges suffice
+      const int n_slots = P.n_elecs + P.n_pairs;
+      for (int s0 = 0; s0 < n_slots; s0 += 32) {
+        uint32_t lo = 0, c = 0;
+        if (s0 + (int)lane < n_slots) slot_range(P, up, dn, s0 + lane, eps_min, eps_max, &lo, &c);
+        uint64_t cc = c;
 #pragma unroll
-      for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(kFull, cc, o);
-      tot += cc;
+        for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(kFull, cc, o);
+        tot += cc;
+      }
+    } else {
+      const uint64_t batch = src_batch(Q, S, k, MODE);
+      pt_walk(P, up, dn, eps_min, eps_max, [&](bool, bool ok, uint64_t cu, uint64_t cd) {
+        tot += __popc(__ballot_sync(kFull, ok && in_batch(Q, batch, cu, cd)));
+      });
     }
     if (lane == 0) cnt_out[k] = tot;
   }
@@ -86,11 +149,26 @@ struct OutCols {
   double* v[5];
 };
 
+constexpr uint32_t kPtQ = 64;  // per-warp queue of batch members (< 32 waiting + 32 pushed)
+struct PtQueue {
+  uint64_t u[kPtQ];
+  uint64_t d[kPtQ];
+};
+
+// Emits the batch members of each source into its slots [off, off + count) (one batch: every
+// index entry of the window, as counted by slot ranges).  Members wait in a per-warp queue
+// and are finished 32 at a time (variational-set test, H_ai c_i, the value columns), so the
+// set search and the FP64 element run with full warps; slots of members rejected there, or
+// of entries that make no valid candidate, are written invalid.  Members keep their walk
+// order.
 template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32)
     k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
               const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out) {
+  __shared__ PtQueue qs[kPtWarps];
+  PtQueue& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
   const uint32_t wpg = gridDim.x * kPtWarps;
   for (uint32_t k = k_begin + blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < k_end; k += wpg) {
     const uint32_t i = src_det(S, k, MODE);
@@ -99,55 +177,31 @@ __global__ void __launch_bounds__(kPtWarps * 32)
     const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
-    uint64_t batch = Q.batch;
+    const uint64_t batch = src_batch(Q, S, k, MODE);
     double count = 1.0, weight = 1.0;
     bool dtm_src = true;
     uint64_t iter_tag = 0;
     if (MODE == kSto) {
-      batch = S.batch[k];
       dtm_src = S.is_dtm[k] != 0;
       count = dtm_src ? 1.0 : S.count[k];
       weight = dtm_src ? 1.0 : S.weight[k];
       iter_tag = static_cast<uint64_t>(S.iter[k]) << Q.iter_shift;
     }
     uint64_t base = off[k - k_begin];
-    const int n_slots = P.n_elecs + P.n_pairs;
-    for (int s0 = 0; s0 < n_slots; s0 += 32) {
-      const int slot = s0 + lane;
-      uint32_t lo = 0, c = 0;
-      if (slot < n_slots) slot_range(P, up, dn, slot, eps_min, eps_max, &lo, &c);
-      uint32_t inc = c;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(kFull, inc, o);
-        if (lane >= (unsigned)o) inc += t;
-      }
-      const uint32_t total = __shfl_sync(kFull, inc, 31);
-      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-        const uint32_t t = t0 + lane;
-        uint32_t ol = 0;
-#pragma unroll
-        for (uint32_t step = 16; step; step >>= 1) {
-          const uint32_t v = __shfl_sync(kFull, inc, ol + step - 1);
-          if (v <= t) ol += step;
-        }
-        const uint32_t o_inc = __shfl_sync(kFull, inc, ol);
-        const uint32_t o_c = __shfl_sync(kFull, c, ol);
-        const uint32_t o_lo = __shfl_sync(kFull, lo, ol);
-        if (t >= total) continue;
-        const uint32_t e = o_lo + (t - (o_inc - o_c));
-        uint64_t cu, cd;
-        bool single;
-        bool ok = make_candidate(P, up, dn, s0 + (int)ol, e, &cu, &cd, &single);
+    uint32_t qh = 0, qn = 0;
+    auto drain = [&](uint32_t m) {
+      __syncwarp();
+      if (lane < m) {
+        const uint32_t sl = (qh + lane) & (kPtQ - 1);
+        const uint64_t cu = q.u[sl], cd = q.d[sl];
+        // handler order of solver.h:703-713: batch (done), variational set, |H_ai c_i|
+        bool ok = cu != kInvalid && !in_set(P, cu, cd);
         double hc = 0.0;
-        // handler order of solver.h:703-713: batch, variational set, |H_ai c_i|
-        if (ok && rehash(det_hash(cu, cd)) % Q.n_batches != batch) ok = false;
-        if (ok && in_set(P, cu, cd)) ok = false;
         if (ok) {
           hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
           if (fabs(hc) < Q.eps) ok = false;
         }
-        const uint64_t pos = base + t;
+        const uint64_t pos = base + lane;
         out_up[pos] = ok ? (cu | iter_tag) : kInvalid;
         out_dn[pos] = ok ? cd : kInvalid;
         if (MODE == kDtm) {
@@ -172,8 +226,23 @@ __global__ void __launch_bounds__(kPtWarps * 32)
           out.v[4][pos] = v4;
         }
       }
-      base += total;
-    }
+      __syncwarp();
+      qh += m;
+      qn -= m;
+      base += m;
+    };
+    pt_walk(P, up, dn, eps_min, eps_max, [&](bool slot, bool ok, uint64_t cu, uint64_t cd) {
+      const bool mine = Q.n_batches <= 1 ? slot : (ok && in_batch(Q, batch, cu, cd));
+      const unsigned bal = __ballot_sync(kFull, mine);
+      if (mine) {
+        const uint32_t sl = (qh + qn + __popc(bal & lt)) & (kPtQ - 1);
+        q.u[sl] = ok ? cu : kInvalid;
+        q.d[sl] = ok ? cd : kInvalid;
+      }
+      qn += __popc(bal);
+      if (qn >= 32u) drain(32u);
+    });
+    if (qn) drain(qn);
   }
 }
 
@@ -419,7 +488,10 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   pt_setup(c, st);
   const uint32_t n_var = static_cast<uint32_t>(c->up.size());
   StoSources S{};
-  const std::vector<uint64_t> hc = pt_counts<MODE>(c, st, Q, S, n_var);
+  // slots per source over all batches (sizes the automatic batch count)
+  Q.n_batches = 1;
+  Q.batch = 0;
+  std::vector<uint64_t> hc = pt_counts<MODE>(c, st, Q, S, n_var);
   if (n_batches == 0) {
     // Automatic batch count: every candidate pair costs ~48 device bytes while a batch is
     // processed (keys, value columns, compaction, sort ping-pong); keep a batch within 40% of
@@ -442,6 +514,8 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   for (size_t batch = 0; batch < n_batches; batch++) {
     Q.batch = batch;
     bu.n = bd.n = 0;
+    // with several batches each source's slots are its candidates in this batch
+    if (n_batches > 1) hc = pt_counts<MODE>(c, st, Q, S, n_var);
     const size_t bn = pt_emit_reduce<MODE>(c, st, Q, S, n_var, hc, bu, bd, bv, 0);
     double bs, bsq;
     pt_batch_sums<MODE>(c, bu, bd, bv, bn, e_var, &bs, &bsq);
