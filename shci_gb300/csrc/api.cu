@@ -355,6 +355,22 @@ shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols,
     if (!H.valid) throw ArgError("no Hamiltonian built");
     cudaStream_t s = c->stream;
     const size_t n = H.n, nnz = H.nnz;
+    if (!H.packed) {
+      // rows sized by an upper bound: hand out a packed copy
+      DevBuf<uint64_t> p;
+      DevBuf<uint32_t> cl;
+      DevBuf<double> v;
+      p.mt = &c->mem;
+      cl.mt = &c->mem;
+      v.mt = &c->mem;
+      pack_hamiltonian(c, p, cl, v);
+      if (row_ptr) SHCI_CUDA(cudaMemcpyAsync(row_ptr, p.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+      if (cols) SHCI_CUDA(cudaMemcpyAsync(cols, cl.p, nnz * 4, cudaMemcpyDeviceToHost, s));
+      if (vals) SHCI_CUDA(cudaMemcpyAsync(vals, v.p, nnz * 8, cudaMemcpyDeviceToHost, s));
+      if (diag) SHCI_CUDA(cudaMemcpyAsync(diag, H.diag.p, n * 8, cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      return;
+    }
     if (row_ptr) SHCI_CUDA(cudaMemcpyAsync(row_ptr, H.row_ptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
     if (cols) SHCI_CUDA(cudaMemcpyAsync(cols, H.col.p, nnz * 4, cudaMemcpyDeviceToHost, s));
     if (diag) SHCI_CUDA(cudaMemcpyAsync(diag, H.diag.p, n * 8, cudaMemcpyDeviceToHost, s));
@@ -432,6 +448,13 @@ shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
     H.val64.resize(nnz ? nnz : 1);
     H.diag.resize(n);
     SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p, row_ptr, (n + 1) * 8, cudaMemcpyHostToDevice, s));
+    std::vector<uint32_t> len(n);
+    for (size_t i = 0; i < n; i++) len[i] = static_cast<uint32_t>(row_ptr[i + 1] - row_ptr[i]);
+    H.row_cnt.resize(n + 1);
+    SHCI_CUDA(cudaMemcpyAsync(H.row_cnt.p, len.data(), n * 4, cudaMemcpyHostToDevice, s));
+    H.packed = true;
+    H.bound_valid = false;
+    SHCI_CUDA(cudaStreamSynchronize(s));
     if (nnz) {
       SHCI_CUDA(cudaMemcpyAsync(H.col.p, cols, nnz * 4, cudaMemcpyHostToDevice, s));
       SHCI_CUDA(cudaMemcpyAsync(H.val64.p, vals, nnz * 8, cudaMemcpyHostToDevice, s));

@@ -59,13 +59,14 @@ struct DevHamiltonian {
   size_t cand_parts[3] = {0, 0, 0};  // scan: same beta, same alpha, alpha single x beta single;
                                      // join: core entries, 0, 0
   int precision = SHCI_PREC_FP64;
-  DevBuf<uint64_t> row_ptr;   // [n+1]
+  bool packed = true;     // rows contiguous (row_ptr[i+1] = row_ptr[i] + row_cnt[i])
+  DevBuf<uint64_t> row_ptr;   // [n+1] row i = [row_ptr[i], row_ptr[i] + row_cnt[i])
   DevBuf<uint32_t> col;       // [nnz]
   DevBuf<double> val64;       // [nnz]   FP64 storage
   DevBuf<float> val32;        // [nnz]   mixed storage: FP32 value
   DevBuf<float> res32;        // [nnz]   mixed storage: FP32 residual (value - (double)val32)
   DevBuf<double> diag;        // [n]
-  DevBuf<uint32_t> row_cnt;   // [n] scratch
+  DevBuf<uint32_t> row_cnt;   // [n+1] elements of each row
   bool valid = false;
   // mixed-storage H*v (spmv.cu): row abs-sum bound and fixed-point scratch
   bool bound_valid = false;

@@ -20,6 +20,7 @@
 // element set the reference builds (its incremental update only changes the order in which
 // rows are filled).  A count pass sizes each row, a scan gives row offsets, and a fill pass
 // writes columns / values in the same deterministic traversal order.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
@@ -398,6 +399,42 @@ void build_index(shci_ctx* c) {
   build_singles(c, ix.ub, ix.n_beta, ix.bs_off, ix.bs_list, &ix.bs_str);
 }
 
+// Allocates the element store for `cap` elements in the build's precision.
+static void alloc_store(shci_ctx* c, int precision, size_t cap) {
+  auto& H = c->H;
+  if (cap == 0) cap = 1;
+  H.col.resize(cap, 1.1);
+  if (precision == SHCI_PREC_FP64) {
+    H.val32.release();
+    H.res32.release();
+    H.val64.resize(cap, 1.1);
+  } else {
+    H.val64.release();
+    H.val32.resize(cap, 1.1);
+    H.res32.resize(cap, 1.1);
+  }
+}
+
+// Bytes free for the element store: device free memory within the context's budget.
+static size_t store_room(shci_ctx* c) {
+  size_t free_b = 0, total_b = 0;
+  SHCI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  // the store's current allocation is reused or freed before the new one is made
+  const auto& H = c->H;
+  size_t held = H.col.cap * 4 + H.val64.cap * 8 + H.val32.cap * 4 + H.res32.cap * 4;
+  size_t room = free_b + held;
+  if (c->mem.budget)
+    room = std::min(room, c->mem.budget > c->mem.used - held ? c->mem.budget - (c->mem.used - held)
+                                                             : (size_t)0);
+  return room;
+}
+
+// Builds H for the current dets.  Paths:
+//   join, one pass  - rows sized by their join candidate counts (an upper bound), filled in a
+//                     single pass that also records each row's kept length (rows not packed);
+//   join, two pass  - count, scan, fill (packed rows), when the bound does not fit in memory;
+//   scan            - group index + scan traversal, count and fill (packed rows).
+// SHCI_HBUILD=scan forces the scan path, SHCI_HBUILD=join2 the two-pass join.
 size_t build_hamiltonian(shci_ctx* c, int precision) {
   auto& H = c->H;
   auto& ix = c->idx;
@@ -410,6 +447,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.bound_valid = false;
   const char* force = std::getenv("SHCI_HBUILD");
   const bool scan_only = force && std::strcmp(force, "scan") == 0;
+  const bool two_pass = force && std::strcmp(force, "join2") == 0;
   H.join = !scan_only && join_prepare(c);
   if (!H.join) build_index(c);
   H.row_ptr.resize(n + 1, 1.25);
@@ -425,32 +463,52 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
   SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
-  // a mixed build also sums |H_ij| per det during the count (the H*v fixed-point bound)
+  // a mixed build also sums |H_ij| per det (the H*v fixed-point bound)
   float* absacc = nullptr;
   if (precision == SHCI_PREC_MIXED) {
     H.rowabs.resize(n, 1.1);
     SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
     absacc = H.rowabs.p;
   }
-  {
-    ProfScope ps(c->prof, s, "hbuild_count");
-    k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n,
-                                             H.diag.p);
-    SHCI_LAUNCH_CHECK();
-    if (H.join) {
-      join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid,
-                absacc);
-    } else {
-      k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                               H.row_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                               nullptr, work, absacc);
-      SHCI_LAUNCH_CHECK();
+  k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, H.diag.p);
+  SHCI_LAUNCH_CHECK();
+  const int fill_mode = precision == SHCI_PREC_FP64 ? 1 : 2;
+  uint64_t nnz = 0;
+  bool one_pass = false;
+  if (H.join && !two_pass) {
+    const uint64_t cap = join_row_caps(c, H.row_ptr.p);
+    one_pass = static_cast<double>(cap) * 12.0 * 1.1 < 0.9 * static_cast<double>(store_room(c));
+    if (one_pass) {
+      alloc_store(c, precision, cap);
+      {
+        ProfScope ps(c->prof, s, "hbuild_fill");
+        join_rows(c, fill_mode, H.row_cnt.p, H.row_ptr.p, H.col.p, H.val64.p, H.val32.p,
+                  H.res32.p, work, grid, absacc);
+      }
+      c->k0.resize(n, 1.25);
+      widen_u32_u64(H.row_cnt.p, c->k0.p, n, s);
+      nnz = exclusive_scan_u64(c->k0.p, c->k0.p, n, s, c->sort);
+      H.packed = false;
     }
   }
-  // row_ptr = exclusive scan of counts (counts widened to 64 bit)
-  widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
-  const uint64_t nnz = exclusive_scan_u64(H.row_ptr.p, H.row_ptr.p, n, s, c->sort);
-  SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p + n, &nnz, 8, cudaMemcpyHostToDevice, s));
+  if (!one_pass) {
+    {
+      ProfScope ps(c->prof, s, "hbuild_count");
+      if (H.join) {
+        join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid,
+                  absacc);
+      } else {
+        k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                                 H.row_cnt.p, nullptr, nullptr, nullptr,
+                                                 nullptr, nullptr, work, absacc);
+        SHCI_LAUNCH_CHECK();
+      }
+    }
+    // row_ptr = exclusive scan of counts (counts widened to 64 bit)
+    widen_u32_u64(H.row_cnt.p, H.row_ptr.p, n, s);
+    nnz = exclusive_scan_u64(H.row_ptr.p, H.row_ptr.p, n, s, c->sort);
+    SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p + n, &nnz, 8, cudaMemcpyHostToDevice, s));
+  }
   unsigned long long cand[3] = {0, 0, 0};
   SHCI_CUDA(cudaMemcpyAsync(cand, work + 2, 24, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
@@ -462,33 +520,26 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
     H.cand_parts[0] = c->join.m;
     H.cand_parts[1] = H.cand_parts[2] = 0;
   }
-  const size_t cap = nnz ? nnz : 1;
-  H.col.resize(cap, 1.1);
-  if (precision == SHCI_PREC_FP64) {
-    H.val32.release();
-    H.res32.release();
-    H.val64.resize(cap, 1.1);
-  } else {
-    H.val64.release();
-    H.val32.resize(cap, 1.1);
-    H.res32.resize(cap, 1.1);
-  }
-  SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
-  {
-    ProfScope ps(c->prof, s, "hbuild_fill");
-    if (H.join) {
-      join_rows(c, precision == SHCI_PREC_FP64 ? 1 : 2, nullptr, H.row_ptr.p, H.col.p,
-                H.val64.p, H.val32.p, H.res32.p, work, grid, nullptr);
-    } else if (precision == SHCI_PREC_FP64) {
-      k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                               nullptr, H.row_ptr.p, H.col.p, H.val64.p,
-                                               nullptr, nullptr, work, nullptr);
-    } else {
-      k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
-                                               nullptr, H.row_ptr.p, H.col.p, nullptr, H.val32.p,
-                                               H.res32.p, work, nullptr);
+  if (!one_pass) {
+    alloc_store(c, precision, nnz);
+    SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+    {
+      ProfScope ps(c->prof, s, "hbuild_fill");
+      if (H.join) {
+        join_rows(c, fill_mode, nullptr, H.row_ptr.p, H.col.p, H.val64.p, H.val32.p, H.res32.p,
+                  work, grid, nullptr);
+      } else if (precision == SHCI_PREC_FP64) {
+        k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                                 nullptr, H.row_ptr.p, H.col.p, H.val64.p,
+                                                 nullptr, nullptr, work, nullptr);
+      } else {
+        k_hbuild<2><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
+                                                 nullptr, H.row_ptr.p, H.col.p, nullptr,
+                                                 H.val32.p, H.res32.p, work, nullptr);
+      }
+      SHCI_LAUNCH_CHECK();
     }
-    SHCI_LAUNCH_CHECK();
+    H.packed = true;
   }
   SHCI_CUDA(cudaStreamSynchronize(s));
   if (H.join) join_release(c);

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
     if (i >= n) break;
     const uint64_t ui = up[i], di = dn[i];
     RowSink<MODE> sink(q, I, ui, di, MODE ? row_ptr[i] : 0, col, v64, v32, r32);
-    if (MODE == 0 && absacc) sink.track_abs(absacc, i);
+    if (absacc) sink.track_abs(absacc, i);
     uint64_t n_cand = 0;
     for (uint32_t k0 = 0; k0 < K; k0 += 32) {
       const uint32_t k = k0 + lane;
@@ -202,10 +202,28 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
       }
     }
     const uint32_t cnt = sink.finish();
-    if (MODE == 0 && lane == 0) {
-      row_cnt[i] = cnt;
+    if (lane == 0) {
+      if (row_cnt) row_cnt[i] = cnt;
       atomicAdd(reinterpret_cast<unsigned long long*>(work + 2), (unsigned long long)n_cand);
     }
+  }
+}
+
+// Row capacity of a single-pass build: the candidates of row i (members after each of its
+// entries), an upper bound on the elements it keeps.
+__global__ void k_join_caps(const uint64_t* __restrict__ span, uint32_t n, uint32_t K,
+                            uint64_t* caps) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    uint64_t c = 0;
+    for (uint32_t k = lane; k < K; k += 32) {
+      const uint64_t sp = span[(size_t)i * K + k];
+      c += static_cast<uint32_t>(sp >> 32) - static_cast<uint32_t>(sp) - 1u;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+    if (lane == 0) caps[i] = c;
   }
 }
 
@@ -328,15 +346,28 @@ void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr
                                                  nullptr, nullptr, nullptr, nullptr, nullptr,
                                                  work, absacc);
   else if (mode == 1)
-    k_hjoin<1><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
+    k_hjoin<1><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, row_cnt,
                                                  row_ptr, col, v64, nullptr, nullptr, work,
-                                                 nullptr);
+                                                 absacc);
   else
-    k_hjoin<2><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, nullptr,
+    k_hjoin<2><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, row_cnt,
                                                  row_ptr, col, nullptr, v32, r32, work,
-                                                 nullptr);
+                                                 absacc);
   SHCI_LAUNCH_CHECK();
   c->launches += 1;
+}
+
+uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start) {
+  const auto& J = c->join;
+  const uint32_t n = static_cast<uint32_t>(c->up.size());
+  cudaStream_t s = c->stream;
+  k_join_caps<<<grid_for((size_t)n * 32, 256), 256, 0, s>>>(J.span.p, n, J.K, row_start);
+  SHCI_LAUNCH_CHECK();
+  const uint64_t tot = exclusive_scan_u64(row_start, row_start, n, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(row_start + n, &tot, 8, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 1;
+  return tot;
 }
 
 void join_release(shci_ctx* c) {

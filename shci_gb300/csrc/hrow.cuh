@@ -39,7 +39,7 @@ struct RowSink {
   float* r32;
   const unsigned lane, lt;
   uint32_t cnt = 0;                            // elements kept so far in this row
-  float* absacc = nullptr;                     // MODE 0: optional sums of |H| per det
+  float* absacc = nullptr;                     // optional sums of |H| per det
   uint32_t row = 0;
   float rowabs = 0.0f;
   uint32_t qh[2] = {0u, 0u}, qn[2] = {0u, 0u};  // ring heads and lengths (warp-uniform)
@@ -63,7 +63,7 @@ struct RowSink {
       // counting needs |H| only: skip the permutation sign (a sign flip is exact)
       H = t == 0 ? h_one<MODE != 0>(I, ui, di, uj, dj) : h_two<MODE != 0>(I, ui, di, uj, dj);
       keep = keep_elem(H);
-      if (MODE == 0 && absacc && keep) {
+      if (absacc && keep) {
         // |H| rounded up, summed into both dets' totals (the row abs-sum bound of H*v)
         const float a = __double2float_ru(fabs(H));
         atomicAdd(&absacc[j], a);
@@ -111,7 +111,7 @@ struct RowSink {
   __device__ __forceinline__ uint32_t finish() {
     if (qn[0]) drain(0, qn[0]);
     if (qn[1]) drain(1, qn[1]);
-    if (MODE == 0 && absacc) {
+    if (absacc) {
 #pragma unroll
       for (int o = 16; o; o >>= 1) rowabs += __shfl_xor_sync(kFull, rowabs, o);
       if (lane == 0) atomicAdd(&absacc[row], rowabs);
@@ -120,7 +120,7 @@ struct RowSink {
     return cnt;
   }
 
-  // MODE 0: also accumulate sum_j |H_ij| of row i and of each column j into acc.
+  // Also accumulate sum_j |H_ij| of row i and of each column j into acc.
   __device__ __forceinline__ void track_abs(float* acc, uint32_t i) {
     absacc = acc;
     row = i;

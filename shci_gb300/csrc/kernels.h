@@ -15,6 +15,9 @@ namespace shci {
 
 // misc.cu
 void widen_u32_u64(const uint32_t* in, uint64_t* out, size_t n, cudaStream_t s);
+// Packed CSR copy of the element store (FP64 values) on the device.
+void pack_hamiltonian(shci_ctx* c, DevBuf<uint64_t>& ptr, DevBuf<uint32_t>& col,
+                      DevBuf<double>& val);
 void upload_integrals(shci_ctx* c);
 void upload_queues(shci_ctx* c);
 void sync_dets(shci_ctx* c);          // host det list -> device (if dirty)
@@ -31,12 +34,16 @@ void build_index(shci_ctx* c);
 size_t build_hamiltonian(shci_ctx* c, int precision);
 
 // hjoin.cu: two-hole core join.  join_prepare returns false (nothing held) when the join
-// cannot be used for the current dets; join_rows runs one pass (mode as the row kernels).
+// cannot be used for the current dets; join_rows runs one pass (mode as the row kernels;
+// every mode writes each row's kept count to row_cnt when given).
 bool join_prepare(shci_ctx* c);
 void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
                uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
                unsigned grid, float* absacc);
 void join_release(shci_ctx* c);
+// Row starts of a single-pass build: row_start[i] = sum of the candidate counts of rows < i
+// (row_start has n + 1 entries); returns the total capacity.
+uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start);
 
 // spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
 void spmv(shci_ctx* c, const double* x, double* y, bool residual);

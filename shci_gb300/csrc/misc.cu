@@ -23,6 +23,25 @@ __global__ void k_elems(DevIntegrals I, const uint64_t* ui, const uint64_t* di, 
   }
 }
 
+// Packed copy of the element store: row i of the source [row_ptr[i], + row_len[i]) goes to
+// [ptr[i], ptr[i+1]); values as FP64 (FP64 store, or FP32 value + FP32 residual).
+__global__ void k_pack_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+                            const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                            const double* __restrict__ v64, const float* __restrict__ v32,
+                            const float* __restrict__ r32, uint32_t n, uint32_t* out_col,
+                            double* out_val) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    const uint64_t a = row_ptr[i], b = ptr[i];
+    for (uint32_t k = lane; k < row_len[i]; k += 32) {
+      out_col[b + k] = col[a + k];
+      out_val[b + k] = v64 ? v64[a + k]
+                           : static_cast<double>(v32[a + k]) + static_cast<double>(r32[a + k]);
+    }
+  }
+}
+
 template <class T>
 void upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s, MemTracker* mt) {
   b.mt = mt;
@@ -37,6 +56,28 @@ void upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s, MemTracker* m
 void widen_u32_u64(const uint32_t* in, uint64_t* out, size_t n, cudaStream_t s) {
   k_widen<<<grid_for(n, 256), 256, 0, s>>>(in, out, n);
   SHCI_LAUNCH_CHECK();
+}
+
+void pack_hamiltonian(shci_ctx* c, DevBuf<uint64_t>& ptr, DevBuf<uint32_t>& col,
+                      DevBuf<double>& val) {
+  const auto& H = c->H;
+  const size_t n = H.n;
+  cudaStream_t s = c->stream;
+  ptr.resize(n + 1);
+  widen_u32_u64(H.row_cnt.p, ptr.p, n, s);
+  const uint64_t tot = exclusive_scan_u64(ptr.p, ptr.p, n, s, c->sort);
+  SHCI_CUDA(cudaMemcpyAsync(ptr.p + n, &tot, 8, cudaMemcpyHostToDevice, s));
+  col.resize(tot ? tot : 1);
+  val.resize(tot ? tot : 1);
+  const bool fp64 = H.precision == SHCI_PREC_FP64;
+  k_pack_rows<<<grid_for(n * 32, 256), 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, ptr.p, H.col.p,
+                                                   fp64 ? H.val64.p : nullptr,
+                                                   fp64 ? nullptr : H.val32.p,
+                                                   fp64 ? nullptr : H.res32.p,
+                                                   static_cast<uint32_t>(n), col.p, val.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 2;
 }
 
 void upload_integrals(shci_ctx* c) {

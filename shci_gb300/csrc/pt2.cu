@@ -268,38 +268,82 @@ __global__ void k_pt_x(DevIntegrals I, const uint64_t* au, const uint64_t* ad, O
   }
 }
 
-// One block per segment [starts[g], starts[g+1]): out[2g] = sum x, out[2g+1] = sum x^2,
-// reduced in a fixed order.
-__global__ void __launch_bounds__(256)
-    k_seg_reduce2(const double* x, const uint64_t* starts, size_t nseg, double* out) {
+// Sums of x and x^2 over segments [starts[g], starts[g+1]) in a fixed order: pass 1 reduces
+// chunks of kRedChunk elements of each segment (block (chunk, g)), pass 2 reduces each
+// segment's chunk partials.  Only the chunking fixes the order, so results are reproducible.
+constexpr uint32_t kRedChunk = 1u << 16;
+
+__device__ __forceinline__ void block_sum2(double* a, double* b) {
   __shared__ double s1[8], s2[8];
-  for (size_t g = blockIdx.x; g < nseg; g += gridDim.x) {
-    double a = 0.0, b = 0.0;
-    for (uint64_t k = starts[g] + threadIdx.x; k < starts[g + 1]; k += blockDim.x) {
-      a += x[k];
-      b += x[k] * x[k];
-    }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      a += __shfl_xor_sync(kFull, a, o);
-      b += __shfl_xor_sync(kFull, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      s1[threadIdx.x >> 5] = a;
-      s2[threadIdx.x >> 5] = b;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double ta = 0.0, tb = 0.0;
-      for (int w = 0; w < 8; w++) {
-        ta += s1[w];
-        tb += s2[w];
-      }
-      out[2 * g] = ta;
-      out[2 * g + 1] = tb;
-    }
-    __syncthreads();
+  for (int o = 16; o; o >>= 1) {
+    *a += __shfl_xor_sync(kFull, *a, o);
+    *b += __shfl_xor_sync(kFull, *b, o);
   }
+  if ((threadIdx.x & 31) == 0) {
+    s1[threadIdx.x >> 5] = *a;
+    s2[threadIdx.x >> 5] = *b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < 8; w++) {
+      ta += s1[w];
+      tb += s2[w];
+    }
+    *a = ta;
+    *b = tb;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_seg_partial2(const double* __restrict__ x, const uint64_t* __restrict__ starts,
+                   uint32_t n_chunks, double* part) {
+  const uint32_t g = blockIdx.y, ch = blockIdx.x;
+  const uint64_t b0 = starts[g] + (uint64_t)ch * kRedChunk;
+  const uint64_t e = starts[g + 1];
+  const uint64_t b1 = b0 + kRedChunk < e ? b0 + kRedChunk : e;
+  double a = 0.0, b = 0.0;
+  for (uint64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+    a += x[k];
+    b += x[k] * x[k];
+  }
+  block_sum2(&a, &b);
+  if (threadIdx.x == 0) {
+    part[2 * ((size_t)g * n_chunks + ch)] = a;
+    part[2 * ((size_t)g * n_chunks + ch) + 1] = b;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_seg_final2(const double* __restrict__ part, uint32_t n_chunks, double* out) {
+  const uint32_t g = blockIdx.x;
+  double a = 0.0, b = 0.0;
+  for (uint32_t k = threadIdx.x; k < n_chunks; k += blockDim.x) {
+    a += part[2 * ((size_t)g * n_chunks + k)];
+    b += part[2 * ((size_t)g * n_chunks + k) + 1];
+  }
+  block_sum2(&a, &b);
+  if (threadIdx.x == 0) {
+    out[2 * g] = a;
+    out[2 * g + 1] = b;
+  }
+}
+
+// out[2g], out[2g+1] = sum, sum of squares of x over segment g (total length m).
+void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t nseg, size_t m,
+                 double* out) {
+  cudaStream_t s = c->stream;
+  const uint32_t n_chunks = static_cast<uint32_t>((m + kRedChunk - 1) / kRedChunk) + 1;
+  DevBuf<double> part;
+  part.mt = &c->mem;
+  part.resize(2 * (size_t)n_chunks * nseg);
+  k_seg_partial2<<<dim3(n_chunks, nseg), 256, 0, s>>>(x, starts, n_chunks, part.p);
+  SHCI_LAUNCH_CHECK();
+  k_seg_final2<<<nseg, 256, 0, s>>>(part.p, n_chunks, out);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 2;
 }
 
 // starts[it] = first k with (au[k] >> shift) >= it, for it = 0..n_it (au sorted ascending)
@@ -468,8 +512,7 @@ void pt_batch_sums(shci_ctx* c, DevBuf<uint64_t>& bu, DevBuf<uint64_t>& bd, DevB
     SHCI_LAUNCH_CHECK();
     const uint64_t st2[2] = {0, bn};
     SHCI_CUDA(cudaMemcpyAsync(starts.p, st2, 16, cudaMemcpyHostToDevice, s));
-    k_seg_reduce2<<<1, 256, 0, s>>>(x.p, starts.p, 1, out.p);
-    SHCI_LAUNCH_CHECK();
+    seg_reduce2(c, x.p, starts.p, 1, bn, out.p);
   }
   double h[2];
   SHCI_CUDA(cudaMemcpyAsync(h, out.p, 16, cudaMemcpyDeviceToHost, s));
@@ -718,8 +761,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
         SHCI_LAUNCH_CHECK();
         k_iter_starts<<<1, 128, 0, s>>>(bu.p, bn, shift, n_it, starts.p);
         SHCI_LAUNCH_CHECK();
-        k_seg_reduce2<<<n_it, 256, 0, s>>>(x.p, starts.p, n_it, o.p);
-        SHCI_LAUNCH_CHECK();
+        seg_reduce2(c, x.p, starts.p, n_it, bn, o.p);
       }
       std::vector<double> h(2 * n_it);
       SHCI_CUDA(cudaMemcpyAsync(h.data(), o.p, h.size() * 8, cudaMemcpyDeviceToHost, s));

@@ -35,14 +35,15 @@ namespace {
 
 template <int MODE>  // 0: FP64 values, 1: FP32 values, 2: FP32 value + FP32 residual
 __global__ void __launch_bounds__(256)
-    k_spmv(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ col,
+    k_spmv(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+           const uint32_t* __restrict__ col,
            const double* __restrict__ v64, const float* __restrict__ v32,
            const float* __restrict__ r32, const double* __restrict__ diag,
            const double* __restrict__ x, double* __restrict__ y, uint32_t n) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-    const uint64_t rs = row_ptr[i], re = row_ptr[i + 1];
+    const uint64_t rs = row_ptr[i], re = rs + row_len[i];
     const double xi = x[i];
     double acc = 0.0;
     for (uint64_t k = rs + lane; k < re; k += 32) {
@@ -124,13 +125,14 @@ __global__ void k_split_x(const double* __restrict__ x, uint32_t n, float2* xs,
 // Off-diagonal row abs sums of the full symmetric matrix, in float.
 template <bool RES>
 __global__ void __launch_bounds__(256)
-    k_rowabs(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ col,
+    k_rowabs(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+             const uint32_t* __restrict__ col,
              const float* __restrict__ v32, const float* __restrict__ r32,
              const double* __restrict__ diag, float* rowabs, uint32_t n) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-    const uint64_t rs = row_ptr[i], re = row_ptr[i + 1];
+    const uint64_t rs = row_ptr[i], re = rs + row_len[i];
     float acc = 0.0f;
     for (uint64_t k = rs + lane; k < re; k += 32) {
       const float a = fabsf(v32[k]) + (RES ? fabsf(r32[k]) : 0.0f);
@@ -157,7 +159,8 @@ __global__ void k_max_bound(const float* __restrict__ a, const double* __restric
 // Mixed H*v: float-pair products, fixed-point accumulation (off-diagonal part only).
 template <bool RES>
 __global__ void __launch_bounds__(256)
-    k_spmv_fix(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ col,
+    k_spmv_fix(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+               const uint32_t* __restrict__ col,
                const float* __restrict__ v32, const float* __restrict__ r32,
                const float2* __restrict__ xs, const double* __restrict__ scal,
                unsigned long long* __restrict__ yfix, uint32_t n) {
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(256)
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-    const uint64_t rs = row_ptr[i], re = row_ptr[i + 1];
+    const uint64_t rs = row_ptr[i], re = rs + row_len[i];
     const float2 xi = xs[i];
     float ah = 0.0f, al = 0.0f;
     for (uint64_t k = rs + lane; k < re; k += 32) {
@@ -242,7 +245,7 @@ void mixed_bound(shci_ctx* c, unsigned grid) {
   const uint32_t n = static_cast<uint32_t>(H.n);
   H.rowabs.resize(n, 1.1);
   SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, (size_t)n * 4, s));
-  k_rowabs<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.col.p, H.val32.p, H.res32.p, H.diag.p,
+  k_rowabs<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, H.res32.p, H.diag.p,
                                       H.rowabs.p, n);
   SHCI_LAUNCH_CHECK();
   c->launches += 1;
@@ -262,7 +265,7 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   if (H.precision == SHCI_PREC_FP64) {
     ProfScope ps(c->prof, s, "spmv");
     SHCI_CUDA(cudaMemsetAsync(y, 0, H.n * sizeof(double), s));
-    k_spmv<0><<<grid, 256, 0, s>>>(H.row_ptr.p, H.col.p, H.val64.p, nullptr, nullptr, H.diag.p,
+    k_spmv<0><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val64.p, nullptr, nullptr, H.diag.p,
                                    x, y, n);
     SHCI_LAUNCH_CHECK();
     c->launches += 1;
@@ -279,10 +282,10 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
       x, n, xs, reinterpret_cast<unsigned long long*>(H.scal.p + 1));
   SHCI_LAUNCH_CHECK();
   if (residual)
-    k_spmv_fix<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.col.p, H.val32.p, H.res32.p, xs,
+    k_spmv_fix<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, H.res32.p, xs,
                                            H.scal.p, H.yfix.p, n);
   else
-    k_spmv_fix<false><<<grid, 256, 0, s>>>(H.row_ptr.p, H.col.p, H.val32.p, nullptr, xs,
+    k_spmv_fix<false><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, nullptr, xs,
                                             H.scal.p, H.yfix.p, n);
   SHCI_LAUNCH_CHECK();
   k_fix_out<<<grid_for(n, 256), 256, 0, s>>>(H.yfix.p, H.diag.p, x, H.scal.p, y, n);

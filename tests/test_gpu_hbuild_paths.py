@@ -1,4 +1,5 @@
-"""The two Hamiltonian build traversals (two-hole core join, group scan) produce the same
+"""The Hamiltonian build paths (two-hole core join in one pass with rows sized by an upper
+bound, the same join in two passes with packed rows, and the group scan) produce the same
 element set with bit-identical FP64 values on the 24,087-det C-atom wavefunction, also when
 the join's core hash is narrowed so that most buckets merge (colliding cores)."""
 import numpy as np
@@ -44,14 +45,16 @@ def _build(monkeypatch, dets, env):
 def test_join_scan_and_collisions_agree(monkeypatch, c_dets):
     s_join = _build(monkeypatch, c_dets, {})
     s_scan = _build(monkeypatch, c_dets, {"SHCI_HBUILD": "scan"})
+    s_two = _build(monkeypatch, c_dets, {"SHCI_HBUILD": "join2"})
     s_coll = _build(monkeypatch, c_dets, {"SHCI_JOIN_BITS": "10"})
     assert s_join[1]["path"] == "core_join" and s_coll[1]["path"] == "core_join"
+    assert s_two[1]["path"] == "core_join"
     assert s_scan[1]["path"] == "group_scan"
     n = len(c_dets[0])
     assert s_join[1]["core_entries"] == n * 15  # C(6, 2) electron pairs per det
     # 1024 buckets for ~361k entries: nearly all cores collide, far more candidates
     assert s_coll[1]["candidates"] > 20 * s_join[1]["candidates"]
-    for other in (s_scan, s_coll):
+    for other in (s_scan, s_two, s_coll):
         assert other[0] == s_join[0] == 4714387  # reference log, examples/C/out:243
         assert np.array_equal(other[3], s_join[3])
         for (ca, va), (cb, vb) in zip(s_join[2], other[2]):
