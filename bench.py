@@ -6,10 +6,11 @@ Workload (the largest configuration of the metric): synthetic FCIDUMP, n = 40 or
 (one iteration each, as the reference's eps_vars_schedule), then the first eps_var = 2e-5
 iteration: its selection gives the determinant list (~4.5M dets) the timed step works on.
 
-One step = Hamiltonian<S>::update (device det index + count pass + fill pass, mixed storage:
+One step = Hamiltonian<S>::update (two-hole core join index + single fill pass, mixed storage:
 FP32 value + FP32 residual) + one full Davidson::diagonalize call (the reference's maximum of
-9 H*v products, tol = 0 so every step does the same work, FP64 vectors and accumulation) +
-the FP64 Rayleigh-quotient correction of the Ritz vector.  value = device seconds per step
+9 H*v products, tol = 0 so every step does the same work, FP64 vectors, float-pair products
+and 64-bit fixed-point sums in H*v) + the FP64-accurate Rayleigh-quotient correction of the
+Ritz vector.  value = device seconds per step
 (inputs resident in HBM); e2e = the same through the public API with the det list and start
 vector copied from pinned host memory each step and the energy read back.
 
@@ -361,8 +362,13 @@ def run_ours(args):
         "join_keys": 16.0 * n + 8.0 * m,
         "join_sort": 4 * 20.0 * m,
         "join_buckets": 20.0 * m,
-        "spmv": 8.0 * nnz + 8 * (n + 1) + 16 * n + 16 * n + 8 * n,
+        "spmv": 8.0 * nnz + 8 * (n + 1) + 4 * n + 16 * n + 16 * n + 8 * n,
     }
+    # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
+    # one full-size H*v launch of the n=26 workload: 1.2946e9 B for 152,895,046 stored
+    # elements = 8.467 B per element, scaled here by the step's element count (the store is
+    # read once; x, y and the diagonal stay in L2).
+    measured_traffic = {"spmv": 8.467 * nnz}
     kernels = {}
     for k, (ms_l, cnt) in per.items():
         b = alg.get(k)
@@ -373,7 +379,7 @@ def run_ours(args):
             kernels[k]["candidates_per_s"] = cand / (ms_l * 1e-3)
     dk = kernels[dom]
     roof = {"kernel": dom, "bound": "hbm", "achieved": dk["gbs"], "peak": hbm, "unit": "GB/s",
-            "frac": dk["frac"], "traffic": None, "peak_kind": peak_kind,
+            "frac": dk["frac"], "traffic": measured_traffic.get(dom), "peak_kind": peak_kind,
             "alg_bytes_per_launch": alg.get(dom)}
     cpu = None
     if not args.no_cpu_baseline:
