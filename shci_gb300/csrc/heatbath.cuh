@@ -65,15 +65,18 @@ __device__ __forceinline__ size_t c2(size_t a, size_t b) {
 }
 
 // Entry range [lo, lo + cnt) of slot `slot` for the det (eps window [eps_min, eps_max)).
+// *orbs (optional) receives the slot's electron orbitals for make_candidate_at: the moved
+// orbital of a single, or the two spin-orbitals p | q << 8 of a pair.
 __device__ __forceinline__ void slot_range(const SelParams& P, uint64_t up, uint64_t dn, int slot,
                                            double eps_min, double eps_max, uint32_t* lo,
-                                           uint32_t* cnt) {
+                                           uint32_t* cnt, uint32_t* orbs = nullptr) {
   *lo = 0;
   *cnt = 0;
   const int n = P.n_orbs;
   if (slot < P.n_elecs) {
     if (eps_min > P.max_singles) return;
     const int p = slot < P.n_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
+    if (orbs) *orbs = static_cast<uint32_t>(p);
     const uint32_t a = P.s_off[p], b = P.s_off[p + 1];
     *lo = a;
     *cnt = first_below(P.s_S, a, b, eps_min) - a;
@@ -83,6 +86,7 @@ __device__ __forceinline__ void slot_range(const SelParams& P, uint64_t up, uint
   const uint32_t pr = P.pair_tab[slot - P.n_elecs];
   const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
   const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
+  if (orbs) *orbs = static_cast<uint32_t>(p) | (static_cast<uint32_t>(q) << 8);
   int p2 = p, q2 = q;
   if (p >= n && q >= n) {
     p2 -= n;
@@ -143,6 +147,50 @@ __device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, 
   const uint32_t pr = P.pair_tab[slot - P.n_elecs];
   const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
   const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
+  const uint32_t rs = P.d_rs[e];
+  int r = rs & 0xffff, s = rs >> 16;
+  if (p >= n && q >= n) {
+    r += n;
+    s += n;
+  } else if (p < n && q >= n && p > q - n) {
+    const int tmp = s - n;
+    s = r + n;
+    r = tmp;
+  }
+  const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
+  if (occ_r) return false;
+  const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);
+  if (occ_s) return false;
+  uint64_t u = up, d = dn;
+  if (p < n) u &= ~(1ull << p); else d &= ~(1ull << (p - n));
+  if (q < n) u &= ~(1ull << q); else d &= ~(1ull << (q - n));
+  if (r < n) u |= 1ull << r; else d |= 1ull << (r - n);
+  if (s < n) u |= 1ull << s; else d |= 1ull << (s - n);
+  *cu = u;
+  *cd = d;
+  return true;
+}
+
+// make_candidate with the slot's electron orbitals already known (from slot_range).
+__device__ __forceinline__ bool make_candidate_at(const SelParams& P, uint64_t up, uint64_t dn,
+                                                  int slot, uint32_t orbs, uint32_t e,
+                                                  uint64_t* cu, uint64_t* cd) {
+  const int n = P.n_orbs;
+  *cu = up;
+  *cd = dn;
+  if (slot < P.n_elecs) {
+    const int p = static_cast<int>(orbs);
+    const int r = static_cast<int>(P.s_r[e]);
+    if (slot < P.n_up) {
+      if (up >> r & 1) return false;
+      *cu = (up & ~(1ull << p)) | (1ull << r);
+    } else {
+      if (dn >> r & 1) return false;
+      *cd = (dn & ~(1ull << p)) | (1ull << r);
+    }
+    return true;
+  }
+  const int p = static_cast<int>(orbs & 0xffu), q = static_cast<int>(orbs >> 8);
   const uint32_t rs = P.d_rs[e];
   int r = rs & 0xffff, s = rs >> 16;
   if (p >= n && q >= n) {

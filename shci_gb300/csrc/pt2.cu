@@ -38,6 +38,7 @@ struct PtParams {
   double eps_dtm;    // psto: second column threshold
   double eps_psto;   // sto: column split threshold
   uint64_t n_batches;
+  uint64_t batch_magic;  // floor((2^64 - 1) / n_batches) for batch_of (set by set_batches)
   uint64_t batch;    // dtm / psto: the batch being computed
   double factor;     // sto: 1 / (n_samples - n_dtm - 1)
   int iter_shift;    // sto: bit position of the iteration index in the emitted up key
@@ -68,8 +69,8 @@ __device__ __forceinline__ void pt_walk(const SelParams& P, uint64_t up, uint64_
   const int n_slots = P.n_elecs + P.n_pairs;
   for (int s0 = 0; s0 < n_slots; s0 += 32) {
     const int slot = s0 + lane;
-    uint32_t lo = 0, c = 0;
-    if (slot < n_slots) slot_range(P, up, dn, slot, eps_min, eps_max, &lo, &c);
+    uint32_t lo = 0, c = 0, orbs = 0;
+    if (slot < n_slots) slot_range(P, up, dn, slot, eps_min, eps_max, &lo, &c, &orbs);
     uint32_t inc = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -88,22 +89,40 @@ __device__ __forceinline__ void pt_walk(const SelParams& P, uint64_t up, uint64_
       const uint32_t o_inc = __shfl_sync(kFull, inc, ol);
       const uint32_t o_c = __shfl_sync(kFull, c, ol);
       const uint32_t o_lo = __shfl_sync(kFull, lo, ol);
+      const uint32_t o_orbs = __shfl_sync(kFull, orbs, ol);
       uint64_t cu = 0, cd = 0;
-      bool single = false, ok = false;
+      bool ok = false;
       if (t < total) {
         const uint32_t e = o_lo + (t - (o_inc - o_c));
-        ok = make_candidate(P, up, dn, s0 + (int)ol, e, &cu, &cd, &single);
+        ok = make_candidate_at(P, up, dn, s0 + (int)ol, o_orbs, e, &cu, &cd);
       }
       f(t < total, ok, cu, cd);
     }
   }
 }
 
+// h % n_batches exactly, without a 64-bit division: a mask for powers of two, else the
+// quotient estimate floor(h * magic / 2^64) with magic = floor((2^64 - 1) / n_batches), which
+// is at most 2 below the true quotient, corrected by subtraction.
+__device__ __forceinline__ uint64_t batch_of(const PtParams& Q, uint64_t h) {
+  const uint64_t nb = Q.n_batches;
+  if ((nb & (nb - 1)) == 0) return h & (nb - 1);
+  uint64_t r = h - __umul64hi(h, Q.batch_magic) * nb;
+  if (r >= nb) r -= nb;
+  if (r >= nb) r -= nb;
+  return r;
+}
+
 // Candidate a of source i belongs to the batch being computed (the first test of the
-// handler, solver.h:703-705).  One batch: every candidate.
+// handler, solver.h:703-705: rehash(DetHasher(a)) % n_batches).  One batch: every candidate.
 __device__ __forceinline__ bool in_batch(const PtParams& Q, uint64_t batch, uint64_t cu,
                                          uint64_t cd) {
-  return Q.n_batches <= 1 || rehash(det_hash(cu, cd)) % Q.n_batches == batch;
+  return Q.n_batches <= 1 || batch_of(Q, rehash(det_hash(cu, cd))) == batch;
+}
+
+void set_batches(PtParams& Q, uint64_t n_batches) {
+  Q.n_batches = n_batches;
+  Q.batch_magic = n_batches ? ~0ull / n_batches : 0;
 }
 
 __device__ __forceinline__ uint64_t src_batch(const PtParams& Q, const StoSources& S, uint32_t k,
@@ -532,7 +551,7 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   const uint32_t n_var = static_cast<uint32_t>(c->up.size());
   StoSources S{};
   // slots per source over all batches (sizes the automatic batch count)
-  Q.n_batches = 1;
+  set_batches(Q, 1);
   Q.batch = 0;
   std::vector<uint64_t> hc = pt_counts<MODE>(c, st, Q, S, n_var);
   if (n_batches == 0) {
@@ -547,7 +566,7 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
     n_batches = static_cast<size_t>(std::ceil(tot * per / (0.4 * free_b)));
     if (n_batches < 1) n_batches = 1;
   }
-  Q.n_batches = n_batches;
+  set_batches(Q, n_batches);
   Pt2Out out;
   double esum = 0.0, esq = 0.0;
   size_t n_sum = 0;
@@ -733,7 +752,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     PtParams Q{};
     Q.eps = eps_pt;
     Q.eps_psto = eps_pt_psto;
-    Q.n_batches = n_batches;
+    set_batches(Q, n_batches);
     Q.factor = factor;
     Q.iter_shift = shift;
     const std::vector<uint64_t> hc = pt_counts<kSto>(c, st, Q, S, n_src);

@@ -237,6 +237,15 @@ def test_pt2_psto_matches_oracle_and_reference(shci, c_oracle, c_atom_pins):
     vo16, uo16, no16, bo16 = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], 16, 0.0, 0.0)
     assert b16 == bo16 == 16 and n16 == no16 and u16 == 0.0
     assert abs(v16 - vo16) < 1e-13
+    # batch counts that are not powers of two (batch = rehash % n_batches without a division)
+    for nb in (3, 7, 100):
+        vb, ub, nbd, bb = c.pt2_psto(ev, 5e-6, pin["eps_pt_psto"], nb, 0.0, 0.0)
+        vob, uob, nob, bob = c_oracle.pt_psto(5e-6, pin["eps_pt_psto"], nb, 0.0, 0.0)
+        assert bb == bob == nb and nbd == nob
+        assert abs(vb - vob) < 1e-13
+        vd, ud, nd = c.pt2_dtm(ev, 5e-6, nb)
+        vod, uod, nod = c_oracle.pt_dtm(5e-6, nb)
+        assert nd == nod and abs(vd - vod) < 1e-13
 
 
 def test_pt2_sto_matches_oracle(shci, oracle_mod, w1_fcidump):
