@@ -197,6 +197,7 @@ def run_pt2(ctx, stream, e_var):
         for _ in range(4):
             ev = torch.cuda.Event(enable_timing=True)
             t.append(ev)
+        ctx.profile(True)
         t[0].record(stream)
         dtm, _, n_dtm = ctx.pt2_dtm(e_var, eps_dtm, 0)
         t[1].record(stream)
@@ -208,7 +209,12 @@ def run_pt2(ctx, stream, e_var):
                                         100, TARGET_ERROR, psto[1])
         t[3].record(stream)
         torch.cuda.synchronize()
+        prof = ctx.profile_get()
+        ctx.profile(False)
         ms = [t[k].elapsed_time(t[k + 1]) for k in range(3)]
+        # device time per stage kind over all three PT2 stages; the rest of the wall time is
+        # host work (sampling, batch bookkeeping) and small launches
+        out["device_ms"] = {k: round(v[0], 2) for k, v in prof.items() if k.startswith("pt2")}
         e2 = dtm + psto[0] + sto
         out.update({"s": sum(ms) / 1e3, "dtm_s": ms[0] / 1e3, "psto_s": ms[1] / 1e3,
                     "sto_s": ms[2] / 1e3, "n_pt_dets_dtm": n_dtm, "psto_batches": psto[3],

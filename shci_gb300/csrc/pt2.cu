@@ -16,7 +16,11 @@
 // src/util.cc:128-175), a chunk of iterations is processed in one device pass with the
 // iteration index stored above the orbital bits of the key, and the reference's stopping
 // rules are then applied iteration by iteration.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
 #include <numeric>
 #include <random>
 #include <stack>
@@ -52,7 +56,12 @@ struct StoSources {
   const double* weight;
   const uint32_t* batch;
   const uint8_t* is_dtm;
+  const uint32_t* remap;  // optional: launch source k' is source remap[k'] (re-runs)
 };
+
+__device__ __forceinline__ uint32_t src_index(const StoSources& S, uint32_t k) {
+  return S.remap ? S.remap[k] : k;
+}
 
 __device__ __forceinline__ uint32_t src_det(const StoSources& S, uint32_t k, int mode) {
   return mode == kSto ? S.det[k] : k;
@@ -137,7 +146,8 @@ __global__ void __launch_bounds__(kPtWarps * 32)
   const unsigned lane = threadIdx.x & 31;
   const uint32_t wpg = gridDim.x * kPtWarps;
   for (uint32_t k = blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < n_src; k += wpg) {
-    const uint32_t i = src_det(S, k, MODE);
+    const uint32_t kk = src_index(S, k);
+    const uint32_t i = src_det(S, kk, MODE);
     const double ac = fabs(P.coef[i]);
     const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
@@ -155,7 +165,7 @@ __global__ void __launch_bounds__(kPtWarps * 32)
         tot += cc;
       }
     } else {
-      const uint64_t batch = src_batch(Q, S, k, MODE);
+      const uint64_t batch = src_batch(Q, S, kk, MODE);
       pt_walk(P, up, dn, eps_min, eps_max, [&](bool, bool ok, uint64_t cu, uint64_t cd) {
         tot += __popc(__ballot_sync(kFull, ok && in_batch(Q, batch, cu, cd)));
       });
@@ -174,43 +184,50 @@ struct PtQueue {
   uint64_t d[kPtQ];
 };
 
-// Emits the batch members of each source into its slots [off, off + count) (one batch: every
-// index entry of the window, as counted by slot ranges).  Members wait in a per-warp queue
-// and are finished 32 at a time (variational-set test, H_ai c_i, the value columns), so the
-// set search and the FP64 element run with full warps; slots of members rejected there, or
-// of entries that make no valid candidate, are written invalid.  Members keep their walk
-// order.
+// Emits the batch members of each source into its region [off[k], off[k + 1]) (one batch:
+// every index entry of the window, as counted by slot ranges).  Members wait in a per-warp
+// queue and are finished 32 at a time (variational-set test, H_ai c_i, the value columns), so
+// the set search and the FP64 element run with full warps; slots of members rejected there,
+// of entries that make no valid candidate, and the unused tail of the region are written
+// invalid.  Members keep their walk order.  A region may be sized by an estimate (several
+// batches): when the members do not fit, the whole region is written invalid and
+// overflow[k] is set, and the caller emits that source again with an exact count.
 template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32)
     k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
-              const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out) {
+              const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out,
+              uint8_t* overflow) {
   __shared__ PtQueue qs[kPtWarps];
   PtQueue& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t wpg = gridDim.x * kPtWarps;
   for (uint32_t k = k_begin + blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < k_end; k += wpg) {
-    const uint32_t i = src_det(S, k, MODE);
+    const uint32_t kk = src_index(S, k);
+    const uint32_t i = src_det(S, kk, MODE);
     const double coef = P.coef[i];
     const double ac = fabs(coef);
     const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
-    const uint64_t batch = src_batch(Q, S, k, MODE);
+    const uint64_t batch = src_batch(Q, S, kk, MODE);
     double count = 1.0, weight = 1.0;
     bool dtm_src = true;
     uint64_t iter_tag = 0;
     if (MODE == kSto) {
-      dtm_src = S.is_dtm[k] != 0;
-      count = dtm_src ? 1.0 : S.count[k];
-      weight = dtm_src ? 1.0 : S.weight[k];
-      iter_tag = static_cast<uint64_t>(S.iter[k]) << Q.iter_shift;
+      dtm_src = S.is_dtm[kk] != 0;
+      count = dtm_src ? 1.0 : S.count[kk];
+      weight = dtm_src ? 1.0 : S.weight[kk];
+      iter_tag = static_cast<uint64_t>(S.iter[kk]) << Q.iter_shift;
     }
-    uint64_t base = off[k - k_begin];
+    const uint64_t start = off[k - k_begin], limit = off[k - k_begin + 1];
+    uint64_t base = start;
+    bool over = false;  // warp-uniform
     uint32_t qh = 0, qn = 0;
     auto drain = [&](uint32_t m) {
       __syncwarp();
-      if (lane < m) {
+      if (base + m > limit) over = true;
+      if (lane < m && !over) {
         const uint32_t sl = (qh + lane) & (kPtQ - 1);
         const uint64_t cu = q.u[sl], cd = q.d[sl];
         // handler order of solver.h:703-713: batch (done), variational set, |H_ai c_i|
@@ -262,6 +279,9 @@ __global__ void __launch_bounds__(kPtWarps * 32)
       if (qn >= 32u) drain(32u);
     });
     if (qn) drain(qn);
+    // invalid tail, or (overflow) the whole region
+    for (uint64_t p = (over ? start : base) + lane; p < limit; p += 32) out_up[p] = kInvalid;
+    if (over && lane == 0) overflow[k - k_begin] = 1;
   }
 }
 
@@ -429,36 +449,44 @@ constexpr int n_cols() {
   return MODE == kDtm ? 1 : MODE == kPsto ? 2 : 5;
 }
 
-// Emits and reduces the pairs of the sources [0, n_src) for one (batch / set of iterations);
-// returns the unique count, keys in (bu, bd) and value columns in bv[0..n_cols).
+// Emits the pairs of the sources [0, n_src) for one batch (or set of iterations), appending
+// the valid ones to (bu, bd, bv) after the first *bn; slots[k] = the size of source k's
+// region.  Sources whose region overflowed (regions sized by an estimate) are appended to
+// *over as launch indices.  The accumulation is sorted and reduced in place whenever it
+// grows past kCap, to keep it bounded.
 template <int MODE>
-size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
-                      uint32_t n_src, const std::vector<uint64_t>& hc, DevBuf<uint64_t>& bu,
-                      DevBuf<uint64_t>& bd, DevBuf<double>* bv, int a_bits) {
+void pt_emit_append(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
+                    uint32_t n_src, const std::vector<uint64_t>& slots, DevBuf<uint64_t>& bu,
+                    DevBuf<uint64_t>& bd, DevBuf<double>* bv, size_t* bn, int a_bits,
+                    std::vector<uint32_t>* over) {
   constexpr int NV = n_cols<MODE>();
   cudaStream_t s = c->stream;
   const uint64_t kCap = 1ull << 27;
   DevBuf<uint64_t> cu, cd;
   DevBuf<double> cv[NV];
+  DevBuf<uint8_t> d_over;
   cu.mt = cd.mt = &c->mem;
+  d_over.mt = &c->mem;
   for (int v = 0; v < NV; v++) cv[v].mt = &c->mem;
-  size_t bn = 0;
   uint32_t k0 = 0;
   while (k0 < n_src) {
     uint64_t tot = 0;
     uint32_t k1 = k0;
-    while (k1 < n_src && (k1 == k0 || tot + hc[k1] <= kCap)) tot += hc[k1++];
+    while (k1 < n_src && (k1 == k0 || tot + slots[k1] <= kCap)) tot += slots[k1++];
     if (tot > 0) {
-      std::vector<uint64_t> off(k1 - k0);
+      std::vector<uint64_t> off(k1 - k0 + 1);
       uint64_t acc = 0;
       for (uint32_t k = k0; k < k1; k++) {
         off[k - k0] = acc;
-        acc += hc[k];
+        acc += slots[k];
       }
+      off[k1 - k0] = acc;
       DevBuf<uint64_t> d_off;
       d_off.mt = &c->mem;
       d_off.resize(off.size());
       SHCI_CUDA(cudaMemcpyAsync(d_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
+      d_over.resize(k1 - k0);
+      SHCI_CUDA(cudaMemsetAsync(d_over.p, 0, k1 - k0, s));
       cu.resize(tot, 1.25);
       cd.resize(tot, 1.25);
       OutCols oc{};
@@ -471,17 +499,54 @@ size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSour
       {
         ProfScope ps(c->prof, s, "pt2_emit");
         k_pt_emit<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, k0, k1, d_off.p, cu.p,
-                                                          cd.p, oc);
+                                                          cd.p, oc, d_over.p);
         SHCI_LAUNCH_CHECK();
       }
       c->launches += 1;
-      compact_valid(c, cu.p, cd.p, vptr, NV, tot, bu, bd, bv, &bn);
-      if (bn > kCap) {  // keep the accumulation buffer bounded
-        bn = sort_unique_pairs(c, bu, bd, bn, bv, NV, a_bits);
-        bu.n = bd.n = bn;
+      compact_valid(c, cu.p, cd.p, vptr, NV, tot, bu, bd, bv, bn);
+      std::vector<uint8_t> h_over(k1 - k0);
+      SHCI_CUDA(cudaMemcpyAsync(h_over.data(), d_over.p, k1 - k0, cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      for (uint32_t k = k0; k < k1; k++)
+        if (h_over[k - k0]) over->push_back(k);
+      if (*bn > kCap) {  // keep the accumulation buffer bounded
+        *bn = sort_unique_pairs(c, bu, bd, *bn, bv, NV, a_bits);
+        bu.n = bd.n = *bn;
       }
     }
     k0 = k1;
+  }
+}
+
+template <int MODE>
+std::vector<uint64_t> pt_counts(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
+                                uint32_t n_src);
+
+// Emits and reduces the pairs of the sources [0, n_src) for one batch / set of iterations;
+// returns the unique count, keys in (bu, bd) and value columns in bv[0..n_cols).  slots are
+// exact counts or estimates; sources whose estimated region overflowed are emitted again,
+// after the others, with exact counts.
+template <int MODE>
+size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSources& S,
+                      uint32_t n_src, const std::vector<uint64_t>& slots, DevBuf<uint64_t>& bu,
+                      DevBuf<uint64_t>& bd, DevBuf<double>* bv, int a_bits) {
+  constexpr int NV = n_cols<MODE>();
+  cudaStream_t s = c->stream;
+  size_t bn = 0;
+  std::vector<uint32_t> over;
+  pt_emit_append<MODE>(c, st, Q, S, n_src, slots, bu, bd, bv, &bn, a_bits, &over);
+  if (!over.empty()) {
+    DevBuf<uint32_t> remap;
+    remap.mt = &c->mem;
+    remap.resize(over.size());
+    SHCI_CUDA(cudaMemcpyAsync(remap.p, over.data(), over.size() * 4, cudaMemcpyHostToDevice, s));
+    StoSources S2 = S;
+    S2.remap = remap.p;
+    const uint32_t n2 = static_cast<uint32_t>(over.size());
+    const std::vector<uint64_t> exact = pt_counts<MODE>(c, st, Q, S2, n2);
+    std::vector<uint32_t> over2;
+    pt_emit_append<MODE>(c, st, Q, S2, n2, exact, bu, bd, bv, &bn, a_bits, &over2);
+    if (!over2.empty()) throw std::logic_error("PT2 emission: exact regions overflowed");
   }
   {
     ProfScope ps(c->prof, s, "pt2_reduce");
@@ -489,6 +554,22 @@ size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSour
   }
   bu.n = bd.n = bn;
   return bn;
+}
+
+// Region sizes from bounds (each source's window entries, an exact count with one batch):
+// with several batches a source's members are a binomial(bound, 1 / n_batches) count, and
+// bound / n_batches * 1.3 + 64 exceeds its mean by many standard deviations (overflowing
+// sources are re-run exactly).  SHCI_PT_SLOTS="slack,pad" replaces 1.3 and 64.
+std::vector<uint64_t> region_slots(const std::vector<uint64_t>& bound, uint64_t n_batches) {
+  if (n_batches <= 1) return bound;
+  double slack = 1.3, pad = 64.0;
+  if (const char* e = std::getenv("SHCI_PT_SLOTS")) std::sscanf(e, "%lf,%lf", &slack, &pad);
+  std::vector<uint64_t> r(bound.size());
+  for (size_t k = 0; k < bound.size(); k++) {
+    const double est = std::ceil(static_cast<double>(bound[k]) / n_batches * slack + pad);
+    r[k] = std::min<uint64_t>(bound[k], static_cast<uint64_t>(std::max(0.0, est)));
+  }
+  return r;
 }
 
 template <int MODE>
@@ -500,8 +581,11 @@ std::vector<uint64_t> pt_counts(shci_ctx* c, PtSetup& st, const PtParams& Q, con
   cnt.resize(n_src ? n_src : 1);
   std::vector<uint64_t> hc(n_src);
   if (n_src) {
-    k_pt_count<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, n_src, cnt.p);
-    SHCI_LAUNCH_CHECK();
+    {
+      ProfScope ps(c->prof, s, "pt2_count");
+      k_pt_count<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, n_src, cnt.p);
+      SHCI_LAUNCH_CHECK();
+    }
     SHCI_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_src * 8, cudaMemcpyDeviceToHost, s));
     SHCI_CUDA(cudaStreamSynchronize(s));
     c->launches += 1;
@@ -567,6 +651,8 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
     if (n_batches < 1) n_batches = 1;
   }
   set_batches(Q, n_batches);
+  // regions per source: exact with one batch, estimated from the window counts otherwise
+  const std::vector<uint64_t> slots = region_slots(hc, n_batches);
   Pt2Out out;
   double esum = 0.0, esq = 0.0;
   size_t n_sum = 0;
@@ -576,9 +662,7 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   for (size_t batch = 0; batch < n_batches; batch++) {
     Q.batch = batch;
     bu.n = bd.n = 0;
-    // with several batches each source's slots are its candidates in this batch
-    if (n_batches > 1) hc = pt_counts<MODE>(c, st, Q, S, n_var);
-    const size_t bn = pt_emit_reduce<MODE>(c, st, Q, S, n_var, hc, bu, bd, bv, 0);
+    const size_t bn = pt_emit_reduce<MODE>(c, st, Q, S, n_var, slots, bu, bd, bv, 0);
     double bs, bsq;
     pt_batch_sums<MODE>(c, bu, bd, bv, bn, e_var, &bs, &bsq);
     n_sum += bn;
@@ -755,7 +839,9 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     set_batches(Q, n_batches);
     Q.factor = factor;
     Q.iter_shift = shift;
-    const std::vector<uint64_t> hc = pt_counts<kSto>(c, st, Q, S, n_src);
+    PtParams Q1 = Q;
+    set_batches(Q1, 1);
+    const std::vector<uint64_t> hc = region_slots(pt_counts<kSto>(c, st, Q1, S, n_src), n_batches);
     DevBuf<uint64_t> bu, bd;
     DevBuf<double> bv[5];
     bu.mt = bd.mt = &c->mem;

@@ -248,6 +248,26 @@ def test_pt2_psto_matches_oracle_and_reference(shci, c_oracle, c_atom_pins):
         assert nd == nod and abs(vd - vod) < 1e-13
 
 
+def test_pt2_overflowing_regions_rerun_exactly(shci, c_oracle, monkeypatch):
+    """With several batches each source's output region is sized by an estimate; regions far
+    too small (SHCI_PT_SLOTS) make nearly every source overflow and be emitted again with an
+    exact count: the results still equal the oracle's."""
+    up, dn, coefs = c_oracle.dets()
+    ev = c_oracle.energy_var
+    monkeypatch.setenv("SHCI_PT_SLOTS", "0.3,0")
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    for nb in (4, 7):
+        v, u, n, b = c.pt2_psto(ev, 5e-6, 5e-7, nb, 0.0, 0.0)
+        vo, uo, no, bo = c_oracle.pt_psto(5e-6, 5e-7, nb, 0.0, 0.0)
+        assert b == bo == nb and n == no
+        assert abs(v - vo) < 1e-13
+        vd, ud, nd = c.pt2_dtm(ev, 5e-6, nb)
+        vod, uod, nod = c_oracle.pt_dtm(5e-6, nb)
+        assert nd == nod and abs(vd - vod) < 1e-13
+
+
 def test_pt2_sto_matches_oracle(shci, oracle_mod, w1_fcidump):
     """Stochastic stage: the host draws the same samples as the reference's generator, so
     every iteration's estimate equals the oracle's."""
