@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <map>
 #include <string>
 #include <vector>
@@ -36,6 +37,29 @@ struct Profiler {
     }
     pending.clear();
   }
+  // Host time of a named stage (wall clock, ms).
+  void host(const char* name, double ms) {
+    auto& e = acc[name];
+    e.first += ms;
+    e.second += 1;
+  }
+};
+
+// Wall-clock timing of host work when profiling is on.
+class HostScope {
+ public:
+  HostScope(Profiler& p, const char* name)
+      : p_(p), name_(name), t0_(std::chrono::steady_clock::now()) {}
+  ~HostScope() {
+    if (p_.on)
+      p_.host(name_, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                               t0_).count());
+  }
+
+ private:
+  Profiler& p_;
+  const char* name_;
+  std::chrono::steady_clock::time_point t0_;
 };
 
 // Records an event pair around the enclosed launches when profiling is on.

@@ -17,6 +17,7 @@
 // iteration index stored above the orbital bits of the key, and the reference's stopping
 // rules are then applied iteration by iteration.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -503,7 +504,10 @@ void pt_emit_append(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSource
         SHCI_LAUNCH_CHECK();
       }
       c->launches += 1;
-      compact_valid(c, cu.p, cd.p, vptr, NV, tot, bu, bd, bv, bn);
+      {
+        ProfScope ps(c->prof, s, "pt2_compact");
+        compact_valid(c, cu.p, cd.p, vptr, NV, tot, bu, bd, bv, bn);
+      }
       std::vector<uint8_t> h_over(k1 - k0);
       SHCI_CUDA(cudaMemcpyAsync(h_over.data(), d_over.p, k1 - k0, cudaMemcpyDeviceToHost, s));
       SHCI_CUDA(cudaStreamSynchronize(s));
@@ -698,32 +702,28 @@ void alias_tables(const std::vector<double>& p, std::vector<double>& np, std::ve
   np.assign(L, 0.0);
   al.assign(L, 0);
   std::vector<double> t(L);
-  std::stack<size_t> small, large;
+  std::vector<size_t> small, large;  // used as stacks (back = top)
+  small.reserve(L);
+  large.reserve(L);
   for (size_t i = 0; i < L; i++) {
     t[i] = p[i] * L;
-    if (t[i] < 1.) small.push(i);
-    else large.push(i);
+    if (t[i] < 1.) small.push_back(i);
+    else large.push_back(i);
   }
   while (!small.empty() && !large.empty()) {
-    const size_t l = large.top(), s = small.top();
+    const size_t l = large.back(), s = small.back();
     np[s] = t[s];
     al[s] = l;
     t[l] = t[l] + t[s] - 1.;
     if (t[l] < 1.) {
-      large.pop();
-      small.top() = l;
+      large.pop_back();
+      small.back() = l;
     } else {
-      small.pop();
+      small.pop_back();
     }
   }
-  while (!large.empty()) {
-    np[large.top()] = 1.;
-    large.pop();
-  }
-  while (!small.empty()) {
-    np[small.top()] = 1.;
-    small.pop();
-  }
+  for (size_t i : large) np[i] = 1.;
+  for (size_t i : small) np[i] = 1.;
 }
 
 }  // namespace
@@ -761,6 +761,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   cudaStream_t s = c->stream;
   SHCI_CUDA(cudaMemcpyAsync(coefs.data(), c->d_coef.p, n_var * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
+  const auto t_setup = std::chrono::steady_clock::now();
   // probabilities (solver.h:921-933)
   double sum_w = 0.0;
   for (size_t i = 0; i < n_var; i++) sum_w += std::abs(coefs[i]);
@@ -781,6 +782,10 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   // stopping rules cannot fire, later passes 2 (results past the stop are discarded).
   const uint32_t kFirstChunk = 6, kNextChunk = 2;
 
+  std::vector<uint32_t> cnt(n_var, 0u);  // per-iteration sample counts (zero between uses)
+  if (c->prof.on)
+    c->prof.host("pt2_host_setup", std::chrono::duration<double, std::milli>(
+                                       std::chrono::steady_clock::now() - t_setup).count());
   PtSetup st;
   pt_setup(c, st);
   Pt2Out out;
@@ -794,25 +799,29 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     std::vector<uint32_t> h_det, h_iter, h_batch;
     std::vector<double> h_count, h_weight;
     std::vector<uint8_t> h_dtm;
-    for (uint32_t it = 0; it < n_it; it++) {
-      std::unordered_map<size_t, unsigned> cnt;
-      std::vector<size_t> list;
-      for (size_t k = 0; k < n_dets_in_sample - n_dtm; k++) {
-        const size_t r1 = ui_var(gen);
-        const double r2 = ur(gen);
-        const size_t id = r2 < aprob[r1] ? r1 : alias[r1];
-        if (cnt.count(id) == 0) list.push_back(id);
-        cnt[id]++;
-      }
-      const size_t batch_id = ui_batch(gen);
-      for (size_t k = 0; k < list.size(); k++) {
-        const size_t i = list[k];
-        h_det.push_back(static_cast<uint32_t>(i));
-        h_iter.push_back(it);
-        h_batch.push_back(static_cast<uint32_t>(batch_id));
-        h_count.push_back(static_cast<double>(cnt[i]));
-        h_weight.push_back((n_dets_in_sample - n_dtm) * probs[i]);
-        h_dtm.push_back(k < n_dtm ? 1 : 0);
+    {
+      HostScope hs(c->prof, "pt2_host_sample");
+      for (uint32_t it = 0; it < n_it; it++) {
+        // sample counts per det, and the dets in order of first draw (the reference's
+        // unordered_map counts and insertion-ordered list); cnt is cleared after use
+        std::vector<size_t> list;
+        for (size_t k = 0; k < n_dets_in_sample - n_dtm; k++) {
+          const size_t r1 = ui_var(gen);
+          const double r2 = ur(gen);
+          const size_t id = r2 < aprob[r1] ? r1 : alias[r1];
+          if (cnt[id]++ == 0) list.push_back(id);
+        }
+        const size_t batch_id = ui_batch(gen);
+        for (size_t k = 0; k < list.size(); k++) {
+          const size_t i = list[k];
+          h_det.push_back(static_cast<uint32_t>(i));
+          h_iter.push_back(it);
+          h_batch.push_back(static_cast<uint32_t>(batch_id));
+          h_count.push_back(static_cast<double>(cnt[i]));
+          h_weight.push_back((n_dets_in_sample - n_dtm) * probs[i]);
+          h_dtm.push_back(k < n_dtm ? 1 : 0);
+        }
+        for (size_t i : list) cnt[i] = 0;
       }
     }
     const uint32_t n_src = static_cast<uint32_t>(h_det.size());
