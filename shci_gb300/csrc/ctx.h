@@ -120,6 +120,8 @@ struct shci_ctx {
 
   // sorted membership keys of the current det list (for selection / PT2)
   shci::DevBuf<uint64_t> set_up, set_dn;
+  shci::DevBuf<unsigned long long> set_hash;  // hash set of the det list (in_set)
+  uint64_t set_hash_mask = 0;
 
   std::vector<double> eps_tried;
 

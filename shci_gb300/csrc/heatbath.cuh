@@ -31,6 +31,8 @@ struct SelParams {
   const uint64_t* set_up;    // sorted variational set
   const uint64_t* set_dn;
   uint32_t set_n;
+  const unsigned long long* set_hash;  // hash set of the variational dets (see in_set)
+  uint64_t set_hash_mask;
   double eps_var;
   double max_hci, max_singles;
   int n_orbs, n_up, n_elecs, n_pairs;
@@ -103,7 +105,37 @@ __device__ __forceinline__ void slot_range(const SelParams& P, uint64_t up, uint
   *cnt = e - s;
 }
 
+// Slot hash of a det for the variational hash set: the reference's det hash, remixed
+// (SplitMix64 finaliser) so that its low bits index the table and its high bits fingerprint.
+__host__ __device__ __forceinline__ uint64_t set_slot_hash(uint64_t u, uint64_t d) {
+  uint64_t h = det_hash(u, d);
+  h ^= h >> 30;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 27;
+  h *= 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  return h;
+}
+
+// Is (u, d) a variational det?  With the hash set (slots hold fingerprint << 32 | det id + 1,
+// linear probing, at most half full) one or two probes and a comparison against the det
+// list; otherwise a binary search of the sorted set.
 __device__ __forceinline__ bool in_set(const SelParams& P, uint64_t u, uint64_t d) {
+  if (P.set_hash) {
+    const uint64_t h = set_slot_hash(u, d);
+    const uint32_t fp = static_cast<uint32_t>(h >> 32);
+    uint64_t p = h & P.set_hash_mask;
+    for (uint64_t probe = 0; probe <= P.set_hash_mask; probe++) {
+      const unsigned long long v = P.set_hash[p];
+      if (v == 0ull) return false;
+      if (static_cast<uint32_t>(v >> 32) == fp) {
+        const uint32_t id = static_cast<uint32_t>(v) - 1u;
+        if (P.up[id] == u && P.dn[id] == d) return true;
+      }
+      p = (p + 1) & P.set_hash_mask;
+    }
+    return false;
+  }
   uint32_t lo = 0, hi = P.set_n;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;

@@ -434,6 +434,8 @@ void pt_setup(shci_ctx* c, PtSetup& st) {
   P.set_up = c->set_up.p;
   P.set_dn = c->set_dn.p;
   P.set_n = static_cast<uint32_t>(c->set_up.n);
+  P.set_hash = c->set_hash.p;
+  P.set_hash_mask = c->set_hash_mask;
   P.max_hci = c->Q.max_hci;
   P.max_singles = c->Q.max_singles;
   P.n_orbs = c->I.n;

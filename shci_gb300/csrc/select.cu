@@ -269,6 +269,22 @@ void compact_valid(shci_ctx* c, const uint64_t* a, const uint64_t* b, const doub
 }
 
 // Sorted copy of the whole det list, the membership set used by selection and PT2.
+// Inserts det ids into the variational hash set (slot = fingerprint << 32 | id + 1, linear
+// probing; the table is at most half full, so every insertion finds an empty slot).
+__global__ void k_hash_insert(const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
+                              size_t n, unsigned long long* table, uint64_t mask) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t h = set_slot_hash(up[i], dn[i]);
+    const unsigned long long v = ((h >> 32) << 32) | (static_cast<unsigned long long>(i) + 1ull);
+    uint64_t p = h & mask;
+    for (uint64_t probe = 0; probe <= mask; probe++) {
+      if (atomicCAS(&table[p], 0ull, v) == 0ull) break;
+      p = (p + 1) & mask;
+    }
+  }
+}
+
 void rebuild_det_set(shci_ctx* c) {
   const size_t n = c->up.size();
   cudaStream_t s = c->stream;
@@ -279,6 +295,17 @@ void rebuild_det_set(shci_ctx* c) {
   SHCI_CUDA(cudaMemcpyAsync(c->set_dn.p, c->d_dn.p, n * 8, cudaMemcpyDeviceToDevice, s));
   const size_t nu = sort_unique_pairs(c, c->set_up, c->set_dn, n);
   if (nu != n) throw ArgError("the det list contains duplicates");
+  // hash set over the det list: a power of two >= 2n slots
+  size_t slots = 1024;
+  while (slots < 2 * n) slots <<= 1;
+  c->set_hash.mt = &c->mem;
+  c->set_hash.resize(slots, 1.0);
+  c->set_hash_mask = slots - 1;
+  SHCI_CUDA(cudaMemsetAsync(c->set_hash.p, 0, slots * 8, s));
+  k_hash_insert<<<grid_for(n, 256), 256, 0, s>>>(c->d_up.p, c->d_dn.p, n, c->set_hash.p,
+                                                 c->set_hash_mask);
+  SHCI_LAUNCH_CHECK();
+  c->launches += 1;
 }
 
 size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
@@ -342,6 +369,8 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
     P.set_up = c->set_up.p;
     P.set_dn = c->set_dn.p;
     P.set_n = static_cast<uint32_t>(c->set_up.n);
+    P.set_hash = c->set_hash.p;
+    P.set_hash_mask = c->set_hash_mask;
     const uint32_t n_src = n_dets > pass ? static_cast<uint32_t>((n_dets - pass + 4) / 5) : 0;
     size_t pass_n = 0;
     pass_up.n = pass_dn.n = 0;
