@@ -52,11 +52,20 @@ __device__ __forceinline__ int elec_orb(uint64_t up, uint64_t dn, int e, int n_u
   return e < n_up ? nth_bit(up, e) : nth_bit(dn, e - n_up) + n;
 }
 
+// First k in [lo, hi) with a[k] < x, for a descending array of non-negative values and
+// any x.  Non-negative doubles order like the integers of their bit patterns (a negative or
+// NaN x compares false against every entry, as in FP64), so the comparisons run on the
+// integer pipe (the FP64 pipe is slow on GB300) with the same result.
 __device__ __forceinline__ uint32_t first_below(const double* a, uint32_t lo, uint32_t hi,
                                                 double x) {
+  long long xb = __double_as_longlong(x);
+  if ((xb & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) xb = -1;  // NaN: never above an entry
+  const long long* ab = reinterpret_cast<const long long*>(a);
+  // the usual cases: the window starts at the slot's largest entry or is empty
+  if (lo < hi && ab[lo] < xb) return lo;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (a[mid] < x) hi = mid;
+    if (ab[mid] < xb) hi = mid;
     else lo = mid + 1;
   }
   return lo;
