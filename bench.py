@@ -104,6 +104,18 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(value, device):
+    """The job's clock for N independent replicas: the largest per-rank value (identity on
+    one rank or without an initialised process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_workload(data_dir):
     from shci_gb300 import synthetic
     return synthetic.workload_fcidump(WORKLOAD, data_dir), synthetic.WORKLOADS[WORKLOAD]
@@ -308,11 +320,7 @@ def run_ours(args):
     ctx.profile(False)
     ms = ev0.elapsed_time(ev1) / args.steps
     stats = ctx.hamiltonian_stats()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, f"cuda:{local}")
 
     # PT2 on the step's wavefunction (the metric's "PT2 s"): dtm, psto, sto stages
     pt2 = run_pt2(ctx, stream, e_mixed) if args.pt2 else None
