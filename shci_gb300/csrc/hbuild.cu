@@ -543,6 +543,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   }
   SHCI_CUDA(cudaStreamSynchronize(s));
   if (H.join) join_release(c);
+  if (row_sort_enabled()) sort_rows(c);
   c->prof.flush();
   H.valid = true;
   c->launches += 5;

@@ -45,10 +45,15 @@ void join_release(shci_ctx* c);
 // (row_start has n + 1 entries); returns the total capacity.
 uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start);
 
+// rowsort.cu: sorts each row of the element store by column (tiles of 2048 elements), so
+// that H*v's scattered accesses share sectors; SHCI_ROW_SORT=0 turns the pass off.
+bool row_sort_enabled();
+void sort_rows(shci_ctx* c);
+
 // spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
 void spmv(shci_ctx* c, const double* x, double* y, bool residual);
-// Mixed H*v needs a bound on the row abs sums: the count pass of a mixed build sums |H_ij|
-// into H.rowabs (off-diagonal), and this turns the sums into the bound.
+// Mixed H*v needs a bound on the row abs sums: a mixed build sums |H_ij| into H.rowabs
+// (off-diagonal) during its count or single fill pass, and this turns the sums into the bound.
 void finish_mixed_bound(shci_ctx* c);
 
 // davidson.cu

@@ -1,0 +1,262 @@
+// Column order of the element store's rows (a post-pass of the Hamiltonian build).
+//
+// H*v (spmv.cu) streams a row's (col, val) pairs 32 at a time, one per lane, and each pair
+// costs a scattered read of x[j] and a scattered atomic on y[j].  Those scattered accesses
+// bound the kernel, and a warp instruction costs one L1 wavefront per distinct line it
+// touches, so columns that fall in the same 32-byte sector or 128-byte line should sit in
+// the same 32-element chunk of the row.  The build emits a row in the order its traversal
+// finds the columns (unrelated to j), so this pass sorts every row by column, in tiles of
+// 2,048 elements: on the n = 40 10a10b workload that cuts the distinct sectors per element
+// from 0.99 to about 0.85 and the distinct lines from 0.98 to about 0.69.  Only the order
+// inside a row changes: connection lists and values are the same (the reference's
+// SparseMatrix rows carry no order beyond the diagonal first, src/solver/sparse_matrix.h).
+//
+// A CTA takes one row at a time (work counter) and sorts its elements in tiles of kTile,
+// fully by column, with few shared-memory accesses per element (random shared accesses
+// bound this pass).  Each thread holds kPer elements in registers.  A 65,536-bin bitmap
+// over the tile's column range [jmin, jmax] (bin width 2^s, the smallest that covers the
+// range) marks the occupied bins; prefix popcounts give each occupied bin a dense id; one
+// shared atomic per element counts its bin and returns its arrival index; the counts are
+// scanned into bin starts.  Columns are unique within a row, so an element alone in its bin
+// has its final slot (the bin start); the elements of a bin holding several (nearby
+// columns, at most 2^s) are ranked by counting the smaller columns of the bin.  Each element
+// is stored once at its final slot and the tile goes back to global memory coalesced.  The
+// outcome does not depend on the order of the atomics: every tile ends up in strictly
+// increasing column order.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+
+#include "ctx.h"
+#include "kernels.h"
+
+namespace shci {
+
+namespace {
+
+constexpr int kTile = 2048;          // elements per sorted tile
+constexpr int kSortWarps = 8;
+constexpr int kSortThreads = kSortWarps * 32;
+constexpr int kBinWords = 2048;      // 65,536-bin bitmap
+constexpr int kPer = kTile / kSortThreads;
+static_assert(kBinWords == kTile && kPer * kSortThreads == kTile, "one scan layout for both");
+
+struct SortSmem {
+  uint32_t bm[kBinWords];   // occupied bins
+  uint32_t pre[kBinWords];  // occupied bins before each bitmap word; then bin members' columns
+  uint32_t cnt[kTile];      // per dense bin: count, then start
+  uint32_t ocol[kTile];     // the tile in column order
+  uint64_t oval[kTile];     // FP64 value, or FP32 value (low word) + FP32 residual (high word)
+  uint32_t wsum[kSortWarps];
+  uint32_t jmin, jmax, row;
+};
+
+// Block-wide exclusive scan of a[0, m) in place, m <= kTile (kPer consecutive entries per
+// thread; threads past m contribute nothing).
+__device__ void scan_in_place(SortSmem& S, uint32_t* a, int m) {
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int base = threadIdx.x * kPer;
+  uint32_t v[kPer], tot = 0;
+  if (base < m) {
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      v[k] = base + k < m ? a[base + k] : 0u;
+      tot += v[k];
+    }
+  }
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= (unsigned)o) inc += t;
+  }
+  if (lane == 31) S.wsum[warp] = inc;
+  __syncthreads();
+  if (base < m) {
+    uint32_t run = inc - tot;
+    for (unsigned w = 0; w < warp; w++) run += S.wsum[w];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      if (base + k < m) a[base + k] = run;
+      run += v[k];
+    }
+  }
+  __syncthreads();
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kSortThreads, 3)
+    k_sort_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+                uint32_t n, uint32_t* col, double* v64, float* v32, float* r32, unsigned* work) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SortSmem& S = *reinterpret_cast<SortSmem*>(smem_raw);
+  const unsigned lane = threadIdx.x & 31;
+  while (true) {
+    if (threadIdx.x == 0) S.row = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t i = S.row;
+    __syncthreads();
+    if (i >= n) break;
+    const uint32_t len = row_len[i];
+    if (len <= 32) continue;  // one chunk: its order does not matter
+    for (uint32_t t0 = 0; t0 < len; t0 += kTile) {
+      const int L = static_cast<int>(min(static_cast<uint32_t>(kTile), len - t0));
+      if (L <= 32) break;
+      const uint64_t g = row_ptr[i] + t0;
+      constexpr int W = kBinWords;
+      if (threadIdx.x == 0) {
+        S.jmin = 0xffffffffu;
+        S.jmax = 0u;
+      }
+      for (int t = threadIdx.x; t < W; t += kSortThreads) S.bm[t] = 0u;
+      for (int t = threadIdx.x; t < L; t += kSortThreads) S.cnt[t] = 0u;
+      // all of a thread's loads are issued before any is used
+      uint32_t rj[kPer];
+      uint64_t rv[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; k++) {
+        const int p = threadIdx.x + k * kSortThreads;
+        if (p < L) {
+          rj[k] = col[g + p];
+          if (MIXED)
+            rv[k] = static_cast<uint64_t>(__float_as_uint(v32[g + p])) |
+                    (static_cast<uint64_t>(__float_as_uint(r32[g + p])) << 32);
+          else
+            rv[k] = static_cast<uint64_t>(__double_as_longlong(v64[g + p]));
+        }
+      }
+      uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+      for (int k = 0; k < kPer; k++)
+        if (threadIdx.x + k * kSortThreads < L) {
+          lo = min(lo, rj[k]);
+          hi = max(hi, rj[k]);
+        }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+        hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+      }
+      __syncthreads();  // bitmap and counts cleared, jmin / jmax reset
+      if (lane == 0) {
+        atomicMin(&S.jmin, lo);
+        atomicMax(&S.jmax, hi);
+      }
+      __syncthreads();
+      // bin b = (j - jmin) >> s < 65,536
+      const uint32_t jmin = S.jmin;
+      const uint32_t wide = (S.jmax - jmin) >> 16;
+      const int s = wide ? 32 - __clz(wide) : 0;
+#pragma unroll
+      for (int k = 0; k < kPer; k++)
+        if (threadIdx.x + k * kSortThreads < L) {
+          const uint32_t b = (rj[k] - jmin) >> s;
+          atomicOr(&S.bm[b >> 5], 1u << (b & 31));
+        }
+      __syncthreads();
+      for (int t = threadIdx.x; t < W; t += kSortThreads) S.pre[t] = __popc(S.bm[t]);
+      __syncthreads();
+      scan_in_place(S, S.pre, W);
+      const uint32_t nb = S.pre[W - 1] + __popc(S.bm[W - 1]);  // occupied bins
+      // dense bin id and arrival index of each element
+      uint32_t rd[kPer], ra[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; k++)
+        if (threadIdx.x + k * kSortThreads < L) {
+          const uint32_t b = (rj[k] - jmin) >> s, w = b >> 5;
+          rd[k] = S.pre[w] + __popc(S.bm[w] & ((1u << (b & 31)) - 1u));
+          ra[k] = atomicAdd(&S.cnt[rd[k]], 1u);
+        }
+      __syncthreads();
+      scan_in_place(S, S.cnt, static_cast<int>(nb));  // bin starts
+      // rd <- bin start, ra <- bin size | slot << 16; members of shared bins list their
+      // columns in pre (free now)
+#pragma unroll
+      for (int k = 0; k < kPer; k++)
+        if (threadIdx.x + k * kSortThreads < L) {
+          const uint32_t st = S.cnt[rd[k]];
+          const uint32_t en = rd[k] + 1 < nb ? S.cnt[rd[k] + 1] : static_cast<uint32_t>(L);
+          const uint32_t slot = st + ra[k];
+          if (en - st > 1) S.pre[slot] = rj[k];
+          rd[k] = st;
+          ra[k] = (en - st) | (slot << 16);
+        }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kPer; k++)
+        if (threadIdx.x + k * kSortThreads < L) {
+          const uint32_t st = rd[k], m = ra[k] & 0xffffu, slot = ra[k] >> 16;
+          uint32_t rank = 0;
+          // smaller columns of the bin (ties, absent for unique columns, by slot)
+          if (m > 1)
+            for (uint32_t q = st; q < st + m; q++) {
+              const uint32_t jq = S.pre[q];
+              rank += (jq < rj[k]) | ((jq == rj[k]) & (q < slot));
+            }
+          S.ocol[st + rank] = rj[k];
+          S.oval[st + rank] = rv[k];
+        }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kPer; k++) {
+        const int p = threadIdx.x + k * kSortThreads;
+        if (p < L) {
+          col[g + p] = S.ocol[p];
+          const uint64_t v = S.oval[p];
+          if (MIXED) {
+            v32[g + p] = __uint_as_float(static_cast<uint32_t>(v));
+            r32[g + p] = __uint_as_float(static_cast<uint32_t>(v >> 32));
+          } else {
+            v64[g + p] = __longlong_as_double(static_cast<long long>(v));
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace
+
+bool row_sort_enabled() {
+  const char* e = std::getenv("SHCI_ROW_SORT");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+
+void sort_rows(shci_ctx* c) {
+  auto& H = c->H;
+  const uint32_t n = static_cast<uint32_t>(H.n);
+  if (n == 0 || H.nnz == 0) return;
+  cudaStream_t s = c->stream;
+  int dev_sms = 0, per_sm = 0;
+  SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  const size_t smem = sizeof(SortSmem);
+  const bool mixed = H.precision != SHCI_PREC_FP64;
+  if (mixed) {
+    SHCI_CUDA(cudaFuncSetAttribute(k_sort_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+    SHCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sort_rows<true>,
+                                                            kSortThreads, smem));
+  } else {
+    SHCI_CUDA(cudaFuncSetAttribute(k_sort_rows<false>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+    SHCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sort_rows<false>,
+                                                            kSortThreads, smem));
+  }
+  const unsigned grid = static_cast<unsigned>(dev_sms) * static_cast<unsigned>(std::max(1, per_sm));
+  c->err_word.resize(8);
+  unsigned* work = c->err_word.p;
+  SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  ProfScope ps(c->prof, s, "hbuild_rowsort");
+  if (mixed)
+    k_sort_rows<true><<<grid, kSortThreads, smem, s>>>(H.row_ptr.p, H.row_cnt.p, n, H.col.p,
+                                                       nullptr, H.val32.p, H.res32.p, work);
+  else
+    k_sort_rows<false><<<grid, kSortThreads, smem, s>>>(H.row_ptr.p, H.row_cnt.p, n, H.col.p,
+                                                        H.val64.p, nullptr, nullptr, work);
+  SHCI_LAUNCH_CHECK();
+  c->launches += 1;
+}
+
+}  // namespace shci

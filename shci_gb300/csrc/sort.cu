@@ -1,11 +1,11 @@
 // Device-wide exclusive scan and stable LSD radix sort.
 //
 // Radix sort: 8-bit digits, one pass per digit over [begin_bit, end_bit).  Each pass is
-//   (1) per-tile digit histograms (warp-aggregated shared atomics),
+//   (1) per-tile digit histograms (shared atomics),
 //   (2) an exclusive scan of the digit-major [256 x tiles] histogram -> scatter bases,
 //   (3) a stable scatter: each 4096-item tile is walked in 16 rounds of 256 consecutive items;
-//       within a round an item's rank among equal digits comes from __match_any_sync (inside
-//       its warp) plus the per-warp counts of lower warps, so input order is preserved.  The
+//       within a round an item's rank among equal digits comes from ballots (inside its
+//       warp) plus the per-warp counts of lower warps, so input order is preserved.  The
 //       tile is first placed digit-sorted in shared memory and then written out run by run,
 //       so global writes are coalesced.
 // Passes whose digit is constant over all keys are skipped (a pre-pass ORs key differences).
@@ -121,22 +121,37 @@ __global__ void k_radix_hist(const K* keys, size_t n, int shift, uint32_t* hist,
                              unsigned n_tiles) {
   __shared__ uint32_t s_h[256];
   s_h[threadIdx.x] = 0;
-  __syncthreads();
   const size_t t0 = (size_t)blockIdx.x * kSortTile;
-  const unsigned lane = threadIdx.x & 31;
+  // every load of the thread is issued before the first count
+  unsigned d[kSortRounds];
+#pragma unroll
   for (int r = 0; r < kSortRounds; r++) {
     const size_t idx = t0 + (size_t)r * kSortThreads + threadIdx.x;
-    const bool valid = idx < n;
-    const unsigned d = valid ? (unsigned)((keys[idx] >> shift) & 255u) : 256u;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&s_h[d], __popc(peers));
+    d[r] = idx < n ? (unsigned)((keys[idx] >> shift) & 255u) : 256u;
   }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortRounds; r++)
+    if (d[r] < 256u) atomicAdd(&s_h[d[r]], 1u);
   __syncthreads();
   hist[(size_t)threadIdx.x * n_tiles + blockIdx.x] = s_h[threadIdx.x];
 }
 
+// Lanes of the warp holding the same 8-bit digit as this lane (valid lanes only): one ballot
+// per digit bit, which GB300 issues at about twice the rate of __match_any_sync.
+__device__ __forceinline__ unsigned radix_peers(unsigned d, bool valid) {
+  unsigned m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const bool bit = (d >> b) & 1u;
+    const unsigned bb = __ballot_sync(0xffffffffu, valid && bit);
+    m &= bit ? bb : ~bb;
+  }
+  return m;
+}
+
 // Stable scatter of one tile.  Items are ranked round by round (256 consecutive items per
-// round: rank among equal digits from __match_any_sync inside the warp plus the counts of
+// round: rank among equal digits from ballots inside the warp plus the counts of
 // lower warps and earlier rounds), placed at their digit-sorted position in shared memory,
 // and then written out in that order, so each digit's run of the tile goes to global memory
 // as consecutive addresses (coalesced) instead of one scattered write per item.  offs is the
@@ -182,7 +197,7 @@ __global__ void __launch_bounds__(kSortThreads)
     const bool valid = idx < n;
     const K k = valid ? kin[idx] : K(0);
     const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned peers = radix_peers(d, valid);
     const unsigned rank = __popc(peers & ((1u << lane) - 1u));
     if (valid && rank == 0) s_wcnt[warp][d] = __popc(peers);
     __syncthreads();

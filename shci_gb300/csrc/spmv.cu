@@ -33,13 +33,12 @@ namespace shci {
 
 namespace {
 
-template <int MODE>  // 0: FP64 values, 1: FP32 values, 2: FP32 value + FP32 residual
+// FP64 store: FP64 products, FP64 atomics.
 __global__ void __launch_bounds__(256)
     k_spmv(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
-           const uint32_t* __restrict__ col,
-           const double* __restrict__ v64, const float* __restrict__ v32,
-           const float* __restrict__ r32, const double* __restrict__ diag,
-           const double* __restrict__ x, double* __restrict__ y, uint32_t n) {
+           const uint32_t* __restrict__ col, const double* __restrict__ v64,
+           const double* __restrict__ diag, const double* __restrict__ x, double* __restrict__ y,
+           uint32_t n) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
@@ -48,10 +47,7 @@ __global__ void __launch_bounds__(256)
     double acc = 0.0;
     for (uint64_t k = rs + lane; k < re; k += 32) {
       const uint32_t j = col[k];
-      double v;
-      if (MODE == 0) v = v64[k];
-      else if (MODE == 1) v = static_cast<double>(v32[k]);
-      else v = static_cast<double>(v32[k]) + static_cast<double>(r32[k]);
+      const double v = v64[k];
       acc += v * x[j];
       atomicAdd(&y[j], v * xi);
     }
@@ -265,8 +261,7 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   if (H.precision == SHCI_PREC_FP64) {
     ProfScope ps(c->prof, s, "spmv");
     SHCI_CUDA(cudaMemsetAsync(y, 0, H.n * sizeof(double), s));
-    k_spmv<0><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val64.p, nullptr, nullptr, H.diag.p,
-                                   x, y, n);
+    k_spmv<<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val64.p, H.diag.p, x, y, n);
     SHCI_LAUNCH_CHECK();
     c->launches += 1;
     return;

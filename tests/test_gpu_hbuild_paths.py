@@ -59,3 +59,69 @@ def test_join_scan_and_collisions_agree(monkeypatch, c_dets):
         assert np.array_equal(other[3], s_join[3])
         for (ca, va), (cb, vb) in zip(s_join[2], other[2]):
             assert np.array_equal(ca, cb) and np.array_equal(va, vb)
+
+
+
+@pytest.fixture(scope="module")
+def long_rows(oracle_mod, tmp_path_factory):
+    """n = 26 7a7b synthetic integrals: 15,609 dets after the 1e-3 and 5e-4 selections (rows
+    up to 8,597 elements) and more than 2^16 after 2e-4 and 1e-4 (tiles whose columns span
+    more than 2^16 dets, so the sort's bins hold several columns)."""
+    from shci_gb300 import synthetic
+    path = synthetic.workload_fcidump(2, str(tmp_path_factory.mktemp("w2")))
+    o = oracle_mod.Oracle(path, 7, 7)
+    out = []
+    for eps in (1e-3, 5e-4, 2e-4, 1e-4):
+        o.run_variation_step(eps, False, 5e-5)
+        if eps in (5e-4, 1e-4):
+            out.append(o.dets())
+    return path, out
+
+
+def _raw_rows(monkeypatch, path, dets, env, precision):
+    import shci_gb300
+    for k in ("SHCI_HBUILD", "SHCI_JOIN_BITS", "SHCI_ROW_SORT"):
+        monkeypatch.delenv(k, raising=False)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    c = shci_gb300.Context()
+    c.load_fcidump(path, 7, 7)
+    up, dn, coefs = dets
+    c.set_dets(up, dn, coefs)
+    nnz, _ = c.update_hamiltonian(precision)
+    rp, cols, vals, _ = c.hamiltonian(nnz)
+    return rp, cols, vals
+
+
+@pytest.mark.parametrize("path", ["", "join2", "scan"])
+def test_rows_in_column_order(monkeypatch, long_rows, path):
+    """Every build path leaves each row in strictly increasing column order, tile by tile
+    (2048 elements; rows and tail tiles of 32 or fewer elements fill one H*v chunk and are
+    left as built), with the same elements per tile as the build with the pass turned off."""
+    import shci_gb300
+    fcidump, cases = long_rows
+    env = {"SHCI_HBUILD": path} if path else {}
+    for dets in cases:
+        n = len(dets[0])
+        for prec in (shci_gb300.PREC_FP64, shci_gb300.PREC_MIXED):
+            rp, cols, vals = _raw_rows(monkeypatch, fcidump, dets, env, prec)
+            rp0, cols0, vals0 = _raw_rows(monkeypatch, fcidump, dets,
+                                          dict(env, SHCI_ROW_SORT="0"), prec)
+            assert np.array_equal(rp, rp0)
+            lengths = np.diff(rp.astype(np.int64))
+            row = np.repeat(np.arange(n), lengths)
+            pos = np.arange(len(cols)) - rp[:-1].astype(np.int64)[row]
+            tile = row.astype(np.int64) * (1 << 20) + pos // 2048
+            tile_len = np.minimum(2048, lengths[row] - (pos // 2048) * 2048)
+            sorted_tile = tile_len > 32
+            same_tile = (tile[1:] == tile[:-1]) & sorted_tile[1:]
+            assert np.all(np.diff(cols.astype(np.int64))[same_tile] > 0), (n, prec)
+            g0 = cols0.astype(np.int64)
+            assert np.any(np.diff(g0)[same_tile] < 0)  # the switch does turn the pass off
+            # the sorted build is the unsorted build's tiles in column order
+            o = np.lexsort((np.where(sorted_tile, g0, 0), tile))
+            assert np.array_equal(cols, cols0[o]) and np.array_equal(vals, vals0[o])
+        if n < 65536:
+            assert lengths.max() > 2048  # rows span several tiles
+        else:
+            assert lengths.max() > 2048 and n > 65536
