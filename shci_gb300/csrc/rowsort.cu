@@ -11,15 +11,17 @@
 // inside a row changes: connection lists and values are the same (the reference's
 // SparseMatrix rows carry no order beyond the diagonal first, src/solver/sparse_matrix.h).
 //
-// A CTA takes one row at a time (work counter) and sorts its elements in tiles of kTile,
-// fully by column, with few shared-memory accesses per element (random shared accesses
-// bound this pass).  Each thread holds kPer elements in registers.  A 65,536-bin bitmap
+// A CTA takes one row at a time (work counter; the next row is taken early and its first
+// tile prefetched into L2 while the current one is sorted) and sorts its elements in tiles
+// of kTile, fully by column, with few shared-memory accesses per element (random shared
+// accesses bound this pass).  Each thread holds kPer elements in registers.  A 65,536-bin bitmap
 // over the tile's column range [jmin, jmax] (bin width 2^s, the smallest that covers the
 // range) marks the occupied bins; prefix popcounts give each occupied bin a dense id; one
 // shared atomic per element counts its bin and returns its arrival index; the counts are
 // scanned into bin starts.  Columns are unique within a row, so an element alone in its bin
 // has its final slot (the bin start); the elements of a bin holding several (nearby
-// columns, at most 2^s) are ranked by counting the smaller columns of the bin.  Each element
+// columns, at most 2^s) are ranked by the popcount of a mask of the bin's columns below
+// their own (bins of up to 128 columns) or by counting the smaller columns of the bin.  Each element
 // is stored once at its final slot and the tile goes back to global memory coalesced.  The
 // outcome does not depend on the order of the atomics: every tile ends up in strictly
 // increasing column order.
@@ -35,32 +37,39 @@ namespace shci {
 namespace {
 
 constexpr int kTile = 2048;          // elements per sorted tile
-constexpr int kSortWarps = 8;
+constexpr int kSortWarps = 16;
 constexpr int kSortThreads = kSortWarps * 32;
 constexpr int kBinWords = 2048;      // 65,536-bin bitmap
 constexpr int kPer = kTile / kSortThreads;
 static_assert(kBinWords == kTile && kPer * kSortThreads == kTile, "one scan layout for both");
 
 struct SortSmem {
-  uint32_t bm[kBinWords];   // occupied bins
-  uint32_t pre[kBinWords];  // occupied bins before each bitmap word; then bin members' columns
+  // aux[0, kBinWords): occupied bins; aux[kBinWords, 2 kBinWords): occupied bins before each
+  // bitmap word.  Once every element has its dense bin id, aux holds the column masks of the
+  // bins with several elements (or, for bins wider than 128 columns, their columns).
+  uint32_t aux[2 * kBinWords];
   uint32_t cnt[kTile];      // per dense bin: count, then start
   uint32_t ocol[kTile];     // the tile in column order
   uint64_t oval[kTile];     // FP64 value, or FP32 value (low word) + FP32 residual (high word)
-  uint32_t wsum[kSortWarps];
-  uint32_t jmin, jmax, row;
+  uint32_t wsum[kSortWarps], wlo[kSortWarps], whi[kSortWarps];
+  uint32_t row, next;
 };
 
-// Block-wide exclusive scan of a[0, m) in place, m <= kTile (kPer consecutive entries per
-// thread; threads past m contribute nothing).
-__device__ void scan_in_place(SortSmem& S, uint32_t* a, int m) {
+enum ScanMode { kScanPack, kScanPopc };
+
+// Block-wide exclusive scan into dst[0, m), m <= kTile (kPer consecutive entries per thread;
+// threads past m contribute nothing).  kScanPack: in place (src == dst), keeping each count
+// in the low 16 bits (dst[i] = start << 16 | count).  kScanPopc: of the popcounts of src.
+template <ScanMode MODE>
+__device__ void block_scan(SortSmem& S, const uint32_t* src, uint32_t* dst, int m) {
   const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int base = threadIdx.x * kPer;
   uint32_t v[kPer], tot = 0;
   if (base < m) {
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
-      v[k] = base + k < m ? a[base + k] : 0u;
+      v[k] = base + k < m ? src[base + k] : 0u;
+      if (MODE == kScanPopc) v[k] = __popc(v[k]);
       tot += v[k];
     }
   }
@@ -72,43 +81,51 @@ __device__ void scan_in_place(SortSmem& S, uint32_t* a, int m) {
   }
   if (lane == 31) S.wsum[warp] = inc;
   __syncthreads();
+  // exclusive prefix of the warp totals, by a shuffle scan in every warp
+  const uint32_t w0 = lane < static_cast<unsigned>(kSortWarps) ? S.wsum[lane] : 0u;
+  uint32_t ws = w0;
+#pragma unroll
+  for (int o = 1; o < kSortWarps; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, ws, o);
+    if (lane >= (unsigned)o) ws += t;
+  }
+  const uint32_t before = __shfl_sync(kFull, ws - w0, warp);
   if (base < m) {
-    uint32_t run = inc - tot;
-    for (unsigned w = 0; w < warp; w++) run += S.wsum[w];
+    uint32_t run = inc - tot + before;
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
-      if (base + k < m) a[base + k] = run;
+      if (base + k < m) dst[base + k] = MODE == kScanPack ? (run << 16) | v[k] : run;
       run += v[k];
     }
   }
   __syncthreads();
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 template <bool MIXED>
-__global__ void __launch_bounds__(kSortThreads, 3)
+__global__ void __launch_bounds__(kSortThreads, 2)
     k_sort_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
                 uint32_t n, uint32_t* col, double* v64, float* v32, float* r32, unsigned* work) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SortSmem& S = *reinterpret_cast<SortSmem*>(smem_raw);
   const unsigned lane = threadIdx.x & 31;
-  while (true) {
-    if (threadIdx.x == 0) S.row = atomicAdd(work, 1u);
+  if (threadIdx.x == 0) S.row = atomicAdd(work, 1u);
+  __syncthreads();
+  uint32_t i = S.row;
+  while (i < n) {
+    // the next row is taken now so that its first tile can be prefetched into L2
+    if (threadIdx.x == 0) S.next = atomicAdd(work, 1u);
     __syncthreads();
-    const uint32_t i = S.row;
-    __syncthreads();
-    if (i >= n) break;
+    const uint32_t nxt = S.next;
     const uint32_t len = row_len[i];
-    if (len <= 32) continue;  // one chunk: its order does not matter
-    for (uint32_t t0 = 0; t0 < len; t0 += kTile) {
+    // rows of one chunk keep their order (it does not matter to H*v)
+    for (uint32_t t0 = 0; len > 32 && t0 < len; t0 += kTile) {
       const int L = static_cast<int>(min(static_cast<uint32_t>(kTile), len - t0));
       if (L <= 32) break;
       const uint64_t g = row_ptr[i] + t0;
-      constexpr int W = kBinWords;
-      if (threadIdx.x == 0) {
-        S.jmin = 0xffffffffu;
-        S.jmax = 0u;
-      }
-      for (int t = threadIdx.x; t < W; t += kSortThreads) S.bm[t] = 0u;
       for (int t = threadIdx.x; t < L; t += kSortThreads) S.cnt[t] = 0u;
       // all of a thread's loads are issued before any is used
       uint32_t rj[kPer];
@@ -125,6 +142,12 @@ __global__ void __launch_bounds__(kSortThreads, 3)
             rv[k] = static_cast<uint64_t>(__double_as_longlong(v64[g + p]));
         }
       }
+      uint64_t nptr = 0;
+      uint32_t nlen = 0;
+      if (t0 == 0 && nxt < n) {
+        nptr = row_ptr[nxt];
+        nlen = row_len[nxt];
+      }
       uint32_t lo = 0xffffffffu, hi = 0u;
 #pragma unroll
       for (int k = 0; k < kPer; k++)
@@ -137,65 +160,119 @@ __global__ void __launch_bounds__(kSortThreads, 3)
         lo = min(lo, __shfl_xor_sync(kFull, lo, o));
         hi = max(hi, __shfl_xor_sync(kFull, hi, o));
       }
-      __syncthreads();  // bitmap and counts cleared, jmin / jmax reset
       if (lane == 0) {
-        atomicMin(&S.jmin, lo);
-        atomicMax(&S.jmax, hi);
+        S.wlo[threadIdx.x >> 5] = lo;
+        S.whi[threadIdx.x >> 5] = hi;
       }
-      __syncthreads();
-      // bin b = (j - jmin) >> s < 65,536
-      const uint32_t jmin = S.jmin;
-      const uint32_t wide = (S.jmax - jmin) >> 16;
+      __syncthreads();  // counts cleared, warp ranges written
+      lo = lane < static_cast<unsigned>(kSortWarps) ? S.wlo[lane] : 0xffffffffu;
+      hi = lane < static_cast<unsigned>(kSortWarps) ? S.whi[lane] : 0u;
+      // butterfly over all 32 lanes, so that every lane ends with the block range
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+        hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+      }
+      // bin b = (j - jmin) >> s < 65,536; the bitmap covers the bins up to the last one
+      const uint32_t jmin = lo;
+      const uint32_t wide = (hi - jmin) >> 16;
       const int s = wide ? 32 - __clz(wide) : 0;
+      const int W = static_cast<int>(((hi - jmin) >> s) >> 5) + 1;
+      for (int t = threadIdx.x; t < W; t += kSortThreads) S.aux[t] = 0u;
+      __syncthreads();
 #pragma unroll
       for (int k = 0; k < kPer; k++)
         if (threadIdx.x + k * kSortThreads < L) {
           const uint32_t b = (rj[k] - jmin) >> s;
-          atomicOr(&S.bm[b >> 5], 1u << (b & 31));
+          atomicOr(&S.aux[b >> 5], 1u << (b & 31));
         }
+      if (nlen > 32) {
+        // first tile of the next row -> L2 (16 elements per thread, within the row)
+        const uint32_t e = threadIdx.x * 16u;
+        if (e < min(nlen, static_cast<uint32_t>(kTile))) {
+          prefetch_l2(col + nptr + e);
+          if (MIXED) {
+            prefetch_l2(v32 + nptr + e);
+            prefetch_l2(r32 + nptr + e);
+          } else {
+            prefetch_l2(v64 + nptr + e);
+          }
+        }
+      }
       __syncthreads();
-      for (int t = threadIdx.x; t < W; t += kSortThreads) S.pre[t] = __popc(S.bm[t]);
-      __syncthreads();
-      scan_in_place(S, S.pre, W);
-      const uint32_t nb = S.pre[W - 1] + __popc(S.bm[W - 1]);  // occupied bins
+      block_scan<kScanPopc>(S, S.aux, S.aux + kBinWords, W);
+      const uint32_t nb = S.aux[kBinWords + W - 1] + __popc(S.aux[W - 1]);  // occupied bins
       // dense bin id and arrival index of each element
       uint32_t rd[kPer], ra[kPer];
 #pragma unroll
       for (int k = 0; k < kPer; k++)
         if (threadIdx.x + k * kSortThreads < L) {
           const uint32_t b = (rj[k] - jmin) >> s, w = b >> 5;
-          rd[k] = S.pre[w] + __popc(S.bm[w] & ((1u << (b & 31)) - 1u));
+          rd[k] = S.aux[kBinWords + w] + __popc(S.aux[w] & ((1u << (b & 31)) - 1u));
           ra[k] = atomicAdd(&S.cnt[rd[k]], 1u);
         }
       __syncthreads();
-      scan_in_place(S, S.cnt, static_cast<int>(nb));  // bin starts
-      // rd <- bin start, ra <- bin size | slot << 16; members of shared bins list their
-      // columns in pre (free now)
+      block_scan<kScanPack>(S, S.cnt, S.cnt, static_cast<int>(nb));  // bin start << 16 | size
+      // An element alone in its bin goes to the bin start now.  A bin with several elements
+      // spans at most 2^s columns: for s <= 7 its elements set their bits in a 128-bit mask
+      // (4 words of aux at 4 * (start / 2), distinct for bins of two or more) and rank by
+      // popcount; wider bins list their columns in aux and rank by counting.
+      const bool masks = s <= 7;
+      uint32_t multi = 0;  // bit k: element k shares its bin
 #pragma unroll
       for (int k = 0; k < kPer; k++)
         if (threadIdx.x + k * kSortThreads < L) {
-          const uint32_t st = S.cnt[rd[k]];
-          const uint32_t en = rd[k] + 1 < nb ? S.cnt[rd[k] + 1] : static_cast<uint32_t>(L);
-          const uint32_t slot = st + ra[k];
-          if (en - st > 1) S.pre[slot] = rj[k];
-          rd[k] = st;
-          ra[k] = (en - st) | (slot << 16);
-        }
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < kPer; k++)
-        if (threadIdx.x + k * kSortThreads < L) {
-          const uint32_t st = rd[k], m = ra[k] & 0xffffu, slot = ra[k] >> 16;
-          uint32_t rank = 0;
-          // smaller columns of the bin (ties, absent for unique columns, by slot)
-          if (m > 1)
-            for (uint32_t q = st; q < st + m; q++) {
-              const uint32_t jq = S.pre[q];
-              rank += (jq < rj[k]) | ((jq == rj[k]) & (q < slot));
+          const uint32_t e = S.cnt[rd[k]];
+          const uint32_t st = e >> 16, m = e & 0xffffu;
+          if (m == 1) {
+            S.ocol[st] = rj[k];
+            S.oval[st] = rv[k];
+          } else {
+            const uint32_t slot = st + ra[k];
+            if (!masks) {
+              S.aux[slot] = rj[k];
+            } else if (ra[k] == 0) {
+              uint32_t* mk = S.aux + 4 * (st >> 1);
+              mk[0] = mk[1] = mk[2] = mk[3] = 0u;
             }
-          S.ocol[st + rank] = rj[k];
-          S.oval[st + rank] = rv[k];
+            multi |= 1u << k;
+            rd[k] = st;
+            ra[k] = m | (slot << 16);
+          }
         }
+      if (nb < static_cast<uint32_t>(L)) {  // some bin holds several elements
+        __syncthreads();
+        if (masks) {
+#pragma unroll
+          for (int k = 0; k < kPer; k++)
+            if ((multi >> k) & 1u) {
+              const uint32_t off = (rj[k] - jmin) & ((1u << s) - 1u);
+              atomicOr(&S.aux[4 * (rd[k] >> 1) + (off >> 5)], 1u << (off & 31));
+            }
+          __syncthreads();
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++)
+          if ((multi >> k) & 1u) {
+            const uint32_t st = rd[k];
+            uint32_t rank = 0;
+            if (masks) {
+              const uint32_t off = (rj[k] - jmin) & ((1u << s) - 1u);
+              const uint32_t* mk = S.aux + 4 * (st >> 1);
+              for (uint32_t w = 0; w < (off >> 5); w++) rank += __popc(mk[w]);
+              rank += __popc(mk[off >> 5] & ((1u << (off & 31)) - 1u));
+            } else {
+              const uint32_t m = ra[k] & 0xffffu, slot = ra[k] >> 16;
+              // smaller columns of the bin (ties, absent for unique columns, by slot)
+              for (uint32_t q = st; q < st + m; q++) {
+                const uint32_t jq = S.aux[q];
+                rank += (jq < rj[k]) | ((jq == rj[k]) & (q < slot));
+              }
+            }
+            S.ocol[st + rank] = rj[k];
+            S.oval[st + rank] = rv[k];
+          }
+      }
       __syncthreads();
 #pragma unroll
       for (int k = 0; k < kPer; k++) {
@@ -213,6 +290,8 @@ __global__ void __launch_bounds__(kSortThreads, 3)
       }
       __syncthreads();
     }
+    __syncthreads();  // S.next read by every thread before it is replaced
+    i = nxt;
   }
 }
 
