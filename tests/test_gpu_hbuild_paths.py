@@ -125,3 +125,29 @@ def test_rows_in_column_order(monkeypatch, long_rows, path):
             assert lengths.max() > 2048  # rows span several tiles
         else:
             assert lengths.max() > 2048 and n > 65536
+
+
+def test_mixed_store_is_fp32_split_of_fp64(monkeypatch, c_dets):
+    """The mixed store holds hi = float(H) and lo = float(H - hi) of every FP64 element:
+    hi + lo, exact in FP64, equals the same split done here from the FP64 build, element by
+    element."""
+    import shci_gb300
+    rows = {}
+    for prec in (shci_gb300.PREC_FP64, shci_gb300.PREC_MIXED):
+        for k in ("SHCI_HBUILD", "SHCI_JOIN_BITS", "SHCI_ROW_SORT"):
+            monkeypatch.delenv(k, raising=False)
+        c = shci_gb300.Context()
+        c.load_fcidump(C_ATOM, 4, 2, "d2h")
+        up, dn, coefs = c_dets
+        c.set_dets(up, dn, coefs)
+        nnz, _ = c.update_hamiltonian(prec)
+        rp, cols, vals, _ = c.hamiltonian(nnz)
+        row = np.repeat(np.arange(len(up)), np.diff(rp.astype(np.int64)))
+        o = np.lexsort((cols, row))
+        rows[prec] = (cols[o], vals[o])
+    c64, v64 = rows[shci_gb300.PREC_FP64]
+    cm, vm = rows[shci_gb300.PREC_MIXED]
+    assert np.array_equal(c64, cm)
+    hi = v64.astype(np.float32)
+    lo = (v64 - hi.astype(np.float64)).astype(np.float32)
+    assert np.array_equal(vm, hi.astype(np.float64) + lo.astype(np.float64))
