@@ -7,7 +7,7 @@ Workload (the largest configuration of the metric): synthetic FCIDUMP, n = 40 or
 iteration: its selection gives the determinant list (~4.5M dets) the timed step works on.
 
 One step = Hamiltonian<S>::update (two-hole core join index + single fill pass, mixed storage:
-FP32 value + FP32 residual) + one full Davidson::diagonalize call (the reference's maximum of
+FP32 value + FP32 residual, rows then sorted by column) + one full Davidson::diagonalize call (the reference's maximum of
 9 H*v products, tol = 0 so every step does the same work, FP64 vectors, float-pair products
 and 64-bit fixed-point sums in H*v) + the FP64-accurate Rayleigh-quotient correction of the
 Ritz vector.  value = device seconds per step
@@ -368,14 +368,17 @@ def run_ours(args):
     # strings are gathered from the L2-resident det list.  Building the join writes keys and
     # entry ids (4 B keys + 4 B ids per entry), sorts them (4 passes; each reads the keys for
     # the histogram, then reads and writes keys and ids: 20 B/entry) and writes spans and det
-    # ids (read 8 B, write 12 B per entry).  H*v: read the store once (col + FP32 value = 8
-    # B/element), row offsets, x (twice), y read-modify-write and the diagonal.
+    # ids (read 8 B, write 12 B per entry).  Row sort: read and write each stored element
+    # (u32 column + FP32 value + FP32 residual: 24 B) and read each row's offset and length.
+    # H*v: read the store once (col + FP32 value = 8 B/element), row offsets, x (twice), y
+    # read-modify-write and the diagonal.
     alg = {
         "hbuild_count": 16.0 * n + 4 * n + 8 * n + 8.0 * m + 4.0 * cand * (m > 0),
         "hbuild_fill": 16.0 * n + 8 * (n + 1) + 12.0 * nnz + (8.0 * m + 4.0 * cand) * (m > 0),
         "join_keys": 16.0 * n + 8.0 * m,
         "join_sort": 4 * 20.0 * m,
         "join_buckets": 20.0 * m,
+        "hbuild_rowsort": 24.0 * nnz + 12.0 * n,
         "spmv": 8.0 * nnz + 8 * (n + 1) + 4 * n + 16 * n + 16 * n + 8 * n,
     }
     # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
@@ -389,7 +392,7 @@ def run_ours(args):
         g = (b / (ms_l * 1e-3) / 1e9) if b else None
         kernels[k] = {"ms_per_launch": ms_l, "launches": cnt,
                       "gbs": g, "frac": (g / hbm) if g else None}
-        if k.startswith("hbuild"):
+        if k in ("hbuild_count", "hbuild_fill"):
             kernels[k]["candidates_per_s"] = cand / (ms_l * 1e-3)
     dk = kernels[dom]
     roof = {"kernel": dom, "bound": "hbm", "achieved": dk["gbs"], "peak": hbm, "unit": "GB/s",
