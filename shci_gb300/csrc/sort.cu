@@ -3,11 +3,10 @@
 // Radix sort: 8-bit digits, one pass per digit over [begin_bit, end_bit).  Each pass is
 //   (1) per-tile digit histograms (shared atomics),
 //   (2) an exclusive scan of the digit-major [256 x tiles] histogram -> scatter bases,
-//   (3) a stable scatter: each 4096-item tile is walked in 16 rounds of 256 consecutive items;
-//       within a round an item's rank among equal digits comes from ballots (inside its
-//       warp) plus the per-warp counts of lower warps, so input order is preserved.  The
-//       tile is first placed digit-sorted in shared memory and then written out run by run,
-//       so global writes are coalesced.
+//   (3) a stable scatter of each 4096-item tile: every warp holds 512 consecutive items in
+//       registers, counts their digits, and after one scan over (digit, warp) places them
+//       chunk by chunk (ranks of equal digits from ballots) into a digit-sorted copy of the
+//       tile in shared memory, written out run by run so global writes are coalesced.
 // Passes whose digit is constant over all keys are skipped (a pre-pass ORs key differences).
 // Keys are 32 or 64 bit, values 32 or 64 bit.
 #include "sort.cuh"
@@ -150,69 +149,87 @@ __device__ __forceinline__ unsigned radix_peers(unsigned d, bool valid) {
   return m;
 }
 
-// Stable scatter of one tile.  Items are ranked round by round (256 consecutive items per
-// round: rank among equal digits from ballots inside the warp plus the counts of
-// lower warps and earlier rounds), placed at their digit-sorted position in shared memory,
-// and then written out in that order, so each digit's run of the tile goes to global memory
-// as consecutive addresses (coalesced) instead of one scattered write per item.  offs is the
-// exclusively scanned digit-major histogram with the total appended, so the tile's count of
-// digit d is offs[d * n_tiles + tile + 1] - offs[d * n_tiles + tile].
+// Stable scatter of one tile.  Warp w owns the tile's items [512 w, 512 w + 512) and holds
+// them in registers (16 chunks of 32 consecutive items).  Each warp counts its digits into
+// its own shared counters; one scan over (digit, warp) turns the counts into offsets, so
+// warp w's items of digit d follow those of lower warps; the warp then places its chunks in
+// order, ranking equal digits of a chunk with ballots, into a digit-sorted copy of the tile
+// in shared memory, which goes to global memory run by run (coalesced) at the digit's
+// global offset.  offs is the exclusively scanned digit-major histogram with the total
+// appended, so the tile's count of digit d is offs[d * n_tiles + tile + 1] - offs[d *
+// n_tiles + tile].
 template <class K, class V>
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const K* __restrict__ kin, const V* __restrict__ vin, K* __restrict__ kout,
                     V* __restrict__ vout, size_t n, int shift, const uint32_t* __restrict__ offs,
                     unsigned n_tiles) {
+  constexpr int kW = kSortThreads / 32;
+  constexpr int kC = kSortTile / kSortThreads;  // chunks of 32 items per warp
   extern __shared__ __align__(16) unsigned char s_raw[];
   K* s_k = reinterpret_cast<K*>(s_raw);
   V* s_v = reinterpret_cast<V*>(s_raw + sizeof(K) * kSortTile);
-  __shared__ uint32_t s_gbase[256], s_lstart[256], s_run[256];
-  __shared__ uint32_t s_wcnt[kSortThreads / 32][256];
-  __shared__ uint32_t s_scan[kSortThreads / 32];
+  __shared__ uint32_t s_wc[kW][256];
+  __shared__ uint32_t s_gbase[256], s_lstart[256], s_ws[kW];
   const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const unsigned lt = (1u << lane) - 1u;
   const size_t t0 = (size_t)blockIdx.x * kSortTile;
+  const size_t hi = (size_t)tid * n_tiles + blockIdx.x;
+  const uint32_t g0 = offs[hi];
+  const uint32_t tcnt = offs[hi + 1] - g0;
+  s_gbase[tid] = g0;
+#pragma unroll
+  for (int w = 0; w < kW; w++) s_wc[w][tid] = 0;
+  K kk[kC];
+  V vv[kC];
+  const size_t wb = t0 + (size_t)warp * 32 * kC + lane;
+#pragma unroll
+  for (int c = 0; c < kC; c++) {
+    const size_t idx = wb + (size_t)c * 32;
+    kk[c] = idx < n ? kin[idx] : K(0);
+    vv[c] = idx < n ? vin[idx] : V(0);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < kC; c++)
+    if (wb + (size_t)c * 32 < n) atomicAdd(&s_wc[warp][(unsigned)((kk[c] >> shift) & 255u)], 1u);
+  __syncthreads();
   {
-    const size_t hi = (size_t)tid * n_tiles + blockIdx.x;
-    const uint32_t g = offs[hi];
-    const uint32_t cnt = offs[hi + 1] - g;
-    s_gbase[tid] = g;
-    s_run[tid] = 0;
-    // block exclusive scan of the tile's digit counts -> local digit starts
-    uint32_t inc = cnt;
+    // digit d = tid: its start in the tile (exclusive scan of the tile's counts), then the
+    // start of each warp's items of d
+    uint32_t inc = tcnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
       if (lane >= (unsigned)o) inc += t;
     }
-    if (lane == 31) s_scan[warp] = inc;
+    if (lane == 31) s_ws[warp] = inc;
     __syncthreads();
-    uint32_t before = 0;
-    for (unsigned w = 0; w < warp; w++) before += s_scan[w];
-    s_lstart[tid] = before + inc - cnt;
-  }
-  for (int r = 0; r < kSortRounds; r++) {
+    uint32_t run = inc - tcnt;
+    for (unsigned w = 0; w < warp; w++) run += s_ws[w];
+    s_lstart[tid] = run;
 #pragma unroll
-    for (int w = 0; w < kSortThreads / 32; w++) s_wcnt[w][tid] = 0;
-    __syncthreads();
-    const size_t idx = t0 + (size_t)r * kSortThreads + tid;
-    const bool valid = idx < n;
-    const K k = valid ? kin[idx] : K(0);
-    const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
-    const unsigned peers = radix_peers(d, valid);
-    const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-    if (valid && rank == 0) s_wcnt[warp][d] = __popc(peers);
-    __syncthreads();
-    if (valid) {
-      unsigned pre = 0;
-      for (unsigned w = 0; w < warp; w++) pre += s_wcnt[w][d];
-      const unsigned lp = s_lstart[d] + s_run[d] + pre + rank;
-      s_k[lp] = k;
-      s_v[lp] = vin[idx];
+    for (int w = 0; w < kW; w++) {
+      const uint32_t c = s_wc[w][tid];
+      s_wc[w][tid] = run;
+      run += c;
     }
-    __syncthreads();
-    unsigned tot = 0;
+  }
+  __syncthreads();
 #pragma unroll
-    for (int w = 0; w < kSortThreads / 32; w++) tot += s_wcnt[w][tid];
-    s_run[tid] += tot;
+  for (int c = 0; c < kC; c++) {
+    const bool valid = wb + (size_t)c * 32 < n;
+    const unsigned d = valid ? (unsigned)((kk[c] >> shift) & 255u) : 0u;
+    const unsigned pm = radix_peers(d, valid);
+    uint32_t off = 0;
+    if (valid) off = s_wc[warp][d];
+    __syncwarp();
+    if (valid) {
+      const uint32_t pos = off + __popc(pm & lt);
+      s_k[pos] = kk[c];
+      s_v[pos] = vv[c];
+      if ((pm & lt) == 0) s_wc[warp][d] = off + __popc(pm);
+    }
+    __syncwarp();
   }
   __syncthreads();
   const unsigned tile_n = static_cast<unsigned>(n - t0 < (size_t)kSortTile ? n - t0 : kSortTile);
