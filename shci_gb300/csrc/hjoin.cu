@@ -231,6 +231,7 @@ void release_sort_pingpong(shci_ctx* c) {
   c->sort.kalt.release();
   c->sort.kalt32.release();
   c->sort.valt32.release();
+  c->sort.valt64.release();
 }
 
 void sort_keys(DevBuf<uint32_t>& k, DevBuf<uint32_t>& v, size_t m, int bits, shci_ctx* c) {
