@@ -382,10 +382,10 @@ def run_ours(args):
         "spmv": 8.0 * nnz + 8 * (n + 1) + 4 * n + 16 * n + 16 * n + 8 * n,
     }
     # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
-    # one full-size H*v launch of the n=26 workload: 1.2946e9 B for 152,895,046 stored
-    # elements = 8.467 B per element, scaled here by the step's element count (the store is
+    # one full-size H*v launch of the n=26 workload: 1.2964e9 B for 152,895,046 stored
+    # elements = 8.479 B per element, scaled here by the step's element count (the store is
     # read once; x, y and the diagonal stay in L2).
-    measured_traffic = {"spmv": 8.467 * nnz}
+    measured_traffic = {"spmv": 8.479 * nnz}
     kernels = {}
     for k, (ms_l, cnt) in per.items():
         b = alg.get(k)
