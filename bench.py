@@ -10,7 +10,7 @@ One step = Hamiltonian<S>::update (two-hole core join index + single fill pass, 
 FP32 value + FP32 residual, rows then sorted by column) + one full Davidson::diagonalize call (the reference's maximum of
 9 H*v products, tol = 0 so every step does the same work, FP64 vectors, float-pair products
 and 64-bit fixed-point sums in H*v) + the FP64-accurate Rayleigh-quotient correction of the
-Ritz vector.  value = device seconds per step
+Ritz vector (a pass over the FP32 residual store).  value = device seconds per step
 (inputs resident in HBM); e2e = the same through the public API with the det list and start
 vector copied from pinned host memory each step and the energy read back.
 

@@ -60,6 +60,7 @@ void after_integrals(shci_ctx* c) {
   c->dets_dirty = true;
   c->eps_tried.clear();
   c->H.valid = false;
+  c->H.build_id++;
 }
 
 }  // namespace
@@ -249,6 +250,7 @@ shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
     c->dets_dirty = false;
     c->eps_tried.clear();
     c->H.valid = false;
+    c->H.build_id++;
   });
 }
 
@@ -463,12 +465,14 @@ shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
     c->d_coef.resize(n);
     SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, init, n * 8, cudaMemcpyHostToDevice, s));
     H.valid = true;
+    H.build_id++;
     auto r = davidson(c, tol);
     SHCI_CUDA(cudaMemcpyAsync(evec, c->d_coef.p, n * 8, cudaMemcpyDeviceToHost, s));
     SHCI_CUDA(cudaStreamSynchronize(s));
     *eval = r.eval;
     if (converged) *converged = r.converged ? 1 : 0;
-    H.valid = false;       // the context's own Hamiltonian is gone
+    H.valid = false;  // the context's own Hamiltonian is gone
+    H.build_id++;
     c->dets_dirty = true;  // coefficients were overwritten
   });
 }
@@ -481,6 +485,7 @@ shci_status shci_select(shci_ctx* c, double eps_var, int var_sd, size_t* n_new) 
     const size_t k = select_dets(c, eps_var, var_sd != 0);
     if (n_new) *n_new = k;
     c->H.valid = false;
+    c->H.build_id++;
   });
 }
 

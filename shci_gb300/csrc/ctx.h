@@ -60,6 +60,7 @@ struct DevHamiltonian {
                                      // join: core entries, 0, 0
   int precision = SHCI_PREC_FP64;
   bool packed = true;     // rows contiguous (row_ptr[i+1] = row_ptr[i] + row_cnt[i])
+  uint64_t build_id = 0;  // changes whenever the stored matrix does
   DevBuf<uint64_t> row_ptr;   // [n+1] row i = [row_ptr[i], row_ptr[i] + row_cnt[i])
   DevBuf<uint32_t> col;       // [nnz]
   DevBuf<double> val64;       // [nnz]   FP64 storage
@@ -93,6 +94,10 @@ struct Davidson {
   DevBuf<double> v[5], Hv[5], w, Hw;
   DevBuf<double> scal;     // device scalars
   DevBuf<double> partial;  // dot partial sums
+  DevBuf<double> rt;       // residual-store row sums of the FP64 energy correction
+  // w and Hw hold the last Ritz vector and its image under the Hamiltonian of build ritz_h
+  bool ritz = false;
+  uint64_t ritz_h = 0;
 };
 
 }  // namespace shci

@@ -194,9 +194,19 @@ void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs
   }
 }
 
+__global__ void k_vec_differs(const double* __restrict__ a, const double* __restrict__ b, size_t n,
+                              double* flag) {
+  bool d = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    d |= __double_as_longlong(a[i]) != __double_as_longlong(b[i]);
+  if (__any_sync(kFull, d) && (threadIdx.x & 31) == 0) *flag = 1.0;
+}
+
 DavidsonOut davidson(shci_ctx* c, double tol) {
   DavidsonOut out;
   auto& D = c->dav;
+  D.ritz = false;
   const size_t n = c->H.n;
   cudaStream_t s = c->stream;
   const unsigned g = grid_for(n, 256, 152 * 16);
@@ -288,19 +298,47 @@ DavidsonOut davidson(shci_ctx* c, double tol) {
   }
   SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, D.w.p, n * 8, cudaMemcpyDeviceToDevice, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
+  D.ritz = true;
+  D.ritz_h = c->H.build_id;
   out.eval = lambda;
   out.converged = converged;
   c->prof.flush();
   return out;
 }
 
+// Rayleigh quotient of d_coef with value + residual.  When d_coef is still the Ritz vector w
+// of the last Davidson call on this (mixed) Hamiltonian, w^T H w = w^T Hw + w^T R w with Hw =
+// H32 w kept by Davidson (FP32 values, FP64 diagonal), so only the residual store R is read
+// (2 sum_i w_i (R w)_i over its upper triangle: one gather per element, no atomics);
+// otherwise H w is formed from value + residual.
 double rayleigh_fp64(shci_ctx* c) {
   const size_t n = c->H.n;
   auto& D = c->dav;
+  cudaStream_t s = c->stream;
+  Dots dots(c);
+  if (n > 1 && D.ritz && D.ritz_h == c->H.build_id && c->H.precision != SHCI_PREC_FP64 &&
+      D.w.n == n && c->d_coef.n >= n) {
+    D.scal.reserve(8);
+    SHCI_CUDA(cudaMemsetAsync(D.scal.p, 0, 8, s));
+    k_vec_differs<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(c->d_coef.p, D.w.p, n, D.scal.p);
+    SHCI_LAUNCH_CHECK();
+    double differs = 0.0;
+    SHCI_CUDA(cudaMemcpyAsync(&differs, D.scal.p, 8, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    if (differs == 0.0) {
+      D.rt.mt = &c->mem;
+      D.rt.resize(n, 1.1);
+      residual_rows(c, D.w.p, D.rt.p);
+      const double num = dots.dot_host(D.w.p, D.Hw.p, n) + 2.0 * dots.dot_host(D.w.p, D.rt.p, n);
+      const double den = dots.dot_host(D.w.p, D.w.p, n);
+      c->launches += 1;
+      return num / den;
+    }
+  }
+  D.ritz = false;  // Hw is overwritten below
   D.Hw.mt = &c->mem;
   D.Hw.resize(n, 1.1);
   spmv(c, c->d_coef.p, D.Hw.p, true);
-  Dots dots(c);
   const double num = dots.dot_host(c->d_coef.p, D.Hw.p, n);
   const double den = dots.dot_host(c->d_coef.p, c->d_coef.p, n);
   return num / den;

@@ -444,6 +444,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   H.n = n;
   H.precision = precision;
   H.valid = false;
+  H.build_id++;
   H.bound_valid = false;
   const char* force = std::getenv("SHCI_HBUILD");
   const bool scan_only = force && std::strcmp(force, "scan") == 0;
@@ -546,6 +547,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   if (row_sort_enabled()) sort_rows(c);
   c->prof.flush();
   H.valid = true;
+  H.build_id++;
   c->launches += 5;
   return nnz;
 }

@@ -52,6 +52,8 @@ void sort_rows(shci_ctx* c);
 
 // spmv.cu: y = H x (FP64 vectors on the device); residual adds the FP32 residual store.
 void spmv(shci_ctx* c, const double* x, double* y, bool residual);
+// t_i = sum_j R_ij w_j over the stored (upper) elements of the residual store R (mixed H).
+void residual_rows(shci_ctx* c, const double* w, double* t);
 // Mixed H*v needs a bound on the row abs sums: a mixed build sums |H_ij| into H.rowabs
 // (off-diagonal) during its count or single fill pass, and this turns the sums into the bound.
 void finish_mixed_bound(shci_ctx* c);

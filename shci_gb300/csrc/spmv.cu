@@ -248,7 +248,38 @@ void mixed_bound(shci_ctx* c, unsigned grid) {
   finish_mixed_bound(c);
 }
 
+// t_i = sum over row i's stored elements of residual_ij * w_j (FP64; no atomics: the FP64
+// energy correction needs only w^T R w = 2 sum_i w_i t_i of the residual store R).
+__global__ void __launch_bounds__(256)
+    k_res_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
+               const uint32_t* __restrict__ col, const float* __restrict__ r32,
+               const double* __restrict__ w, double* __restrict__ t, uint32_t n) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    const uint64_t rs = row_ptr[i], re = rs + row_len[i];
+    double acc = 0.0;
+    for (uint64_t k = rs + lane; k < re; k += 32) acc += static_cast<double>(r32[k]) * w[col[k]];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if (lane == 0) t[i] = acc;
+  }
+}
+
 }  // namespace
+
+void residual_rows(shci_ctx* c, const double* w, double* t) {
+  auto& H = c->H;
+  if (!H.valid || H.precision == SHCI_PREC_FP64) throw ArgError("no mixed Hamiltonian built");
+  const uint32_t n = static_cast<uint32_t>(H.n);
+  int sms = 0;
+  SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const unsigned grid = grid_for((size_t)n * 32, 256, (unsigned)sms * 8u);
+  ProfScope ps(c->prof, c->stream, "spmv_res_rows");
+  k_res_rows<<<grid, 256, 0, c->stream>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.res32.p, w, t, n);
+  SHCI_LAUNCH_CHECK();
+  c->launches += 1;
+}
 
 void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   auto& H = c->H;

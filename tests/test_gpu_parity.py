@@ -296,3 +296,30 @@ def test_mixed_precision_energy(shci, c_ham):
     ecorr = c.energy_fp64()
     assert abs(e32 - e64) < 1e-6
     assert abs(ecorr - e64) < 1e-8
+
+
+def test_fp64_energy_correction_paths(shci, c_ham):
+    """The FP64 energy of the Ritz vector right after Davidson reads only the residual store
+    (the FP32-value part comes from Davidson's own H*v products); it equals the Rayleigh
+    quotient with value + residual H*v, and any other vector (changed coefficients, a rebuilt
+    matrix) takes the full product."""
+    _, o, _, _, _, up, dn, coefs = c_ham
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.set_dets(up, dn, coefs)
+    c.update_hamiltonian(shci.PREC_MIXED)
+    c.davidson(1e-10)
+    w = c.dets()[2]
+    e_ritz = c.energy_fp64()
+    y = c.hv(w, True)
+    e_full = float(w @ y) / float(w @ w)
+    assert abs(e_ritz - e_full) <= 1e-13 * abs(e_full)
+    assert abs(e_ritz - float(w @ o.hv(w)) / float(w @ w)) <= 1e-12 * abs(e_full)
+    assert c.energy_fp64() == e_ritz  # repeatable
+    w2 = w + 1e-3 * np.random.default_rng(11).standard_normal(len(w))
+    c.set_coefs(w2)
+    e2 = c.energy_fp64()
+    y2 = o.hv(w2)
+    assert abs(e2 - float(w2 @ y2) / float(w2 @ w2)) <= 1e-12 * abs(e2)
+    c.set_coefs(w)
+    c.update_hamiltonian(shci.PREC_MIXED)  # same matrix, new build: full product
+    assert abs(c.energy_fp64() - e_full) <= 1e-12 * abs(e_full)
