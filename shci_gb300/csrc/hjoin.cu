@@ -133,8 +133,10 @@ struct JoinView {
 // Row kernel of the join (MODE as in RowSink).  A warp per row: lanes take the row's entries
 // 32 at a time, the members after each entry are flattened over the lanes, and every member
 // that passes the canonical-core test goes to the row's queues.
+// Five CTAs per SM (48 registers, a few spilled): 144 ms for the n = 40 fill against 151 ms
+// at the register-limited four (64 registers) and 156 ms at six (40 registers).
 template <int MODE>
-__global__ void __launch_bounds__(kJoinWarps * 32)
+__global__ void __launch_bounds__(kJoinWarps * 32, 5)
     k_hjoin(DevIntegrals I, const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
             uint32_t n, JoinView jv, uint32_t* row_cnt, const uint64_t* row_ptr, uint32_t* col,
             double* v64, float* v32, float* r32, unsigned* work, float* absacc) {
