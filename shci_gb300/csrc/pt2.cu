@@ -35,7 +35,8 @@ namespace shci {
 
 namespace {
 
-constexpr int kPtWarps = 8;
+constexpr int kPtWarps = 8;  // 8 warps per CTA; the walks are capped at 64 registers for
+                              // four CTAs per SM (PT2 1.29 -> 1.26 s at n = 40)
 enum : int { kDtm = 0, kPsto = 1, kSto = 2 };
 
 struct PtParams {
@@ -142,7 +143,7 @@ __device__ __forceinline__ uint64_t src_batch(const PtParams& Q, const StoSource
 
 // Output slots of each source: its candidates in the current batch.
 template <int MODE>
-__global__ void __launch_bounds__(kPtWarps * 32)
+__global__ void __launch_bounds__(kPtWarps * 32, 4)
     k_pt_count(SelParams P, PtParams Q, StoSources S, uint32_t n_src, uint64_t* cnt_out) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t wpg = gridDim.x * kPtWarps;
@@ -194,7 +195,7 @@ struct PtQueue {
 // batches): when the members do not fit, the whole region is written invalid and
 // overflow[k] is set, and the caller emits that source again with an exact count.
 template <int MODE>
-__global__ void __launch_bounds__(kPtWarps * 32)
+__global__ void __launch_bounds__(kPtWarps * 32, 4)
     k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
               const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out,
               uint8_t* overflow) {

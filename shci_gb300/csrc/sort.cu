@@ -158,8 +158,10 @@ __device__ __forceinline__ unsigned radix_peers(unsigned d, bool valid) {
 // global offset.  offs is the exclusively scanned digit-major histogram with the total
 // appended, so the tile's count of digit d is offs[d * n_tiles + tile + 1] - offs[d *
 // n_tiles + tile].
+// Three CTAs per SM (an 80-register cap) for items of up to 12 bytes: 4.5 against 5.5 ms for
+// a pass over 851M u32 pairs; 16-byte items keep two (the cap made them slower).
 template <class K, class V>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, sizeof(K) + sizeof(V) > 12 ? 2 : 3)
     k_radix_scatter(const K* __restrict__ kin, const V* __restrict__ vin, K* __restrict__ kout,
                     V* __restrict__ vout, size_t n, int shift, const uint32_t* __restrict__ offs,
                     unsigned n_tiles) {
