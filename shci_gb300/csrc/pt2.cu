@@ -804,14 +804,26 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     std::vector<uint8_t> h_dtm;
     {
       HostScope hs(c->prof, "pt2_host_sample");
+      const size_t n_draw = n_dets_in_sample - n_dtm;
+      std::vector<size_t> r1s(n_draw);
+      std::vector<double> r2s(n_draw);
+      std::vector<uint32_t> ids(n_draw);
       for (uint32_t it = 0; it < n_it; it++) {
         // sample counts per det, and the dets in order of first draw (the reference's
-        // unordered_map counts and insertion-ordered list); cnt is cleared after use
+        // unordered_map counts and insertion-ordered list); cnt is cleared after use.
+        // The draws come first, in the reference's order; the alias lookups, independent of
+        // one another, then run as one loop whose cache misses overlap.
+        for (size_t k = 0; k < n_draw; k++) {
+          r1s[k] = ui_var(gen);
+          r2s[k] = ur(gen);
+        }
+        for (size_t k = 0; k < n_draw; k++) {
+          const size_t r1 = r1s[k];
+          ids[k] = static_cast<uint32_t>(r2s[k] < aprob[r1] ? r1 : alias[r1]);
+        }
         std::vector<size_t> list;
-        for (size_t k = 0; k < n_dets_in_sample - n_dtm; k++) {
-          const size_t r1 = ui_var(gen);
-          const double r2 = ur(gen);
-          const size_t id = r2 < aprob[r1] ? r1 : alias[r1];
+        for (size_t k = 0; k < n_draw; k++) {
+          const uint32_t id = ids[k];
           if (cnt[id]++ == 0) list.push_back(id);
         }
         const size_t batch_id = ui_batch(gen);
