@@ -371,6 +371,8 @@ def run_ours(args):
     # the histogram, then reads and writes keys and ids: 20 B/entry) and writes spans and det
     # ids (read 8 B, write 12 B per entry).  Row sort: read and write each stored element
     # (u32 column + FP32 value + FP32 residual: 24 B) and read each row's offset and length.
+    # Energy correction: read the store's columns and residuals once (8 B/element), row
+    # offsets and lengths, the Ritz vector, and write the row sums.
     # H*v: read the store once (col + FP32 value = 8 B/element), row offsets, x (twice), y
     # read-modify-write and the diagonal.
     alg = {
@@ -380,6 +382,7 @@ def run_ours(args):
         "join_sort": 4 * 20.0 * m,
         "join_buckets": 20.0 * m,
         "hbuild_rowsort": 24.0 * nnz + 12.0 * n,
+        "spmv_res_rows": 8.0 * nnz + 12.0 * n + 8.0 * n + 8.0 * n,
         "spmv": 8.0 * nnz + 8 * (n + 1) + 4 * n + 16 * n + 16 * n + 8 * n,
     }
     # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
