@@ -108,7 +108,8 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 template <bool MIXED>
 __global__ void __launch_bounds__(kSortThreads, 2)
     k_sort_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
-                uint32_t n, uint32_t* col, double* v64, float* v32, float* r32, unsigned* work) {
+                uint32_t n, uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
+                int mask_max_s) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SortSmem& S = *reinterpret_cast<SortSmem*>(smem_raw);
   const unsigned lane = threadIdx.x & 31;
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       // spans at most 2^s columns: for s <= 7 its elements set their bits in a 128-bit mask
       // (4 words of aux at 4 * (start / 2), distinct for bins of two or more) and rank by
       // popcount; wider bins list their columns in aux and rank by counting.
-      const bool masks = s <= 7;
+      const bool masks = s <= mask_max_s;
       uint32_t multi = 0;  // bit k: element k shares its bin
 #pragma unroll
       for (int k = 0; k < kPer; k++)
@@ -297,6 +298,9 @@ __global__ void __launch_bounds__(kSortThreads, 2)
 
 }  // namespace
 
+// SHCI_ROW_SORT=0 turns the pass off; SHCI_ROW_SORT=loop ranks every shared bin by counting
+// (the path of bins wider than 128 columns, which only tiles spanning more than 2^23 dets
+// need), so that tests can exercise it on small systems.
 bool row_sort_enabled() {
   const char* e = std::getenv("SHCI_ROW_SORT");
   return !(e && std::strcmp(e, "0") == 0);
@@ -327,13 +331,17 @@ void sort_rows(shci_ctx* c) {
   c->err_word.resize(8);
   unsigned* work = c->err_word.p;
   SHCI_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  const char* e = std::getenv("SHCI_ROW_SORT");
+  const int mask_max_s = e && std::strcmp(e, "loop") == 0 ? -1 : 7;  // 128-bit column masks
   ProfScope ps(c->prof, s, "hbuild_rowsort");
   if (mixed)
     k_sort_rows<true><<<grid, kSortThreads, smem, s>>>(H.row_ptr.p, H.row_cnt.p, n, H.col.p,
-                                                       nullptr, H.val32.p, H.res32.p, work);
+                                                       nullptr, H.val32.p, H.res32.p, work,
+                                                       mask_max_s);
   else
     k_sort_rows<false><<<grid, kSortThreads, smem, s>>>(H.row_ptr.p, H.row_cnt.p, n, H.col.p,
-                                                        H.val64.p, nullptr, nullptr, work);
+                                                        H.val64.p, nullptr, nullptr, work,
+                                                        mask_max_s);
   SHCI_LAUNCH_CHECK();
   c->launches += 1;
 }

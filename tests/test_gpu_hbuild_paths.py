@@ -93,20 +93,21 @@ def _raw_rows(monkeypatch, path, dets, env, precision):
     return rp, cols, vals
 
 
-@pytest.mark.parametrize("path", ["", "join2", "scan"])
+@pytest.mark.parametrize("path", ["", "join2", "scan", "loop"])
 def test_rows_in_column_order(monkeypatch, long_rows, path):
     """Every build path leaves each row in strictly increasing column order, tile by tile
     (2048 elements; rows and tail tiles of 32 or fewer elements fill one H*v chunk and are
     left as built), with the same elements per tile as the build with the pass turned off."""
     import shci_gb300
     fcidump, cases = long_rows
-    env = {"SHCI_HBUILD": path} if path else {}
+    # "loop": the default build, with every shared bin of the sort ranked by counting
+    env = {"SHCI_ROW_SORT": "loop"} if path == "loop" else ({"SHCI_HBUILD": path} if path else {})
     for dets in cases:
         n = len(dets[0])
         for prec in (shci_gb300.PREC_FP64, shci_gb300.PREC_MIXED):
             rp, cols, vals = _raw_rows(monkeypatch, fcidump, dets, env, prec)
             rp0, cols0, vals0 = _raw_rows(monkeypatch, fcidump, dets,
-                                          dict(env, SHCI_ROW_SORT="0"), prec)
+                                          dict(env, SHCI_ROW_SORT="0"), prec)  # unsorted
             assert np.array_equal(rp, rp0)
             lengths = np.diff(rp.astype(np.int64))
             row = np.repeat(np.arange(n), lengths)
