@@ -248,21 +248,37 @@ void mixed_bound(shci_ctx* c, unsigned grid) {
   finish_mixed_bound(c);
 }
 
-// t_i = sum over row i's stored elements of residual_ij * w_j (FP64; no atomics: the FP64
-// energy correction needs only w^T R w = 2 sum_i w_i t_i of the residual store R).
+// t_i = sum over row i's stored elements of residual_ij * w_j (no atomics: the FP64 energy
+// correction needs only w^T R w = 2 sum_i w_i t_i of the residual store R).  w comes split
+// into float pairs and the products and sums are float pairs, as in the mixed H*v (about
+// 2^-44 relative): the FP64 form spent two FP64 operations per element (conversion and FMA),
+// more than the gathers cost on GB300.
 __global__ void __launch_bounds__(256)
     k_res_rows(const uint64_t* __restrict__ row_ptr, const uint32_t* __restrict__ row_len,
                const uint32_t* __restrict__ col, const float* __restrict__ r32,
-               const double* __restrict__ w, double* __restrict__ t, uint32_t n) {
+               const float2* __restrict__ ws, double* __restrict__ t, uint32_t n) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     const uint64_t rs = row_ptr[i], re = rs + row_len[i];
-    double acc = 0.0;
-    for (uint64_t k = rs + lane; k < re; k += 32) acc += static_cast<double>(r32[k]) * w[col[k]];
+    float ah = 0.0f, al = 0.0f;
+    for (uint64_t k = rs + lane; k < re; k += 32) {
+      const float2 wj = ws[col[k]];
+      float p, e, s2, se;
+      prod2<false>(r32[k], 0.0f, wj.x, wj.y, &p, &e);
+      two_sum(ah, p, &s2, &se);
+      ah = s2;
+      al += se + e;
+    }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    if (lane == 0) t[i] = acc;
+    for (int o = 16; o; o >>= 1) {
+      const float bh = __shfl_xor_sync(kFull, ah, o), bl = __shfl_xor_sync(kFull, al, o);
+      float s2, se;
+      two_sum(ah, bh, &s2, &se);
+      ah = s2;
+      al = al + bl + se;
+    }
+    if (lane == 0) t[i] = static_cast<double>(ah) + static_cast<double>(al);
   }
 }
 
@@ -275,10 +291,17 @@ void residual_rows(shci_ctx* c, const double* w, double* t) {
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   const unsigned grid = grid_for((size_t)n * 32, 256, (unsigned)sms * 8u);
-  ProfScope ps(c->prof, c->stream, "spmv_res_rows");
-  k_res_rows<<<grid, 256, 0, c->stream>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.res32.p, w, t, n);
+  cudaStream_t s = c->stream;
+  ProfScope ps(c->prof, s, "spmv_res_rows");
+  H.xs.resize(2 * (size_t)n, 1.1);
+  float2* ws = reinterpret_cast<float2*>(H.xs.p);
+  SHCI_CUDA(cudaMemsetAsync(H.scal.p + 1, 0, 8, s));
+  k_split_x<<<grid_for(n, 256), 256, 0, s>>>(w, n, ws,
+                                             reinterpret_cast<unsigned long long*>(H.scal.p + 1));
   SHCI_LAUNCH_CHECK();
-  c->launches += 1;
+  k_res_rows<<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.res32.p, ws, t, n);
+  SHCI_LAUNCH_CHECK();
+  c->launches += 2;
 }
 
 void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
