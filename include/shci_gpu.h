@@ -206,6 +206,11 @@ shci_status shci_profile_get(shci_ctx* ctx, char* names, double* total_ms, uint6
 shci_status shci_pt2_dtm(shci_ctx* ctx, double energy_var, double eps_pt_dtm, size_t n_batches,
                          double* correction, double* uncert, size_t* n_pt_dets);
 
+/* The PT2 stages' map-reduce (Solver<S>::mapreduce_sum, solver.h:1155-1177): out[0] = sum of
+ * x[k], out[1] = sum of x[k]^2 over k < n (host x), in the fixed-order, compensated
+ * (double-double) reduction the PT2 stages use for their per-det contributions. */
+shci_status shci_mapreduce_sum(shci_ctx* ctx, const double* x, size_t n, double* out);
+
 /* Pseudo-stochastic stage (Solver<S>::get_energy_pt_psto, solver.h:766-896): batches of the
  * PT space between eps_pt_psto and eps_pt_dtm with the reference's batch extrapolation,
  * uncertainty and early stop (uncert <= target_error / 2, or eps_pt_psto <= eps_pt and

@@ -20,11 +20,17 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
+def reference_dir():
+    """The reference checkout: $SHCI_REFERENCE, else /root/reference (may be absent)."""
+    return os.environ.get("SHCI_REFERENCE", "/root/reference")
+
+
 def build(ref=True):
     """Compile the oracle (and, when the reference tree is present, the reference pin)."""
     subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
-    if ref and os.path.isdir("/root/reference/src"):
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    r = reference_dir()
+    if ref and os.path.isdir(os.path.join(r, "src")):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "REF=" + r], check=True)
 
 
 _lib = None

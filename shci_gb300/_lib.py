@@ -74,6 +74,7 @@ def load():
         "shci_hamiltonian_stats": [vp, _u64p],
         "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
         "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, P(d), P(d), P(sz), _f64p, sz],
+        "shci_mapreduce_sum": [vp, _f64p, sz, _f64p],
         "shci_rdm1": [vp, _f64p],
         "shci_rdm2": [vp, _f64p],
         "shci_profile": [vp, i],
@@ -387,6 +388,13 @@ class Context:
                                      psto_uncert, ctypes.byref(v), ctypes.byref(u),
                                      ctypes.byref(n), loops, max_iter))
         return v.value, u.value, loops[: n.value]
+
+    def mapreduce_sum(self, x):
+        """(sum x, sum x^2) by the PT2 stages' compensated device reduction."""
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.zeros(2)
+        self._ck(self.L.shci_mapreduce_sum(self.h, x, len(x), out))
+        return out[0], out[1]
 
     def rdm1(self):
         n = self.n_orbs

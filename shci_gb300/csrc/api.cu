@@ -579,6 +579,28 @@ shci_status shci_pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size
   });
 }
 
+shci_status shci_mapreduce_sum(shci_ctx* c, const double* x, size_t n, double* out) {
+  if (!c || !out || (n && !x)) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    out[0] = out[1] = 0.0;
+    if (n == 0) return;
+    cudaStream_t s = c->stream;
+    DevBuf<double> dx, res;
+    DevBuf<uint64_t> starts;
+    dx.mt = res.mt = &c->mem;
+    starts.mt = &c->mem;
+    dx.resize(n);
+    res.resize(2);
+    starts.resize(2);
+    const uint64_t st[2] = {0, n};
+    SHCI_CUDA(cudaMemcpyAsync(dx.p, x, n * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(starts.p, st, 16, cudaMemcpyHostToDevice, s));
+    seg_reduce2(c, dx.p, starts.p, 1, n, res.p);
+    SHCI_CUDA(cudaMemcpyAsync(out, res.p, 16, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
 shci_status shci_rdm1(shci_ctx* c, double* out) {
   if (!c || !out) return SHCI_ERR_ARG;
   return guard(c, [&]() {

@@ -224,6 +224,41 @@ __host__ __device__ __forceinline__ uint64_t rehash(uint64_t a) {
   return h;
 }
 
+// ---------------------------------------------------------------- compensated sums
+// Double-double accumulator: hi + lo carries the running sum with about 2^-106 relative
+// rounding per step (Knuth's branch-free two-sum, then a renormalising fast two-sum), so a
+// sum of m terms is accurate to about cond * m * 2^-106 instead of m * 2^-53.  No
+// multiplications, so FMA contraction cannot change a result.
+struct Dd {
+  double hi = 0.0, lo = 0.0;
+};
+__host__ __device__ __forceinline__ void two_sum64(double a, double b, double* s, double* e) {
+  const double t = a + b;
+  const double z = t - a;
+  *e = (a - (t - z)) + (b - z);
+  *s = t;
+}
+__host__ __device__ __forceinline__ Dd dd_add(Dd a, Dd b) {
+  double s, e;
+  two_sum64(a.hi, b.hi, &s, &e);
+  e += a.lo + b.lo;
+  Dd r;
+  r.hi = s + e;
+  r.lo = e - (r.hi - s);
+  return r;
+}
+__host__ __device__ __forceinline__ Dd dd_add(Dd a, double b) {
+  Dd t;
+  t.hi = b;
+  return dd_add(a, t);
+}
+__device__ __forceinline__ Dd dd_shfl_xor(Dd a, int o) {
+  Dd r;
+  r.hi = __shfl_xor_sync(kFull, a.hi, o);
+  r.lo = __shfl_xor_sync(kFull, a.lo, o);
+  return r;
+}
+
 // Error word written by kernels (never __trap): host checks it after each launch group.
 enum DevError : unsigned { kDevOk = 0, kDevOverflow = 1, kDevCheck = 2 };
 

@@ -93,6 +93,11 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
                size_t max_iterations, double target_error, double psto_uncert,
                std::vector<double>* loops);
 
+// pt2.cu: out[2g], out[2g+1] = sum and sum of squares of x over segment g = [starts[g],
+// starts[g+1]) (device arrays; m = total length), compensated and in a fixed order.
+void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t nseg, size_t m,
+                 double* out);
+
 // rdm.cu
 void rdm1(shci_ctx* c, double* out);       // host [n*n]
 void rdm2(shci_ctx* c, double* out_half);  // host [n^2 (n^2+1) / 2]

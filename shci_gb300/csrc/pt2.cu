@@ -309,17 +309,20 @@ __global__ void k_pt_x(DevIntegrals I, const uint64_t* au, const uint64_t* ad, O
   }
 }
 
-// Sums of x and x^2 over segments [starts[g], starts[g+1]) in a fixed order: pass 1 reduces
-// chunks of kRedChunk elements of each segment (block (chunk, g)), pass 2 reduces each
-// segment's chunk partials.  Only the chunking fixes the order, so results are reproducible.
+// Sums of x and x^2 over segments [starts[g], starts[g+1]) in a fixed order (the map-reduce of
+// solver.h:1155-1177, whose thread-local FP64 sums this replaces): pass 1 reduces chunks of
+// kRedChunk elements of each segment (block (chunk, g)), pass 2 reduces each segment's chunk
+// partials.  Every partial is a compensated double-double sum (Dd), so the result does not
+// lose accuracy with the number of PT dets (1e8 and more); only the chunking fixes the order,
+// so results are reproducible.
 constexpr uint32_t kRedChunk = 1u << 16;
 
-__device__ __forceinline__ void block_sum2(double* a, double* b) {
-  __shared__ double s1[8], s2[8];
+__device__ __forceinline__ void block_sum2(Dd* a, Dd* b) {
+  __shared__ Dd s1[8], s2[8];
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
-    *a += __shfl_xor_sync(kFull, *a, o);
-    *b += __shfl_xor_sync(kFull, *b, o);
+    *a = dd_add(*a, dd_shfl_xor(*a, o));
+    *b = dd_add(*b, dd_shfl_xor(*b, o));
   }
   if ((threadIdx.x & 31) == 0) {
     s1[threadIdx.x >> 5] = *a;
@@ -327,10 +330,10 @@ __device__ __forceinline__ void block_sum2(double* a, double* b) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double ta = 0.0, tb = 0.0;
+    Dd ta, tb;
     for (int w = 0; w < 8; w++) {
-      ta += s1[w];
-      tb += s2[w];
+      ta = dd_add(ta, s1[w]);
+      tb = dd_add(tb, s2[w]);
     }
     *a = ta;
     *b = tb;
@@ -344,32 +347,49 @@ __global__ void __launch_bounds__(256)
   const uint64_t b0 = starts[g] + (uint64_t)ch * kRedChunk;
   const uint64_t e = starts[g + 1];
   const uint64_t b1 = b0 + kRedChunk < e ? b0 + kRedChunk : e;
-  double a = 0.0, b = 0.0;
+  Dd a, b;
   for (uint64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
-    a += x[k];
-    b += x[k] * x[k];
+    const double v = x[k];
+    a = dd_add(a, v);
+    // v^2 as an exact product pair: hi = v*v rounded, lo = its FMA error
+    const double sq = v * v;
+    Dd t;
+    t.hi = sq;
+    t.lo = fma(v, v, -sq);
+    b = dd_add(b, t);
   }
   block_sum2(&a, &b);
   if (threadIdx.x == 0) {
-    part[2 * ((size_t)g * n_chunks + ch)] = a;
-    part[2 * ((size_t)g * n_chunks + ch) + 1] = b;
+    double* o = part + 4 * ((size_t)g * n_chunks + ch);
+    o[0] = a.hi;
+    o[1] = a.lo;
+    o[2] = b.hi;
+    o[3] = b.lo;
   }
 }
 
 __global__ void __launch_bounds__(256)
     k_seg_final2(const double* __restrict__ part, uint32_t n_chunks, double* out) {
   const uint32_t g = blockIdx.x;
-  double a = 0.0, b = 0.0;
+  Dd a, b;
   for (uint32_t k = threadIdx.x; k < n_chunks; k += blockDim.x) {
-    a += part[2 * ((size_t)g * n_chunks + k)];
-    b += part[2 * ((size_t)g * n_chunks + k) + 1];
+    const double* p = part + 4 * ((size_t)g * n_chunks + k);
+    Dd ta, tb;
+    ta.hi = p[0];
+    ta.lo = p[1];
+    tb.hi = p[2];
+    tb.lo = p[3];
+    a = dd_add(a, ta);
+    b = dd_add(b, tb);
   }
   block_sum2(&a, &b);
   if (threadIdx.x == 0) {
-    out[2 * g] = a;
-    out[2 * g + 1] = b;
+    out[2 * g] = a.hi + a.lo;
+    out[2 * g + 1] = b.hi + b.lo;
   }
 }
+
+}  // namespace
 
 // out[2g], out[2g+1] = sum, sum of squares of x over segment g (total length m).
 void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t nseg, size_t m,
@@ -378,7 +398,7 @@ void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t 
   const uint32_t n_chunks = static_cast<uint32_t>((m + kRedChunk - 1) / kRedChunk) + 1;
   DevBuf<double> part;
   part.mt = &c->mem;
-  part.resize(2 * (size_t)n_chunks * nseg);
+  part.resize(4 * (size_t)n_chunks * nseg);
   k_seg_partial2<<<dim3(n_chunks, nseg), 256, 0, s>>>(x, starts, n_chunks, part.p);
   SHCI_LAUNCH_CHECK();
   k_seg_final2<<<nseg, 256, 0, s>>>(part.p, n_chunks, out);
@@ -386,6 +406,8 @@ void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t 
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->launches += 2;
 }
+
+namespace {
 
 // starts[it] = first k with (au[k] >> shift) >= it, for it = 0..n_it (au sorted ascending)
 __global__ void k_iter_starts(const uint64_t* au, size_t m, int shift, uint32_t n_it,

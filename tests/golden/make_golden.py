@@ -9,6 +9,7 @@ HalfDet unit-test cases (src/det/half_det_test.cc:30-46) are transcribed into hi
 and halfdet_pins.json by reading those files as text.
 
 Usage: python tests/golden/make_golden.py [/path/to/reference]
+(default: $SHCI_REFERENCE, else /root/reference)
 """
 import json
 import os
@@ -106,4 +107,5 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1
+         else os.environ.get("SHCI_REFERENCE", "/root/reference"))

@@ -162,3 +162,22 @@ def test_oracle_pt_batches_partition(oracle_mod, w1_fcidump):
     assert n1 == n4
     assert abs(v1 - v4) < 1e-12
     assert u4 == 0.0
+
+
+def test_oracle_w2_pins(oracle_mod, data_dir):
+    """The oracle's n = 26 (7a7b) run reproduces the committed fixture made by
+    tests/golden/make_w2_pins.py: counts and the det list exactly, energies to 1e-10 Ha."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_w2_pins", os.path.join(GOLDEN, "make_w2_pins.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    pins = json.load(open(os.path.join(GOLDEN, "w2_pins.json")))
+    got = mk.run(data_dir)
+    assert [it["n_dets"] for it in got["iterations"]] == [it["n_dets"] for it in pins["iterations"]]
+    assert [it["nnz"] for it in got["iterations"]] == [it["nnz"] for it in pins["iterations"]]
+    assert got["dets_sha256"] == pins["dets_sha256"]
+    for a, b in zip(got["iterations"], pins["iterations"]):
+        assert abs(a["energy"] - b["energy"]) < 1e-10
+    assert got["pt_dtm"]["n_pt_dets"] == pins["pt_dtm"]["n_pt_dets"]
+    assert abs(got["pt_dtm"]["correction"] - pins["pt_dtm"]["correction"]) < 1e-12
