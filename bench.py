@@ -219,7 +219,7 @@ def run_pt2(ctx, stream, e_var):
             psto = ctx.pt2_psto(e_var, eps_dtm, eps_psto, nb_psto, TARGET_ERROR, eps_pt)
         t[2].record(stream)
         sto, sto_u, loops = ctx.pt2_sto(e_var, eps_psto, eps_pt, nb_sto, n_samples, 347634253,
-                                        100, TARGET_ERROR, psto[1])
+                                        100, TARGET_ERROR, psto[1], semisto=False)
         t[3].record(stream)
         torch.cuda.synchronize()
         prof = ctx.profile_get()

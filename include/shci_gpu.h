@@ -221,18 +221,32 @@ shci_status shci_pt2_psto(shci_ctx* ctx, double energy_var, double eps_pt_dtm,
                           double eps_pt, double* correction, double* uncert, size_t* n_pt_dets,
                           size_t* n_batches_done);
 
-/* Stochastic stage (Solver<S>::get_energy_pt_sto, solver.h:898-1153) with a given sample
- * size: |c_i|-weighted samples drawn on the host with the reference's generator
+/* Stochastic stage (Solver<S>::get_energy_pt_sto, solver.h:898-1153): |c_i|-weighted
+ * samples drawn on the host with the reference's generator
  * (std::default_random_engine(random_seed)) and alias tables, a random hash batch per
  * iteration, the reference's estimator and stopping rules (at most max_iterations).
- * psto_uncert = uncertainty of the preceding psto stage.  semisto must be 0 (see the
- * message returned otherwise).  loops (may be NULL, cap entries) receives each iteration's
- * estimate; out: correction, uncertainty, iterations run. */
+ * n_dets_in_sample = 0 sizes the sample as the reference does when n_dets_in_sample_pt_sto is
+ * unset (solver.h:942-1006): a 1,000-draw pilot counts the PT dets of one hash batch of 128,
+ * and the unique-sample target follows from pt_mem_avail (bytes, shci_pt_mem_avail) and
+ * mem_usage (pt_sto_mem_usage, the reference's default 0.4).  semisto = 1 (the reference's
+ * default semisto_sto) makes the dets above the quantile of the top quarter of that target
+ * deterministic and samples the rest with renormalised weights (solver.h:1009-1036); it needs
+ * n_dets_in_sample = 0 (with a given sample size the reference's quantile heap is empty: the
+ * call returns SHCI_ERR_ARG).  psto_uncert = uncertainty of the preceding psto stage.
+ * loops (may be NULL, cap entries) receives each iteration's estimate; sample_info (may be
+ * NULL) = {n_dets_in_sample used, deterministic dets, unique-sample target}; out: correction,
+ * uncertainty, iterations run. */
 shci_status shci_pt2_sto(shci_ctx* ctx, double energy_var, double eps_pt_psto, double eps_pt,
                          size_t n_batches, size_t n_dets_in_sample, int semisto,
                          unsigned random_seed, size_t max_iterations, double target_error,
-                         double psto_uncert, double* correction, double* uncert,
-                         size_t* n_iterations, double* loops, size_t cap);
+                         double psto_uncert, double pt_mem_avail, double mem_usage,
+                         double* correction, double* uncert, size_t* n_iterations,
+                         size_t* sample_info, double* loops, size_t cap);
+
+/* PT memory of the reference's run_all_perturbations (solver.h:601-611, one process):
+ * mem_total * 0.7 - n_dets * 104 - 32 * (heat-bath queue entries), in bytes (mem_total is the
+ * config's "mem_total", else the machine's memory).  Needs the queues built. */
+shci_status shci_pt_mem_avail(shci_ctx* ctx, double mem_total, double* out);
 
 /* ---- batched small instances ------------------------------------------------------------ */
 

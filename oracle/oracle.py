@@ -81,7 +81,7 @@ def lib():
             "orc_hbuild_sample": (None, [vp, sz, sz, _f64p]),
             "orc_threads": (i, []),
             "orc_pt_psto": (None, [vp, d, d, sz, d, d, _f64p]),
-            "orc_pt_sto": (sz, [vp, d, d, sz, sz, u, sz, d, d, _f64p, _f64p, sz]),
+            "orc_pt_sto": (sz, [vp, d, d, sz, sz, u, sz, d, d, i, d, d, _f64p, _f64p, sz]),
             "orc_rdm1": (None, [vp, _f64p]),
             "orc_rdm2": (None, [vp, _f64p]),
         }
@@ -287,11 +287,20 @@ class Oracle:
         return out[0], out[1], int(out[2]), int(out[3])
 
     def pt_sto(self, eps_psto, eps_pt, n_batches, n_samples, seed=347634253, max_iter=100,
-               target_error=5e-5, psto_uncert=0.0):
-        out = np.zeros(2)
+               target_error=5e-5, psto_uncert=0.0, semisto=False, pt_mem_avail=0.0,
+               mem_usage=0.4, info=None):
+        """n_samples = 0: sample size from the reference's pilot and pt_mem_avail (bytes);
+        semisto: deterministic top quarter.  info (a dict, optional) receives n_samples,
+        n_dtm and n_unique_target."""
+        out = np.zeros(5)
         loops = np.zeros(max_iter)
         n = self.L.orc_pt_sto(self.h, eps_psto, eps_pt, n_batches, n_samples, seed, max_iter,
-                              target_error, psto_uncert, out, loops, max_iter)
+                              target_error, psto_uncert, int(semisto), float(pt_mem_avail),
+                              mem_usage, out, loops, max_iter)
+        if n == (1 << 64) - 1:
+            raise RuntimeError("oracle: semistochastic PT2 needs a sample-size target >= 4")
+        if info is not None:
+            info.update(n_samples=int(out[2]), n_dtm=int(out[3]), n_unique_target=int(out[4]))
         return out[0], out[1], loops[:n]
 
     def rdm1(self):

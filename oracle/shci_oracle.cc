@@ -1368,18 +1368,112 @@ struct Solver {
   }
 
   // ------------------------------------------------ PT2: stochastic stage
-  // src/solver/solver.h:898-1153 with n_dets_in_sample given and semisto_sto = false.
+  // src/solver/solver.h:898-1153.  n_samples == 0: the sample size comes from the 1,000-draw
+  // pilot and the PT memory pt_mem_avail (solver.h:942-1006); semisto: the dets above the
+  // quantile of the top quarter of the unique-sample target are deterministic
+  // (solver.h:1009-1036).  info (may be null) = {n_samples, n_dtm, n_unique_target}.
+  struct StoInfo {
+    size_t n_samples = 0, n_dtm = 0, n_unique_target = 0;
+  };
   PtResult pt_sto(double eps_psto, double eps_pt, size_t n_batches, size_t n_samples,
                   unsigned seed, size_t max_iter, double target_error, double psto_uncert,
-                  std::vector<double>* loops) {
+                  std::vector<double>* loops, bool semisto = false, double pt_mem_avail = 0.0,
+                  double mem_usage = 0.4, StoInfo* info = nullptr) {
     std::unordered_set<Det, DetHasher> vset(sys.dets.begin(), sys.dets.end());
     const size_t n_var = sys.dets.size();
     double sw = 0.0;
     for (size_t i = 0; i < n_var; i++) sw += std::abs(sys.coefs[i]);
-    std::vector<double> probs(n_var);
-    for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(sys.coefs[i]) / sw;
+    std::vector<double> probs(n_var), cum(n_var);
+    for (size_t i = 0; i < n_var; i++) {
+      probs[i] = std::abs(sys.coefs[i]) / sw;
+      cum[i] = i > 0 ? probs[i] + cum[i - 1] : probs[i];
+    }
     std::default_random_engine gen(seed);
     std::uniform_real_distribution<double> ur(0., 1.);
+    size_t n_target = 0;
+    if (n_samples == 0) {
+      // pilot: 1,000 draws by inverse CDF, PT dets of the unique draws in hash batch 0 of 128
+      std::unordered_map<size_t, unsigned> sto;
+      std::vector<size_t> list;
+      for (size_t k = 0; k < 1000; k++) {
+        const double r = ur(gen);
+        const size_t id = std::lower_bound(cum.begin(), cum.end(), r) - cum.begin();
+        if (sto.count(id) == 0) list.push_back(id);
+        sto[id]++;
+      }
+      const int nt = omp_get_max_threads();
+      std::vector<std::unordered_set<Det, DetHasher>> part(nt);
+#pragma omp parallel for schedule(dynamic, 1)
+      for (size_t si = 0; si < list.size(); si++) {
+        auto& m = part[omp_get_thread_num()];
+        const Det& det = sys.dets[list[si]];
+        const double coef = sys.coefs[list[si]];
+        auto handler = [&](const Det& a, int n_excite) {
+          if (vset.count(a)) return;
+          if ((rehash(det_hash(a)) & 127) != 0) return;
+          if (n_excite == 1) {
+            const double hc = sys.hamiltonian_elem(det, a, n_excite) * coef;
+            if (std::abs(hc) < eps_pt) return;
+          }
+          m.insert(a);
+        };
+        sys.find_connected_dets(det, INF / std::abs(coef), eps_pt / std::abs(coef), handler);
+      }
+      std::unordered_set<Det, DetHasher> pts;
+      for (auto& m : part) pts.insert(m.begin(), m.end());
+      const size_t n_pt_batch = pts.size() * 128 / n_batches;
+      const size_t bytes_per_entry = 2 * 16 + 40;  // solver.h:402, 905 (two 64-bit chunks)
+      const size_t cap = n_var / 8 + 1;
+      // a pilot with no PT det gives the reference a division by zero; take the cap
+      n_target = cap;
+      if (n_pt_batch > 0) {
+        const double t = static_cast<double>(static_cast<size_t>(pt_mem_avail)) * mem_usage *
+                         static_cast<double>(list.size()) / static_cast<double>(bytes_per_entry) /
+                         5.0 / static_cast<double>(n_pt_batch);
+        n_target = static_cast<size_t>(t);
+        if (n_target >= cap) n_target = cap;
+      }
+      sto.clear();
+      size_t n_unique = 0;
+      while (n_unique < n_target) {
+        const double r = ur(gen);
+        const size_t id = std::lower_bound(cum.begin(), cum.end(), r) - cum.begin();
+        if (sto.count(id) == 0) n_unique++;
+        n_samples++;
+        sto[id]++;
+      }
+    }
+    std::vector<size_t> dtm_list;
+    if (semisto) {
+      size_t n_heap = n_target / 4;
+      if (n_heap == 0)
+        throw std::runtime_error("semistochastic PT2 needs a sample-size target of at least 4 "
+                                 "(the reference's quantile heap would be empty)");
+      std::priority_queue<double, std::vector<double>, std::greater<double>> heap;
+      for (size_t i = 0; i < n_heap; i++) heap.push(probs[i]);
+      for (size_t i = n_heap; i < n_var; i++)
+        if (heap.top() < probs[i]) {
+          heap.pop();
+          heap.push(probs[i]);
+        }
+      const double C = heap.top();
+      double s2 = 0.0;
+      for (size_t i = 0; i < n_var; i++) {
+        if (probs[i] > C) {
+          probs[i] = 0.;
+          dtm_list.push_back(i);
+        } else {
+          s2 += probs[i];
+        }
+      }
+      for (auto& p : probs) p /= s2;
+    }
+    const size_t n_dtm = dtm_list.size();
+    if (info) {
+      info->n_samples = n_samples;
+      info->n_dtm = n_dtm;
+      info->n_unique_target = n_target;
+    }
     // Vose alias tables (src/util.cc:128-175)
     std::vector<double> ap(n_var), tp(n_var);
     std::vector<size_t> al(n_var, 0);
@@ -1406,14 +1500,14 @@ struct Solver {
     }
     std::uniform_int_distribution<size_t> ui_var(0, n_var - 1);
     std::uniform_int_distribution<size_t> ui_batch(0, n_batches - 1);
-    const double factor = 1. / (n_samples - 1.);
+    const double factor = 1. / (n_samples - n_dtm - 1.);
     PtResult res;
     std::vector<double> lv;
     size_t iteration = 0;
     while (iteration < max_iter) {
-      std::unordered_map<size_t, unsigned> cnt;
-      std::vector<size_t> list;
-      for (size_t k = 0; k < n_samples; k++) {
+      std::unordered_map<size_t, unsigned> cnt;  // stochastic dets only
+      std::vector<size_t> list = dtm_list;       // deterministic dets first
+      for (size_t k = 0; k < n_samples - n_dtm; k++) {
         const size_t r1 = ui_var(gen);
         const double r2 = ur(gen);
         const size_t id = r2 < ap[r1] ? r1 : al[r1];
@@ -1429,8 +1523,9 @@ struct Solver {
         const size_t i = list[si];
         const Det& det = sys.dets[i];
         const double coef = sys.coefs[i];
-        const double count = static_cast<double>(cnt.at(i));
-        const double weight = n_samples * probs[i];
+        const bool is_dtm = si < n_dtm;
+        const double count = is_dtm ? 1. : static_cast<double>(cnt.at(i));
+        const double weight = is_dtm ? 1. : (n_samples - n_dtm) * probs[i];
         auto handler = [&](const Det& a, int n_excite) {
           if (rehash(det_hash(a)) % n_batches != batch_id) return;
           if (vset.count(a)) return;
@@ -1440,13 +1535,15 @@ struct Solver {
           const double x = count * hc / weight;
           v[0] += x;
           if (std::abs(hc) > eps_psto) v[1] += x;
-          const double x2 = count * hc / weight * std::sqrt(factor);
-          if (std::abs(hc) > eps_psto) {
-            v[2] += x2;
-            v[3] += x2;
-          } else {
-            v[2] += x2;
-            v[4] += std::pow(count * hc / weight, 2) * (1. - weight / count + factor);
+          if (!is_dtm) {
+            const double x2 = count * hc / weight * std::sqrt(factor);
+            if (std::abs(hc) > eps_psto) {
+              v[2] += x2;
+              v[3] += x2;
+            } else {
+              v[2] += x2;
+              v[4] += std::pow(count * hc / weight, 2) * (1. - weight / count + factor);
+            }
           }
         };
         sys.find_connected_dets(det, INF / std::abs(coef), eps_pt / std::abs(coef), handler);
@@ -2046,12 +2143,24 @@ void orc_pt_psto(void* h, double eps_dtm, double eps_psto, size_t n_batches, dou
 
 size_t orc_pt_sto(void* h, double eps_psto, double eps_pt, size_t n_batches, size_t n_samples,
                   unsigned seed, size_t max_iter, double target_error, double psto_uncert,
-                  double* out /* value, uncert */, double* loops, size_t cap) {
+                  int semisto, double pt_mem_avail, double mem_usage,
+                  double* out /* value, uncert, n_samples, n_dtm, n_unique_target */,
+                  double* loops, size_t cap) {
   std::vector<double> lv;
-  auto r = S(h).pt_sto(eps_psto, eps_pt, n_batches, n_samples, seed, max_iter, target_error,
-                       psto_uncert, &lv);
+  Solver::StoInfo info;
+  Solver::PtResult r;
+  try {
+    r = S(h).pt_sto(eps_psto, eps_pt, n_batches, n_samples, seed, max_iter, target_error,
+                    psto_uncert, &lv, semisto != 0, pt_mem_avail, mem_usage, &info);
+  } catch (const std::exception&) {
+    out[0] = out[1] = std::nan("");
+    return static_cast<size_t>(-1);
+  }
   out[0] = r.value;
   out[1] = r.uncert;
+  out[2] = static_cast<double>(info.n_samples);
+  out[3] = static_cast<double>(info.n_dtm);
+  out[4] = static_cast<double>(info.n_unique_target);
   for (size_t k = 0; k < lv.size() && k < cap; k++) loops[k] = lv[k];
   return lv.size();
 }

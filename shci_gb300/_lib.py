@@ -73,7 +73,8 @@ def load():
         "shci_pt2_dtm": [vp, d, d, sz, P(d), P(d), P(sz)],
         "shci_hamiltonian_stats": [vp, _u64p],
         "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
-        "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, P(d), P(d), P(sz), _f64p, sz],
+        "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, d, d, P(d), P(d), P(sz), _u64p, _f64p, sz],
+        "shci_pt_mem_avail": [vp, d, P(d)],
         "shci_mapreduce_sum": [vp, _f64p, sz, _f64p],
         "shci_rdm1": [vp, _f64p],
         "shci_rdm2": [vp, _f64p],
@@ -380,14 +381,26 @@ class Context:
         return v.value, u.value, n.value, b.value
 
     def pt2_sto(self, energy_var, eps_pt_psto, eps_pt, n_batches, n_samples, seed=347634253,
-                max_iter=100, target_error=5e-5, psto_uncert=0.0, semisto=False):
+                max_iter=100, target_error=5e-5, psto_uncert=0.0, semisto=False,
+                pt_mem_avail=0.0, mem_usage=0.4, info=None):
+        """n_samples = 0: the reference's pilot sizes the sample from pt_mem_avail (bytes);
+        info (a dict, optional) receives n_samples, n_dtm and n_unique_target."""
         v, u, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
         loops = np.zeros(max_iter)
+        si = np.zeros(3, np.uint64)
         self._ck(self.L.shci_pt2_sto(self.h, energy_var, eps_pt_psto, eps_pt, n_batches,
                                      n_samples, int(semisto), seed, max_iter, target_error,
-                                     psto_uncert, ctypes.byref(v), ctypes.byref(u),
-                                     ctypes.byref(n), loops, max_iter))
+                                     psto_uncert, float(pt_mem_avail), mem_usage,
+                                     ctypes.byref(v), ctypes.byref(u), ctypes.byref(n), si,
+                                     loops, max_iter))
+        if info is not None:
+            info.update(n_samples=int(si[0]), n_dtm=int(si[1]), n_unique_target=int(si[2]))
         return v.value, u.value, loops[: n.value]
+
+    def pt_mem_avail(self, mem_total):
+        out = ctypes.c_double()
+        self._ck(self.L.shci_pt_mem_avail(self.h, float(mem_total), ctypes.byref(out)))
+        return out.value
 
     def mapreduce_sum(self, x):
         """(sum x, sum x^2) by the PT2 stages' compensated device reduction."""

@@ -22,6 +22,8 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "json.h"
 
 using shci_cli::Json;
@@ -46,6 +48,23 @@ std::string fmt(const char* f, ...) {
 
 void ck(shci_ctx* c, shci_status s, const char* what) {
   if (s != SHCI_OK) die(std::string(what) + ": " + shci_last_error(c));
+}
+
+// Util::get_mem_total (src/util.cc:195): MemTotal of /proc/meminfo in kB times 1000 (the
+// default of "mem_total"); the physical page count where /proc is unreadable.
+double machine_memory() {
+  std::ifstream f("/proc/meminfo");
+  std::string key;
+  double kb = 0.0;
+  while (f >> key) {
+    if (key == "MemTotal:") {
+      f >> kb;
+      return kb * 1000.0;
+    }
+    std::getline(f, key);
+  }
+  const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
+  return pages > 0 && page > 0 ? static_cast<double>(pages) * static_cast<double>(page) : 0.0;
 }
 
 // Config::get (src/config.h:21-50): slash-separated keys, defaults for optional ones.
@@ -328,19 +347,24 @@ int main(int, char* argv[]) {
       uncert = u_psto;
     }
     if (eps_pt < eps_pt_psto) {
+      // solver.h:905-1036: the sample size comes from the pilot and the PT memory unless
+      // n_dets_in_sample_pt_sto is set; semisto_sto (default true) needs the pilot
       const size_t n_samples = (size_t)cfg_d("n_dets_in_sample_pt_sto", 0);
-      if (n_samples == 0 || cfg_b("semisto_sto", true))
-        std::printf("Note: this build runs the stochastic stage with an explicit sample size "
-                    "and semisto_sto = false (using %zu samples)\n",
-                    n_samples ? n_samples : (size_t)200000);
+      const bool semisto = cfg_b("semisto_sto", true);
+      double pt_mem = 0.0;
+      ck(c, shci_pt_mem_avail(c, cfg_d("mem_total", machine_memory()), &pt_mem), "PT memory");
       double sto = 0.0, u_sto = 0.0;
-      size_t iters = 0;
+      size_t iters = 0, info[3] = {0, 0, 0};
       ck(c, shci_pt2_sto(c, wf.energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),
-                         n_samples ? n_samples : 200000, 0,
-                         (unsigned)cfg_d("random_seed", 347634253),
-                         (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, &sto,
-                         &u_sto, &iters, nullptr, 0),
+                         n_samples, semisto ? 1 : 0, (unsigned)cfg_d("random_seed", 347634253),
+                         (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, pt_mem,
+                         cfg_d("pt_sto_mem_usage", 0.4), &sto, &u_sto, &iters, info, nullptr, 0),
          "PT2 sto");
+      if (n_samples == 0) {
+        std::printf("Number of unique var dets in sample target: %'zu\n", info[2]);
+        std::printf("Number of dets chosen: %'zu\n", info[0]);
+      }
+      if (semisto) std::printf("Number of deterministic var dets: %'zu\n", info[1]);
       std::printf("PT sto correction (eps1= %.2e, eps_pt= %.2e): %.10f +- %.10f Ha\n", eps_var,
                   eps_pt, sto, u_sto);
       value += sto;

@@ -638,20 +638,42 @@ shci_status shci_pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, dou
 shci_status shci_pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
                          size_t n_batches, size_t n_dets_in_sample, int semisto,
                          unsigned random_seed, size_t max_iterations, double target_error,
-                         double psto_uncert, double* correction, double* uncert,
-                         size_t* n_iterations, double* loops, size_t cap) {
+                         double psto_uncert, double pt_mem_avail, double mem_usage,
+                         double* correction, double* uncert, size_t* n_iterations,
+                         size_t* sample_info, double* loops, size_t cap) {
   if (!c) return SHCI_ERR_ARG;
   return guard(c, [&]() {
     need_integrals(c);
     need_dets(c);
     std::vector<double> lv;
+    size_t info[3] = {0, 0, 0};
     auto r = pt2_sto(c, energy_var, eps_pt_psto, eps_pt, n_batches, n_dets_in_sample,
-                     semisto != 0, random_seed, max_iterations, target_error, psto_uncert, &lv);
+                     semisto != 0, random_seed, max_iterations, target_error, psto_uncert,
+                     pt_mem_avail, mem_usage, &lv, info);
     if (correction) *correction = r.value;
     if (uncert) *uncert = r.uncert;
     if (n_iterations) *n_iterations = r.n_batches_done;
+    if (sample_info)
+      for (int k = 0; k < 3; k++) sample_info[k] = info[k];
     if (loops)
       for (size_t k = 0; k < lv.size() && k < cap; k++) loops[k] = lv[k];
+  });
+}
+
+shci_status shci_pt_mem_avail(shci_ctx* c, double mem_total, double* out) {
+  if (!c || !out) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    if (!c->Q.built) throw ArgError("heat-bath queues not built (call shci_build_queues)");
+    // solver.h:601-611 with one process: bytes per det = two 64-bit chunks per spin (32 B),
+    // helper size = 32 B per heat-bath queue entry (chem_system.cc:112, 195)
+    const size_t mt = static_cast<size_t>(mem_total);
+    const size_t mem_var = c->up.size() * (32 * 3 + 8);
+    const size_t helper = 32 * (c->Q.n_hci + c->Q.n_singles);
+    const double left = static_cast<double>(mt) * 0.7 - static_cast<double>(mem_var) -
+                        static_cast<double>(helper);
+    if (!(left > 0)) throw ArgError("mem_total leaves no memory for PT2");
+    *out = static_cast<double>(static_cast<size_t>(left));
   });
 }
 

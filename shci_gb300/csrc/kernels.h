@@ -91,7 +91,8 @@ Pt2Out pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt
 Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
                size_t n_batches, size_t n_dets_in_sample, bool semisto, unsigned random_seed,
                size_t max_iterations, double target_error, double psto_uncert,
-               std::vector<double>* loops);
+               double pt_mem_avail, double mem_usage, std::vector<double>* loops,
+               size_t* info);
 
 // pt2.cu: out[2g], out[2g+1] = sum and sum of squares of x over segment g = [starts[g],
 // starts[g+1]) (device arrays; m = total length), compensated and in a fixed order.

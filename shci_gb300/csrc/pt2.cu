@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <stdexcept>
 #include <numeric>
+#include <queue>
 #include <random>
 #include <stack>
 #include <unordered_map>
@@ -48,6 +49,7 @@ struct PtParams {
   uint64_t batch;    // dtm / psto: the batch being computed
   double factor;     // sto: 1 / (n_samples - n_dtm - 1)
   int iter_shift;    // sto: bit position of the iteration index in the emitted up key
+  int pilot;         // sto: sample-size pilot (only single excitations face the |H c| test)
 };
 
 // Stochastic sources: entry k = (det, iteration, count, weight, batch, deterministic?)
@@ -235,7 +237,10 @@ __global__ void __launch_bounds__(kPtWarps * 32, 4)
         // handler order of solver.h:703-713: batch (done), variational set, |H_ai c_i|
         bool ok = cu != kInvalid && !in_set(P, cu, cd);
         double hc = 0.0;
-        if (ok) {
+        // the pilot's handler tests |H_ai c_i| for single excitations only (solver.h:958-962)
+        const bool test = MODE != kSto || !Q.pilot ||
+                          popc64(up ^ cu) + popc64(dn ^ cd) == 2;
+        if (ok && test) {
           hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
           if (fabs(hc) < Q.eps) ok = false;
         }
@@ -768,41 +773,167 @@ Pt2Out pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt
   return pt_batched<kPsto>(c, energy_var, Q, n_batches, target_error, eps_pt);
 }
 
-// Stochastic stage (solver.h:898-1153) with n_dets_in_sample given.  psto_uncert is the
-// uncertainty of the preceding stage (it enters the second stopping rule).
+// Number of unique PT dets in hash batch 0 of 128 of the given sources (the sample-size
+// pilot of solver.h:942-972; no |H_ai c_i| test on double excitations).
+size_t pilot_pt_dets(shci_ctx* c, PtSetup& st, const std::vector<size_t>& src, double eps_pt,
+                     int shift) {
+  if (src.empty()) return 0;
+  cudaStream_t s = c->stream;
+  const uint32_t n_src = static_cast<uint32_t>(src.size());
+  std::vector<uint32_t> h_det(src.begin(), src.end()), h_zero(n_src, 0u);
+  std::vector<double> h_one(n_src, 1.0);
+  std::vector<uint8_t> h_dtm(n_src, 1);
+  DevBuf<uint32_t> d_det, d_zero;
+  DevBuf<double> d_one;
+  DevBuf<uint8_t> d_dtm;
+  d_det.mt = d_zero.mt = d_one.mt = d_dtm.mt = &c->mem;
+  d_det.resize(n_src);
+  d_zero.resize(n_src);
+  d_one.resize(n_src);
+  d_dtm.resize(n_src);
+  SHCI_CUDA(cudaMemcpyAsync(d_det.p, h_det.data(), n_src * 4, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(d_zero.p, h_zero.data(), n_src * 4, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(d_one.p, h_one.data(), n_src * 8, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(d_dtm.p, h_dtm.data(), n_src, cudaMemcpyHostToDevice, s));
+  StoSources S{d_det.p, d_zero.p, d_one.p, d_one.p, d_zero.p, d_dtm.p};
+  PtParams Q{};
+  Q.eps = eps_pt;
+  Q.eps_psto = eps_pt;
+  Q.factor = 0.0;
+  Q.iter_shift = shift;
+  Q.pilot = 1;
+  set_batches(Q, 128);
+  PtParams Q1 = Q;
+  set_batches(Q1, 1);
+  const std::vector<uint64_t> hc = region_slots(pt_counts<kSto>(c, st, Q1, S, n_src), 128);
+  DevBuf<uint64_t> bu, bd;
+  DevBuf<double> bv[5];
+  bu.mt = bd.mt = &c->mem;
+  for (auto& b : bv) b.mt = &c->mem;
+  return pt_emit_reduce<kSto>(c, st, Q, S, n_src, hc, bu, bd, bv, shift + 5);
+}
+
+// Stochastic stage (solver.h:898-1153).  n_dets_in_sample = 0: the sample size comes from
+// the reference's 1,000-draw pilot and the PT memory pt_mem_avail (solver.h:942-1006);
+// semisto: the variational dets above the quantile of the top quarter of the unique-sample
+// target are summed deterministically in every iteration and the others sampled with
+// renormalised weights (solver.h:1009-1036).  psto_uncert is the uncertainty of the preceding
+// stage (it enters the second stopping rule).  info = {n_dets_in_sample, n_dtm,
+// n_unique_target} of the run.
 Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
                size_t n_batches, size_t n_dets_in_sample, bool semisto, unsigned random_seed,
                size_t max_iterations, double target_error, double psto_uncert,
-               std::vector<double>* loops) {
+               double pt_mem_avail, double mem_usage, std::vector<double>* loops,
+               size_t* info) {
   if (n_batches == 0) throw ArgError("n_batches must be >= 1");
-  if (n_dets_in_sample < 2) throw ArgError("n_dets_in_sample_pt_sto must be given (>= 2)");
-  if (semisto)
+  if (n_dets_in_sample == 1) throw ArgError("n_dets_in_sample_pt_sto must be 0 (automatic) or >= 2");
+  if (semisto && n_dets_in_sample != 0)
     throw ArgError("semisto_sto with n_dets_in_sample_pt_sto set has no deterministic dets in "
                    "the reference (its 25% quantile heap is empty: solver.h:1009-1021); set "
-                   "semisto_sto to false");
+                   "semisto_sto to false or leave n_dets_in_sample_pt_sto unset");
   const size_t n_var = c->up.size();
   std::vector<double> coefs(n_var);
   sync_dets(c);
   cudaStream_t s = c->stream;
   SHCI_CUDA(cudaMemcpyAsync(coefs.data(), c->d_coef.p, n_var * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
+  const int shift = c->I.n;
+  if (shift > 57) throw ArgError("stochastic PT2 supports n_orbs <= 57");
   const auto t_setup = std::chrono::steady_clock::now();
-  // probabilities (solver.h:921-933)
+  // probabilities and their running sums (solver.h:921-933)
   double sum_w = 0.0;
   for (size_t i = 0; i < n_var; i++) sum_w += std::abs(coefs[i]);
-  std::vector<double> probs(n_var);
-  for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(coefs[i]) / sum_w;
+  std::vector<double> probs(n_var), cum(n_var);
+  for (size_t i = 0; i < n_var; i++) {
+    probs[i] = std::abs(coefs[i]) / sum_w;
+    cum[i] = i > 0 ? probs[i] + cum[i - 1] : probs[i];
+  }
   std::default_random_engine gen(random_seed);
   std::uniform_real_distribution<double> ur(0., 1.);
-  const size_t n_dtm = 0;
+  PtSetup st;
+  pt_setup(c, st);
+  size_t n_target = 0;
+  if (n_dets_in_sample == 0) {
+    // pilot (solver.h:944-972): 1,000 inverse-CDF draws, PT dets of the unique ones in batch
+    // 0 of 128, scaled to a batch of n_batches
+    std::vector<uint8_t> seen(n_var, 0);
+    std::vector<size_t> list;
+    for (size_t k = 0; k < 1000; k++) {
+      const size_t id = std::lower_bound(cum.begin(), cum.end(), ur(gen)) - cum.begin();
+      if (id < n_var && !seen[id]) {
+        seen[id] = 1;
+        list.push_back(id);
+      } else if (id >= n_var) {
+        throw ArgError("coefficient weights do not sum to 1 (empty or non-finite wavefunction)");
+      }
+    }
+    const size_t n_pt = pilot_pt_dets(c, st, list, eps_pt, shift);
+    const size_t n_pt_batch = n_pt * 128 / n_batches;
+    const size_t bytes_per_entry = 2 * 16 + 40;  // solver.h:402, 905 (two 64-bit chunks)
+    const size_t cap = n_var / 8 + 1;
+    // a pilot without PT dets is a division by zero in the reference; the cap is taken
+    n_target = cap;
+    if (n_pt_batch > 0) {
+      const double t = static_cast<double>(static_cast<size_t>(pt_mem_avail)) * mem_usage *
+                       static_cast<double>(list.size()) / static_cast<double>(bytes_per_entry) /
+                       5.0 / static_cast<double>(n_pt_batch);
+      n_target = static_cast<size_t>(t);
+      if (n_target >= cap) n_target = cap;
+    }
+    // draws until the target of unique dets is met (solver.h:990-1000)
+    std::fill(seen.begin(), seen.end(), 0);
+    size_t n_unique = 0;
+    while (n_unique < n_target) {
+      const size_t id = std::lower_bound(cum.begin(), cum.end(), ur(gen)) - cum.begin();
+      if (id >= n_var)
+        throw ArgError("coefficient weights do not sum to 1 (empty or non-finite wavefunction)");
+      if (!seen[id]) {
+        seen[id] = 1;
+        n_unique++;
+      }
+      n_dets_in_sample++;
+    }
+  }
+  std::vector<uint32_t> dtm_list;
+  if (semisto) {
+    // the top n_target / 4 weights by a min-heap quantile (solver.h:1009-1036)
+    const size_t n_heap = n_target / 4;
+    if (n_heap == 0)
+      throw ArgError("semistochastic PT2 needs a sample-size target of at least 4 (the "
+                     "reference's quantile heap would be empty)");
+    std::priority_queue<double, std::vector<double>, std::greater<double>> heap;
+    for (size_t i = 0; i < n_heap; i++) heap.push(probs[i]);
+    for (size_t i = n_heap; i < n_var; i++)
+      if (heap.top() < probs[i]) {
+        heap.pop();
+        heap.push(probs[i]);
+      }
+    const double C = heap.top();
+    double s2 = 0.0;
+    for (size_t i = 0; i < n_var; i++) {
+      if (probs[i] > C) {
+        probs[i] = 0.;
+        dtm_list.push_back(static_cast<uint32_t>(i));
+      } else {
+        s2 += probs[i];
+      }
+    }
+    for (auto& p : probs) p /= s2;
+  }
+  const size_t n_dtm = dtm_list.size();
+  if (n_dets_in_sample < n_dtm + 2)
+    throw ArgError("stochastic PT2 sample too small for its deterministic part");
+  if (info) {
+    info[0] = n_dets_in_sample;
+    info[1] = n_dtm;
+    info[2] = n_target;
+  }
   std::vector<double> aprob;
   std::vector<size_t> alias;
   alias_tables(probs, aprob, alias);
   std::uniform_int_distribution<size_t> ui_var(0, n_var - 1);
   std::uniform_int_distribution<size_t> ui_batch(0, n_batches - 1);
   const double factor = 1. / (n_dets_in_sample - n_dtm - 1.);
-  const int shift = c->I.n;
-  if (shift > 57) throw ArgError("stochastic PT2 supports n_orbs <= 57");
   // Iterations per device pass: the first pass runs the 6 iterations before which the
   // stopping rules cannot fire, later passes 2 (results past the stop are discarded).
   const uint32_t kFirstChunk = 6, kNextChunk = 2;
@@ -811,8 +942,6 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   if (c->prof.on)
     c->prof.host("pt2_host_setup", std::chrono::duration<double, std::milli>(
                                        std::chrono::steady_clock::now() - t_setup).count());
-  PtSetup st;
-  pt_setup(c, st);
   Pt2Out out;
   std::vector<double> loop_vals;
   bool done = false;
@@ -849,6 +978,15 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
           if (cnt[id]++ == 0) list.push_back(id);
         }
         const size_t batch_id = ui_batch(gen);
+        // the deterministic dets first (count and weight 1), then the sampled ones
+        for (uint32_t i : dtm_list) {
+          h_det.push_back(i);
+          h_iter.push_back(it);
+          h_batch.push_back(static_cast<uint32_t>(batch_id));
+          h_count.push_back(1.0);
+          h_weight.push_back(1.0);
+          h_dtm.push_back(1);
+        }
         for (size_t k = 0; k < list.size(); k++) {
           const size_t i = list[k];
           h_det.push_back(static_cast<uint32_t>(i));
@@ -856,7 +994,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
           h_batch.push_back(static_cast<uint32_t>(batch_id));
           h_count.push_back(static_cast<double>(cnt[i]));
           h_weight.push_back((n_dets_in_sample - n_dtm) * probs[i]);
-          h_dtm.push_back(k < n_dtm ? 1 : 0);
+          h_dtm.push_back(0);
         }
         for (size_t i : list) cnt[i] = 0;
       }

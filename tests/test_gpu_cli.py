@@ -42,3 +42,27 @@ def test_cli_c_atom_matches_reference_result(tmp_path):
     diag = sum(float(l.split(",")[2]) for l in lines[1:] if l.split(",")[0] == l.split(",")[1])
     assert abs(diag - 6.0) < 1e-8
     assert (tmp_path / "spatialRDM.txt").read_text().splitlines()[0].strip() == "22"
+
+
+def test_cli_stock_stochastic_settings(tmp_path):
+    """A config without n_dets_in_sample_pt_sto and with the default semisto_sto runs the
+    reference's default stochastic stage (pilot-sized sample, deterministic top quarter);
+    mem_total is fixed so the sample size does not depend on the machine."""
+    from shci_gb300 import build
+    exe = build.build_cli()
+    shutil.copyfile(C_ATOM, tmp_path / "FCIDUMP")
+    cfg = {"system": "chem", "n_up": 4, "n_dn": 2, "eps_vars": [5e-5],
+           "eps_vars_schedule": [2e-3, 1e-3, 5e-4, 2e-4, 1e-4], "chem": {"point_group": "d2h"},
+           "eps_pt_dtm": 5e-6, "eps_pt_psto": 1e-7, "eps_pt": 5e-8, "mem_total": 4e9}
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    for line in ("Number of unique var dets in sample target:", "Number of dets chosen:",
+                 "Number of deterministic var dets:"):
+        assert line in out
+    res = json.load(open(tmp_path / "result.json"))
+    ref = json.load(open(os.path.join(GOLDEN, "c_atom_pins.json")))
+    tot = res["energy_total"]["5.00e-05"]["5.00e-08"]
+    ref_tot = ref["energy_total"]["5.00e-05"]["5.00e-08"]
+    assert abs(tot["value"] - ref_tot["value"]) < 5 * (tot["uncert"] + ref_tot["uncert"])

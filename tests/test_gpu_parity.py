@@ -285,6 +285,45 @@ def test_pt2_sto_matches_oracle(shci, oracle_mod, w1_fcidump):
     assert abs(v - vo) < 1e-14 and abs(u - uo) < 1e-13
 
 
+@pytest.mark.parametrize("pt_mem", [1e7, 1e9])
+def test_pt2_semistochastic_auto_sample_matches_oracle(shci, oracle_mod, w1_fcidump, pt_mem):
+    """The reference's default stochastic stage: the sample size from the 1,000-draw pilot and
+    the PT memory (1e7 B: the memory formula decides; 1e9 B: the n_var / 8 + 1 cap does), the
+    top quarter of the unique-sample target deterministic, the rest sampled.  Sample size,
+    deterministic count and every iteration's estimate equal the oracle's."""
+    o = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    o.run_all_variations([2e-4, 1e-4], [], 5e-5)
+    up, dn, coefs = o.dets()
+    c = new_ctx(shci, w1_fcidump, 5, 5)
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    ev = o.energy_var
+    info, info_o = {}, {}
+    v, u, loops = c.pt2_sto(ev, 1e-6, 1e-8, 16, 0, 347634253, 12, 5e-5, 0.0, semisto=True,
+                            pt_mem_avail=pt_mem, info=info)
+    vo, uo, loops_o = o.pt_sto(1e-6, 1e-8, 16, 0, 347634253, 12, 5e-5, 0.0, semisto=True,
+                               pt_mem_avail=pt_mem, info=info_o)
+    assert info == info_o
+    assert info["n_dtm"] > 0 and info["n_samples"] > info["n_dtm"]
+    if pt_mem == 1e9:
+        assert info["n_unique_target"] == len(up) // 8 + 1
+    assert len(loops) == len(loops_o) >= 6
+    assert np.max(np.abs(loops - loops_o)) < 1e-13
+    assert abs(v - vo) < 1e-13 and abs(u - uo) < 1e-13
+    # a given sample size with semisto leaves the reference's quantile heap empty: refused
+    with pytest.raises(shci.ShciError):
+        c.pt2_sto(ev, 1e-6, 1e-8, 16, 3000, 347634253, 12, 5e-5, 0.0, semisto=True)
+
+
+def test_pt_mem_avail_formula(shci, w1_fcidump):
+    """solver.h:601-611 with one process: mem_total * 0.7 - n_dets * 104 - 32 * queue entries."""
+    c = new_ctx(shci, w1_fcidump, 5, 5)
+    q = c.build_queues()
+    n = c.n_dets()
+    got = c.pt_mem_avail(64e9)
+    assert got == float(int(64e9 * 0.7 - n * 104 - 32 * (q["n_hci"] + q["n_singles"])))
+
+
 def test_mixed_precision_energy(shci, c_ham):
     c, _, _, _, _, up, dn, coefs = c_ham
     c.set_coefs(coefs)
