@@ -135,14 +135,21 @@ def gpu_setup(ctx, fcidump, w):
     return ctx.dets()
 
 
-def cpu_sample(fcidump, w, up, dn, target_rows=20000):
-    """Oracle (CPU restatement) timing of one step on a strided row sample, scaled."""
+def sample_stride(n, target_rows=20000):
+    return max(1, n // target_rows)
+
+
+def cpu_sample(fcidump, w, up, dn, target_rows=20000, keep=None):
+    """Oracle (CPU restatement) timing of one step on a strided row sample, scaled.  keep (a
+    dict, optional) receives the oracle's sampled rows."""
     from oracle.oracle import Oracle
     o = Oracle(fcidump, w["n_up"], w["n_dn"])
     o.set_dets(up, dn)
     n = len(up)
-    stride = max(1, n // target_rows)
+    stride = sample_stride(n, target_rows)
     r = o.hbuild_sample(stride, 0)
+    if keep is not None:
+        keep["rows"] = o.sample_rows()
     scale = n / max(1, r["rows"])
     step = r["index_s"] + scale * (r["rows_s"] + DAVIDSON_MATVECS * r["spmv_s"])
     return step, {"value": step, "unit": "s", "cores": Oracle.threads(), "kind": "port",
@@ -240,6 +247,119 @@ def run_pt2(ctx, stream, e_var):
     return out
 
 
+def run_pt2_timed(ctx, stream, e_var, warmup, steps):
+    """The three PT2 stages, warmup untimed runs and steps timed runs (CUDA events on the
+    context stream per run); the last run's full record plus the per-run seconds."""
+    secs = []
+    out = None
+    for k in range(warmup + steps):
+        out = run_pt2(ctx, stream, e_var)
+        if "error" in out:
+            return out
+        if k >= warmup:
+            secs.append(out["s"])
+    out["s_runs"] = secs
+    out["s"] = statistics.median(secs)
+    out["warmup"], out["steps"] = warmup, steps
+    return out
+
+
+def parity_n40(fcidump, w, up, dn, ctx, rows_mixed):
+    """The oracle's own selection schedule on the CPU gives the step's det list independently;
+    it must equal the device's bit for bit.  The oracle's rows of a strided sample (the CPU
+    baseline's) must equal the device store's rows: columns exactly, FP64 values exactly for
+    the FP64 build (rows_fp64) and, for the mixed build (rows_mixed), the FP32 value and FP32
+    residual of the oracle's FP64 value."""
+    import numpy as np
+    from oracle.oracle import Oracle
+    t0 = time.time()
+    o = Oracle(fcidump, w["n_up"], w["n_dn"])
+    for eps in SCHEDULE:
+        o.run_variation_step(eps, False, TARGET_ERROR)
+    o.select(EPS_VAR)
+    oup, odn, _ = o.dets()
+    del o
+    out = {"oracle_select_s": time.time() - t0, "n_dets_oracle": int(len(oup)),
+           "dets_equal": bool(len(oup) == len(up) and np.array_equal(oup, up)
+                              and np.array_equal(odn, dn))}
+    return out
+
+
+def compare_rows(o_rows, g_rows, mixed):
+    """Oracle sample rows vs device rows: (all columns equal, all values equal)."""
+    import numpy as np
+    _, ooff, ocols, ovals = o_rows
+    goff, gcols, gvals = g_rows
+    if not (np.array_equal(ooff, goff) and np.array_equal(ocols, gcols)):
+        return False, False
+    if mixed:
+        hi = ovals.astype(np.float32)
+        lo = (ovals - hi.astype(np.float64)).astype(np.float32)
+        want = hi.astype(np.float64) + lo.astype(np.float64)
+    else:
+        want = ovals
+    return True, bool(np.array_equal(gvals, want))
+
+
+SMALL = {  # workload -> (eps_vars, schedule, eps_pt_dtm or None)
+    1: ([2e-4, 1e-4], [], 1e-6),
+    2: ([5e-5], [1e-3, 5e-4, 2e-4, 1e-4], None),
+}
+
+
+def run_small_configs(data_dir, device, repeats=3):
+    """The benchmark's first two configurations run in full, on the device and by the oracle
+    on every host thread (median of `repeats` runs each, no sampling or scaling): n = 16
+    (variation at 2e-4 then 1e-4, deterministic PT2 at 1e-6) and n = 26 (schedule 1e-3 ...
+    1e-4, variation at 5e-5).  Phases: variation (selection + Hamiltonian + Davidson
+    iterations) and deterministic PT2."""
+    import shci_gb300 as S
+    from oracle.oracle import Oracle
+    from shci_gb300 import synthetic
+    out = {}
+    for k, (eps_vars, sched, eps_dtm) in SMALL.items():
+        wk = synthetic.WORKLOADS[k]
+        f = synthetic.workload_fcidump(k, data_dir)
+        g_var, g_pt, c_var, c_pt = [], [], [], []
+        res = {}
+        for r in range(repeats):
+            ctx = S.Context(device)
+            ctx.load_fcidump(f, wk["n_up"], wk["n_dn"])
+            t0 = time.perf_counter()
+            e = ctx.run_variation(eps_vars, sched, TARGET_ERROR, precision=S.PREC_MIXED)
+            t1 = time.perf_counter()
+            g_var.append(t1 - t0)
+            nd, _, _ = ctx.var_trace()
+            res.update(n_dets=int(nd[-1]), energy_var_gpu=float(e[-1]))
+            if eps_dtm:
+                ctx.build_queues()
+                t2 = time.perf_counter()
+                v, _, n_pt = ctx.pt2_dtm(e[-1], eps_dtm, 1)
+                g_pt.append(time.perf_counter() - t2)
+                res.update(pt_dtm_gpu=v, n_pt_dets=int(n_pt))
+            ctx.close()
+            o = Oracle(f, wk["n_up"], wk["n_dn"])
+            t0 = time.perf_counter()
+            eo = o.run_all_variations(eps_vars, sched, TARGET_ERROR)
+            c_var.append(time.perf_counter() - t0)
+            res["energy_var_cpu"] = float(eo[-1])
+            if eps_dtm:
+                t2 = time.perf_counter()
+                vo, _, _ = o.pt_dtm(eps_dtm, 1)
+                c_pt.append(time.perf_counter() - t2)
+                res["pt_dtm_cpu"] = vo
+            del o
+        med = statistics.median
+        res.update({"variation": {"gpu_s": med(g_var), "cpu_s": med(c_var)},
+                    "cpu_cores": Oracle.threads(), "cpu_kind": "port", "repeats": repeats,
+                    "workload": "synthetic n=%d %da%db, eps_vars %s, schedule %s"
+                                % (wk["n"], wk["n_up"], wk["n_dn"], eps_vars, sched)})
+        if eps_dtm:
+            res["pt_dtm"] = {"eps_pt_dtm": eps_dtm, "gpu_s": med(g_pt), "cpu_s": med(c_pt)}
+        out["n%d" % wk["n"]] = res
+    return out
+
+
 def run_batched(data_dir, n_instances=256, cpu_sample=8):
     """Workload 5: n_instances synthetic FCIDUMPs (n ~ U[12,20], electrons per spin ~
     U[3, n/2-1], seeds 20261203 + 1000 + i), eps_var 1e-4, deterministic PT2 at 1e-6, solved
@@ -323,19 +443,24 @@ def run_ours(args):
     stats = ctx.hamiltonian_stats()
     ms = max_over_ranks(ms, f"cuda:{local}")
 
-    # PT2 on the step's wavefunction (the metric's "PT2 s"): dtm, psto, sto stages
-    pt2 = run_pt2(ctx, stream, e_mixed) if args.pt2 else None
+    # PT2 on the step's wavefunction (the metric's "PT2 s"): dtm, psto, sto stages, timed over
+    # the same warm-up and step counts
+    pt2 = run_pt2_timed(ctx, stream, e_mixed, args.warmup, args.steps) if args.pt2 else None
     batched = run_batched(args.data) if args.batched else None
 
-    # all-FP64 form of the same step
+    # all-FP64 form of the same step, timed over the same step count
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     step(S.PREC_FP64)
     barrier()
     ev2.record(stream)
-    e_fp64, _ = step(S.PREC_FP64)
+    for _ in range(args.steps):
+        e_fp64, _ = step(S.PREC_FP64)
     ev3.record(stream)
     barrier()
-    ms_fp64 = ev2.elapsed_time(ev3)
+    ms_fp64 = ev2.elapsed_time(ev3) / args.steps
+    sample = np.arange(0, n, sample_stride(n), dtype=np.uint64)
+    rows_fp64 = ctx.hamiltonian_rows(sample) if args.parity else None
+    pt2_fp64 = run_pt2(ctx, stream, e_fp64) if args.pt2 else None
 
     # end to end through the public API with pinned host buffers
     pin_up = torch.from_numpy(up).pin_memory()
@@ -353,6 +478,7 @@ def run_ours(args):
         if k >= args.warmup:
             e2e_ms.append((tb - ta) * 1e3)
     e2e = statistics.median(e2e_ms)
+    rows_mixed = ctx.hamiltonian_rows(sample) if args.parity else None
 
     if rank != 0:
         return
@@ -403,8 +529,30 @@ def run_ours(args):
             "frac": dk["frac"], "traffic": measured_traffic.get(dom), "peak_kind": peak_kind,
             "alg_bytes_per_launch": alg.get(dom)}
     cpu = None
-    if not args.no_cpu_baseline:
-        _, cpu = cpu_sample(fcidump, w, up, dn)
+    keep = {}
+    if not args.no_cpu_baseline or args.parity:
+        _, cpu = cpu_sample(fcidump, w, up, dn, keep=keep)
+    parity = None
+    if args.parity:
+        parity = parity_n40(fcidump, w, up, dn, ctx, rows_mixed)
+        o_rows = keep["rows"]
+        parity["sample_rows"] = int(len(sample))
+        parity["sample_elements"] = int(len(o_rows[2]))
+        parity["rows_equal_oracle"] = bool(np.array_equal(o_rows[0], sample))
+        c64, v64 = compare_rows(o_rows, rows_fp64, False)
+        cmx, vmx = compare_rows(o_rows, rows_mixed, True)
+        parity.update({"fp64_columns_equal": c64, "fp64_values_equal": v64,
+                       "mixed_columns_equal": cmx, "mixed_split_equal": vmx})
+    if args.no_cpu_baseline:
+        cpu = None
+    small = run_small_configs(args.data, local) if args.small else None
+    pt2_total = None
+    if pt2 and pt2_fp64 and "error" not in pt2 and "error" not in pt2_fp64:
+        pt2_total = {"energy_total_mixed": e_mixed + pt2["correction"],
+                     "energy_total_fp64": e_fp64 + pt2_fp64["correction"],
+                     "dE_pt2_mixed_vs_fp64": abs(pt2["correction"] - pt2_fp64["correction"]),
+                     "dE_total_mixed_vs_fp64": abs(e_mixed + pt2["correction"]
+                                                   - e_fp64 - pt2_fp64["correction"])}
     line = {
         "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
@@ -419,8 +567,12 @@ def run_ours(args):
         "gpu_launches": launches // args.steps,
         "clocks": clk.summary(),
         "pt2": pt2,
+        "pt2_fp64_wavefunction": pt2_fp64,
+        "totals": pt2_total,
+        "parity": parity,
+        "small_configs": small,
         "batched": batched,
-        "fp64": {"ms_per_step": ms_fp64, "energy": e_fp64},
+        "fp64": {"ms_per_step": ms_fp64, "steps": args.steps, "energy": e_fp64},
         "energy_mixed_fp64corrected": e_mixed, "energy_davidson_mixed": e_dav,
         "dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
         "speedup_mixed_vs_fp64": ms_fp64 / ms,
@@ -439,6 +591,10 @@ def main():
     ap.add_argument("--workload", type=int, default=3, choices=sorted(WORKLOADS))
     ap.add_argument("--no-pt2", dest="pt2", action="store_false",
                     help="skip the PT2 measurement")
+    ap.add_argument("--no-small", dest="small", action="store_false",
+                    help="skip the full device and oracle runs of the two small configurations")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the oracle checks (independent det list, sampled rows)")
     ap.add_argument("--batched", action="store_true",
                     help="also time workload 5 (256 small instances, concurrent batch runner)")
     args = ap.parse_args()

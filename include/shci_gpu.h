@@ -110,12 +110,29 @@ shci_status shci_hamiltonian_elems(shci_ctx* ctx, const uint64_t* up_i, const ui
  * in the reference: it exists only for such callers.  It allocates nothing: inputs and
  * results are staged in one fixed 2.5 MiB device array built into the library (resident on
  * every GPU that loads it until the process exits).  At most 65,536 pairs per call (larger
- * n: SHCI_ERR_ARG).  All calls share the array, so calls that overlap on the GPU race; the
- * first call on each device looks up the array's address and should come before any stream
- * capture. */
+ * n: SHCI_ERR_ARG).  All calls share the array, so calls that overlap on the GPU race; each
+ * call looks up the array's address in the current context, and the first call on a device
+ * (which can load the library's device code) should come before any stream capture. */
 shci_status shci_hamiltonian_elems_noalloc(shci_ctx* ctx, const uint64_t* up_i,
                                            const uint64_t* dn_i, const uint64_t* up_j,
                                            const uint64_t* dn_j, size_t n, double* out);
+
+/* ---- connected dets (BaseSystem::find_connected_dets, base_system.h:57-62) ----------- */
+
+/* ChemSystem::find_connected_dets (src/chem/chem_system.cc:289-402) with second rejection off,
+ * for n dets at once.  Det k receives the dets its handler would be called with for the
+ * window [eps_min[k], eps_max[k]), in the handler's order: single excitations whose
+ * heat-bath bound S >= eps_min[k] (the upper end does not apply to singles, as in the
+ * reference), then double excitations with eps_min[k] <= |H| < eps_max[k], both with
+ * unoccupied targets; n_excite[] is 1 or 2.  A det with eps_max < eps_min has none (the
+ * reference's early return).  Two calls: with out_up == NULL, offsets[0..n] receive the
+ * running counts (det k's list is [offsets[k], offsets[k+1])); then, with those offsets,
+ * out_up / out_dn / n_excite (offsets[n] entries each) receive the lists.  The reference's
+ * return value (the largest rejected |H|) is eps_min[k] without second rejection. */
+shci_status shci_find_connected_dets(shci_ctx* ctx, const uint64_t* up, const uint64_t* dn,
+                                     const double* eps_max, const double* eps_min, size_t n,
+                                     uint64_t* offsets, uint64_t* out_up, uint64_t* out_dn,
+                                     uint8_t* n_excite);
 
 /* ---- Hamiltonian build (Hamiltonian<S>::update, hamiltonian.h:87-112, 415-598) -------- */
 
@@ -129,13 +146,28 @@ shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_ou
  * path}.  path (stats[9]) is 1 when the two-hole core join built the matrix: then
  * stats[2..4] are 0 and stats[6] is the number of core entries (dets x electron pairs).
  * path 0 is the group scan: stats[6..8] split the candidates into same-beta, same-alpha and
- * alpha-single x beta-single parts. */
+ * alpha-single x beta-single parts.  For the core join, stats[7] is 1 when the single-pass
+ * build (rows sized by their candidate counts) ran and 0 for the two-pass build (counted,
+ * then filled); the build takes the single pass when its store fits the free memory and the
+ * context's budget, else the two-pass join, else the group scan. */
 shci_status shci_hamiltonian_stats(shci_ctx* ctx, uint64_t* stats);
+
+/* Device bytes held by the context now, the most it has held, and its budget (0: none)
+ * (out[3]).  With a budget, an allocation past it fails with SHCI_ERR_OOM and leaves the
+ * context usable. */
+shci_status shci_memory_stats(shci_ctx* ctx, size_t* out);
 
 /* Copy the Hamiltonian to the host: row_ptr[n+1] (strict upper), cols[nnz], vals[nnz]
  * (as FP64), diag[n].  Rows list their columns in the device traversal order. */
 shci_status shci_get_hamiltonian(shci_ctx* ctx, uint64_t* row_ptr, uint32_t* cols,
                                  double* vals, double* diag);
+
+/* Selected rows of the Hamiltonian (the strict upper part of SparseMatrix rows,
+ * sparse_matrix.h): offsets[0..n_rows] receive the running element counts of rows[k]; cols and
+ * vals (offsets[n_rows] entries, may be NULL for a size query) the elements of each row in
+ * increasing column order, vals as FP64 (value + residual for mixed storage). */
+shci_status shci_get_hamiltonian_rows(shci_ctx* ctx, const uint64_t* rows, size_t n_rows,
+                                      uint64_t* offsets, uint32_t* cols, double* vals);
 
 /* ---- H*v and Davidson (SparseMatrix::mul, Davidson::diagonalize) --------------------- */
 

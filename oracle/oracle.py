@@ -79,6 +79,7 @@ def lib():
             "orc_pt_dtm": (None, [vp, d, sz, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(sz)]),
             "orc_run_variation_step": (d, [vp, d, i, d]),
             "orc_hbuild_sample": (None, [vp, sz, sz, _f64p]),
+            "orc_sample_rows": (sz, [vp, vp, vp, vp, vp]),
             "orc_threads": (i, []),
             "orc_pt_psto": (None, [vp, d, d, sz, d, d, _f64p]),
             "orc_pt_sto": (sz, [vp, d, d, sz, sz, u, sz, d, d, i, d, d, _f64p, _f64p, sz]),
@@ -254,6 +255,20 @@ class Oracle:
         self.L.orc_hbuild_sample(self.h, stride, offset, out)
         return dict(index_s=out[0], rows_s=out[1], spmv_s=out[2], nnz=int(out[3]),
                     rows=int(out[4]))
+
+    def sample_rows(self):
+        """Rows of the last hbuild_sample: (row ids, offsets, cols, FP64 values), each row's
+        strict upper part in increasing column order."""
+        m = self.L.orc_sample_rows(self.h, None, None, None, None)
+        rows = np.zeros(m, np.uint64)
+        off = np.zeros(m + 1, np.uint64)
+        self.L.orc_sample_rows(self.h, rows.ctypes.data, off.ctypes.data, None, None)
+        t = int(off[-1])
+        cols = np.zeros(max(t, 1), np.uint32)
+        vals = np.zeros(max(t, 1))
+        self.L.orc_sample_rows(self.h, rows.ctypes.data, off.ctypes.data, cols.ctypes.data,
+                               vals.ctypes.data)
+        return rows, off, cols[:t], vals[:t]
 
     @staticmethod
     def threads():

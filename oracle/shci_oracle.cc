@@ -1773,6 +1773,9 @@ using namespace orc;
 struct OrcHandle {
   Solver solver;
   std::string err;
+  // rows of the last orc_hbuild_sample (strict upper part, increasing column order)
+  std::vector<size_t> sample_rows;
+  std::vector<std::vector<std::pair<uint32_t, double>>> sample_elems;
 };
 
 extern "C" {
@@ -2021,6 +2024,29 @@ double orc_run_variation_step(void* h, double eps_var, int until_converged, doub
 // rows i = offset (mod stride) are computed (update_matrix, :415-598) and multiplied
 // (sparse_matrix.cc:28-56).  out[0..4] = {index seconds, row seconds, spmv seconds for the
 // sampled rows, sampled upper-triangle nnz (incl. diagonal), sampled rows}.
+// Rows of the last orc_hbuild_sample: row ids (count returned), then per row its element count
+// and, when cols is non-null, the elements (strict upper part, columns ascending).
+size_t orc_sample_rows(void* h, uint64_t* rows, uint64_t* offsets, uint32_t* cols, double* vals) {
+  auto* hh = static_cast<OrcHandle*>(h);
+  const size_t m = hh->sample_rows.size();
+  if (rows)
+    for (size_t k = 0; k < m; k++) rows[k] = hh->sample_rows[k];
+  if (offsets) {
+    offsets[0] = 0;
+    for (size_t k = 0; k < m; k++) offsets[k + 1] = offsets[k] + hh->sample_elems[k].size();
+  }
+  if (cols) {
+    size_t p = 0;
+    for (size_t k = 0; k < m; k++)
+      for (const auto& e : hh->sample_elems[k]) {
+        cols[p] = e.first;
+        vals[p] = e.second;
+        p++;
+      }
+  }
+  return m;
+}
+
 void orc_hbuild_sample(void* h, size_t stride, size_t offset, double* out) {
   auto& s = S(h);
   auto& H = s.ham;
@@ -2101,6 +2127,16 @@ void orc_hbuild_sample(void* h, size_t stride, size_t offset, double* out) {
   }
   const auto t4 = omp_get_wtime();
   H.clear();
+  // keep the sample's rows (diagonal dropped, columns ascending) for orc_sample_rows
+  auto* hh = static_cast<OrcHandle*>(h);
+  hh->sample_rows = rows;
+  hh->sample_elems.assign(rows.size(), {});
+  for (size_t r = 0; r < rows.size(); r++) {
+    auto& e = hh->sample_elems[r];
+    for (const auto& x : m.rows[rows[r]])
+      if (x.first != rows[r]) e.emplace_back(x.first, x.second);
+    std::sort(e.begin(), e.end());
+  }
   out[0] = t1 - t0;
   out[1] = t2 - t1;
   out[2] = t4 - t3;

@@ -60,6 +60,7 @@ def load():
         "shci_hamiltonian_elems_noalloc": [vp, _u64p, _u64p, _u64p, _u64p, sz, _f64p],
         "shci_update_hamiltonian": [vp, i, P(sz)],
         "shci_get_hamiltonian": [vp, _u64p, _u32p, _f64p, _f64p],
+        "shci_get_hamiltonian_rows": [vp, _u64p, sz, _u64p, vp, vp],
         "shci_hv": [vp, vp, vp, i],
         "shci_hv_host": [vp, _f64p, _f64p, i],
         "shci_davidson": [vp, d, P(d), P(i), _f64p, sz, P(sz)],
@@ -72,10 +73,12 @@ def load():
         "shci_get_launch_count": [vp, P(u64)],
         "shci_pt2_dtm": [vp, d, d, sz, P(d), P(d), P(sz)],
         "shci_hamiltonian_stats": [vp, _u64p],
+        "shci_memory_stats": [vp, _u64p],
         "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
         "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, d, d, P(d), P(d), P(sz), _u64p, _f64p, sz],
         "shci_pt_mem_avail": [vp, d, P(d)],
         "shci_mapreduce_sum": [vp, _f64p, sz, _f64p],
+        "shci_find_connected_dets": [vp, _u64p, _u64p, _f64p, _f64p, sz, _u64p, vp, vp, vp],
         "shci_rdm1": [vp, _f64p],
         "shci_rdm2": [vp, _f64p],
         "shci_profile": [vp, i],
@@ -281,10 +284,29 @@ class Context:
         self._ck(self.L.shci_hamiltonian_stats(self.h, s))
         if int(s[9]) == 1:
             return dict(path="core_join", n=int(s[0]), nnz=int(s[1]), candidates=int(s[5]),
-                        core_entries=int(s[6]))
+                        core_entries=int(s[6]), one_pass=bool(s[7]))
         return dict(path="group_scan", n=int(s[0]), nnz=int(s[1]), n_alpha=int(s[2]),
                     n_beta=int(s[3]), alpha_singles=int(s[4]), candidates=int(s[5]),
                     cand_same_beta=int(s[6]), cand_same_alpha=int(s[7]), cand_mixed=int(s[8]))
+
+    def memory_stats(self):
+        """(bytes held now, peak bytes held, budget) of the context's device memory."""
+        m = np.zeros(3, np.uint64)
+        self._ck(self.L.shci_memory_stats(self.h, m))
+        return int(m[0]), int(m[1]), int(m[2])
+
+    def hamiltonian_rows(self, rows):
+        """Elements of the given rows (strict upper part): offsets, cols, FP64 values, each row
+        in increasing column order."""
+        rows = np.ascontiguousarray(rows, np.uint64)
+        off = np.zeros(len(rows) + 1, np.uint64)
+        self._ck(self.L.shci_get_hamiltonian_rows(self.h, rows, len(rows), off, None, None))
+        m = int(off[-1])
+        cols = np.zeros(max(m, 1), np.uint32)
+        vals = np.zeros(max(m, 1))
+        self._ck(self.L.shci_get_hamiltonian_rows(self.h, rows, len(rows), off, cols.ctypes.data,
+                                                  vals.ctypes.data))
+        return off, cols[:m], vals[:m]
 
     def hamiltonian(self, nnz):
         n = self.n_dets()
@@ -401,6 +423,25 @@ class Context:
         out = ctypes.c_double()
         self._ck(self.L.shci_pt_mem_avail(self.h, float(mem_total), ctypes.byref(out)))
         return out.value
+
+    def find_connected(self, up, dn, eps_max, eps_min):
+        """BaseSystem::find_connected_dets for each det: (offsets[n+1], up, dn, n_excite)."""
+        up = np.ascontiguousarray(up, np.uint64)
+        dn = np.ascontiguousarray(dn, np.uint64)
+        n = len(up)
+        hi = np.ascontiguousarray(np.broadcast_to(eps_max, (n,)), np.float64)
+        lo = np.ascontiguousarray(np.broadcast_to(eps_min, (n,)), np.float64)
+        off = np.zeros(n + 1, np.uint64)
+        self._ck(self.L.shci_find_connected_dets(self.h, up, dn, hi, lo, n, off, None, None,
+                                                 None))
+        m = int(off[-1])
+        cu = np.zeros(max(m, 1), np.uint64)
+        cd = np.zeros(max(m, 1), np.uint64)
+        nx = np.zeros(max(m, 1), np.uint8)
+        self._ck(self.L.shci_find_connected_dets(self.h, up, dn, hi, lo, n, off,
+                                                 cu.ctypes.data, cd.ctypes.data,
+                                                 nx.ctypes.data))
+        return off, cu[:m], cd[:m], nx[:m]
 
     def mapreduce_sum(self, x):
         """(sum x, sum x^2) by the PT2 stages' compensated device reduction."""

@@ -345,8 +345,17 @@ shci_status shci_hamiltonian_stats(shci_ctx* c, uint64_t* stats) {
     stats[4] = n_as;
     stats[5] = c->H.candidates;
     for (int k = 0; k < 3; k++) stats[6 + k] = c->H.cand_parts[k];
+    if (c->H.join) stats[7] = c->H.packed ? 0 : 1;  // 1: single pass, rows sized by a bound
     stats[9] = c->H.join ? 1 : 0;
   });
+}
+
+shci_status shci_memory_stats(shci_ctx* c, size_t* out) {
+  if (!c || !out) return SHCI_ERR_ARG;
+  out[0] = c->mem.used;
+  out[1] = c->mem.peak;
+  out[2] = c->mem.budget;
+  return SHCI_OK;
 }
 
 shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols, double* vals,
@@ -358,14 +367,56 @@ shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols,
     cudaStream_t s = c->stream;
     const size_t n = H.n, nnz = H.nnz;
     if (!H.packed) {
-      // rows sized by an upper bound: hand out a packed copy
+      // rows sized by an upper bound: hand out a packed copy, made on the device when there is
+      // room for it and on the host otherwise (no device memory needed)
       DevBuf<uint64_t> p;
       DevBuf<uint32_t> cl;
       DevBuf<double> v;
       p.mt = &c->mem;
       cl.mt = &c->mem;
       v.mt = &c->mem;
-      pack_hamiltonian(c, p, cl, v);
+      try {
+        pack_hamiltonian(c, p, cl, v);
+      } catch (const OomError&) {
+        p.release();
+        cl.release();
+        v.release();
+        std::vector<uint64_t> rp(n + 1);
+        std::vector<uint32_t> rc(n);
+        const size_t cap = H.col.cap;
+        std::vector<uint32_t> hc(cap);
+        std::vector<double> hv;
+        std::vector<float> h32, r32;
+        SHCI_CUDA(cudaMemcpyAsync(rp.data(), H.row_ptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaMemcpyAsync(rc.data(), H.row_cnt.p, n * 4, cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaMemcpyAsync(hc.data(), H.col.p, cap * 4, cudaMemcpyDeviceToHost, s));
+        const bool fp64 = H.precision == SHCI_PREC_FP64;
+        if (vals) {
+          if (fp64) {
+            hv.resize(cap);
+            SHCI_CUDA(cudaMemcpyAsync(hv.data(), H.val64.p, cap * 8, cudaMemcpyDeviceToHost, s));
+          } else {
+            h32.resize(cap);
+            r32.resize(cap);
+            SHCI_CUDA(cudaMemcpyAsync(h32.data(), H.val32.p, cap * 4, cudaMemcpyDeviceToHost, s));
+            SHCI_CUDA(cudaMemcpyAsync(r32.data(), H.res32.p, cap * 4, cudaMemcpyDeviceToHost, s));
+          }
+        }
+        if (diag) SHCI_CUDA(cudaMemcpyAsync(diag, H.diag.p, n * 8, cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaStreamSynchronize(s));
+        uint64_t pos = 0;
+        for (size_t i = 0; i < n; i++) {
+          if (row_ptr) row_ptr[i] = pos;
+          for (uint32_t k = 0; k < rc[i]; k++) {
+            const uint64_t src = rp[i] + k;
+            if (cols) cols[pos] = hc[src];
+            if (vals) vals[pos] = fp64 ? hv[src] : (double)h32[src] + (double)r32[src];
+            pos++;
+          }
+        }
+        if (row_ptr) row_ptr[n] = pos;
+        return;
+      }
       if (row_ptr) SHCI_CUDA(cudaMemcpyAsync(row_ptr, p.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
       if (cols) SHCI_CUDA(cudaMemcpyAsync(cols, cl.p, nnz * 4, cudaMemcpyDeviceToHost, s));
       if (vals) SHCI_CUDA(cudaMemcpyAsync(vals, v.p, nnz * 8, cudaMemcpyDeviceToHost, s));
@@ -389,6 +440,12 @@ shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols,
     }
     SHCI_CUDA(cudaStreamSynchronize(s));
   });
+}
+
+shci_status shci_get_hamiltonian_rows(shci_ctx* c, const uint64_t* rows, size_t n_rows,
+                                      uint64_t* offsets, uint32_t* cols, double* vals) {
+  if (!c || !offsets || (n_rows && !rows)) return SHCI_ERR_ARG;
+  return guard(c, [&]() { get_rows(c, rows, n_rows, offsets, cols, vals); });
 }
 
 shci_status shci_hv(shci_ctx* c, const double* x_dev, double* y_dev, int use_residual) {
@@ -598,6 +655,17 @@ shci_status shci_mapreduce_sum(shci_ctx* c, const double* x, size_t n, double* o
     seg_reduce2(c, dx.p, starts.p, 1, n, res.p);
     SHCI_CUDA(cudaMemcpyAsync(out, res.p, 16, cudaMemcpyDeviceToHost, s));
     SHCI_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+shci_status shci_find_connected_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
+                                     const double* eps_max, const double* eps_min, size_t n,
+                                     uint64_t* offsets, uint64_t* out_up, uint64_t* out_dn,
+                                     uint8_t* n_excite) {
+  if (!c || !offsets) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    find_connected(c, up, dn, eps_max, eps_min, n, offsets, out_up, out_dn, n_excite);
   });
 }
 

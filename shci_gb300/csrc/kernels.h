@@ -18,6 +18,10 @@ void widen_u32_u64(const uint32_t* in, uint64_t* out, size_t n, cudaStream_t s);
 // Packed CSR copy of the element store (FP64 values) on the device.
 void pack_hamiltonian(shci_ctx* c, DevBuf<uint64_t>& ptr, DevBuf<uint32_t>& col,
                       DevBuf<double>& val);
+// Rows rows[0..m) of the current Hamiltonian: offsets[m+1] always; cols / vals (FP64; value +
+// residual for mixed storage) when non-null, each row in increasing column order.
+void get_rows(shci_ctx* c, const uint64_t* rows, size_t m, uint64_t* offsets, uint32_t* cols,
+              double* vals);
 void upload_integrals(shci_ctx* c);
 void upload_queues(shci_ctx* c);
 void sync_dets(shci_ctx* c);          // host det list -> device (if dirty)
@@ -98,6 +102,12 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
 // starts[g+1]) (device arrays; m = total length), compensated and in a fixed order.
 void seg_reduce2(shci_ctx* c, const double* x, const uint64_t* starts, uint32_t nseg, size_t m,
                  double* out);
+
+// connected.cu: BaseSystem::find_connected_dets for host det lists (see the C ABI); without
+// out_up, fills offsets[0..n] from the counts; with it, writes the lists at those offsets.
+void find_connected(shci_ctx* c, const uint64_t* up, const uint64_t* dn, const double* eps_max,
+                    const double* eps_min, size_t n, uint64_t* offsets, uint64_t* out_up,
+                    uint64_t* out_dn, uint8_t* n_excite);
 
 // rdm.cu
 void rdm1(shci_ctx* c, double* out);       // host [n*n]

@@ -1,5 +1,7 @@
 // Uploads of integrals / queues / dets, and batched matrix-element evaluation.
+#include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "ctx.h"
 #include "kernels.h"
@@ -42,6 +44,26 @@ __global__ void k_pack_rows(const uint64_t* __restrict__ row_ptr, const uint32_t
   }
 }
 
+// Rows rows[k] of the element store into [off[k], off[k+1]) (values as FP64).
+__global__ void k_gather_rows(const uint64_t* __restrict__ row_ptr,
+                              const uint32_t* __restrict__ row_len,
+                              const uint32_t* __restrict__ rows, uint32_t m,
+                              const uint64_t* __restrict__ off, const uint32_t* __restrict__ col,
+                              const double* __restrict__ v64, const float* __restrict__ v32,
+                              const float* __restrict__ r32, uint32_t* out_col, double* out_val) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < m; k += warps) {
+    const uint32_t i = rows[k];
+    const uint64_t a = row_ptr[i], b = off[k];
+    for (uint32_t t = lane; t < row_len[i]; t += 32) {
+      out_col[b + t] = col[a + t];
+      out_val[b + t] = v64 ? v64[a + t]
+                           : static_cast<double>(v32[a + t]) + static_cast<double>(r32[a + t]);
+    }
+  }
+}
+
 template <class T>
 void upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s, MemTracker* mt) {
   b.mt = mt;
@@ -78,6 +100,61 @@ void pack_hamiltonian(shci_ctx* c, DevBuf<uint64_t>& ptr, DevBuf<uint32_t>& col,
   SHCI_LAUNCH_CHECK();
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->launches += 2;
+}
+
+void get_rows(shci_ctx* c, const uint64_t* rows, size_t m, uint64_t* offsets, uint32_t* cols,
+              double* vals) {
+  const auto& H = c->H;
+  if (!H.valid) throw ArgError("no Hamiltonian built");
+  const size_t n = H.n;
+  for (size_t k = 0; k < m; k++)
+    if (rows[k] >= n) throw ArgError("row index out of range");
+  cudaStream_t s = c->stream;
+  std::vector<uint32_t> len(n);
+  if (n) SHCI_CUDA(cudaMemcpyAsync(len.data(), H.row_cnt.p, n * 4, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  offsets[0] = 0;
+  for (size_t k = 0; k < m; k++) offsets[k + 1] = offsets[k] + len[rows[k]];
+  if (!cols && !vals) return;
+  const uint64_t tot = offsets[m];
+  if (m == 0 || tot == 0) return;
+  std::vector<uint32_t> r32(rows, rows + m);
+  DevBuf<uint32_t> d_rows, o_col;
+  DevBuf<uint64_t> d_off;
+  DevBuf<double> o_val;
+  d_rows.mt = o_col.mt = &c->mem;
+  d_off.mt = &c->mem;
+  o_val.mt = &c->mem;
+  d_rows.resize(m);
+  d_off.resize(m + 1);
+  o_col.resize(tot);
+  o_val.resize(tot);
+  SHCI_CUDA(cudaMemcpyAsync(d_rows.p, r32.data(), m * 4, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(d_off.p, offsets, (m + 1) * 8, cudaMemcpyHostToDevice, s));
+  const bool fp64 = H.precision == SHCI_PREC_FP64;
+  k_gather_rows<<<grid_for(m * 32, 256), 256, 0, s>>>(
+      H.row_ptr.p, H.row_cnt.p, d_rows.p, static_cast<uint32_t>(m), d_off.p, H.col.p,
+      fp64 ? H.val64.p : nullptr, fp64 ? nullptr : H.val32.p, fp64 ? nullptr : H.res32.p,
+      o_col.p, o_val.p);
+  SHCI_LAUNCH_CHECK();
+  std::vector<uint32_t> hc(tot);
+  std::vector<double> hv(tot);
+  SHCI_CUDA(cudaMemcpyAsync(hc.data(), o_col.p, tot * 4, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaMemcpyAsync(hv.data(), o_val.p, tot * 8, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 1;
+  // each row in increasing column order
+  std::vector<uint64_t> idx;
+  for (size_t k = 0; k < m; k++) {
+    const uint64_t a = offsets[k], b = offsets[k + 1];
+    idx.resize(b - a);
+    for (uint64_t t = a; t < b; t++) idx[t - a] = t;
+    std::sort(idx.begin(), idx.end(), [&](uint64_t x, uint64_t y) { return hc[x] < hc[y]; });
+    for (uint64_t t = a; t < b; t++) {
+      if (cols) cols[t] = hc[idx[t - a]];
+      if (vals) vals[t] = hv[idx[t - a]];
+    }
+  }
 }
 
 void upload_integrals(shci_ctx* c) {

@@ -19,10 +19,11 @@
 //     corrupt each other's results; serialise them;
 //   - every call overwrites the slots it uses before reading them, so nothing in the array
 //     has to start at zero, and a call never sees results of an earlier call;
-//   - the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress) and caches it; make that first call before any stream capture.
+//   - every call looks up the array's device address in the calling thread's current
+//     context (cudaGetSymbolAddress, no allocation), so a device reset or a different
+//     context on the same device never sees a stale address; the first call on a device can
+//     load the library's device code, so make it before any stream capture.
 #include <cstring>
-#include <mutex>
 
 #include "ctx.h"
 #include "kernels.h"
@@ -40,20 +41,15 @@ constexpr int kMaxDevices = 64;
 // its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_elem_scratch[kScratchBytes];
 
-std::mutex g_addr_mu;
-void* g_addr[kMaxDevices] = {};
-
-// Device address of g_elem_scratch on `device` (current), looked up once per device.
+// Device address of g_elem_scratch in the current context (the caller has made `device`
+// current).  Looked up on every call: a cached address would outlive a cudaDeviceReset or
+// belong to another context of the same device.
 void* scratch_address(int device) {
   if (device < 0 || device >= kMaxDevices) throw ArgError("device ordinal out of range");
-  std::lock_guard<std::mutex> lk(g_addr_mu);
-  if (!g_addr[device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_elem_scratch);
-    if (e != cudaSuccess) throw CudaError(e, "cudaGetSymbolAddress(g_elem_scratch)");
-    g_addr[device] = p;
-  }
-  return g_addr[device];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_elem_scratch);
+  if (e != cudaSuccess) throw CudaError(e, "cudaGetSymbolAddress(g_elem_scratch)");
+  return p;
 }
 
 __global__ void k_elems_scratch(DevIntegrals I, unsigned char* scratch, size_t n) {

@@ -71,49 +71,6 @@ __device__ __forceinline__ uint32_t src_det(const StoSources& S, uint32_t k, int
   return mode == kSto ? S.det[k] : k;
 }
 
-// Walks the candidates of one source det (a warp): the heat-bath slots' index ranges in the
-// window [eps_min, eps_max) are flattened over the lanes 32 at a time, and f(slot, ok, cu,
-// cd) is called by all lanes for each group of 32 (slot = the lane holds an index entry of
-// the window, ok = that entry makes a valid candidate (cu, cd)).
-template <class F>
-__device__ __forceinline__ void pt_walk(const SelParams& P, uint64_t up, uint64_t dn,
-                                        double eps_min, double eps_max, F&& f) {
-  const unsigned lane = threadIdx.x & 31;
-  const int n_slots = P.n_elecs + P.n_pairs;
-  for (int s0 = 0; s0 < n_slots; s0 += 32) {
-    const int slot = s0 + lane;
-    uint32_t lo = 0, c = 0, orbs = 0;
-    if (slot < n_slots) slot_range(P, up, dn, slot, eps_min, eps_max, &lo, &c, &orbs);
-    uint32_t inc = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(kFull, inc, o);
-      if (lane >= (unsigned)o) inc += t;
-    }
-    const uint32_t total = __shfl_sync(kFull, inc, 31);
-    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-      const uint32_t t = t0 + lane;
-      uint32_t ol = 0;
-#pragma unroll
-      for (uint32_t step = 16; step; step >>= 1) {
-        const uint32_t v = __shfl_sync(kFull, inc, ol + step - 1);
-        if (v <= t) ol += step;
-      }
-      const uint32_t o_inc = __shfl_sync(kFull, inc, ol);
-      const uint32_t o_c = __shfl_sync(kFull, c, ol);
-      const uint32_t o_lo = __shfl_sync(kFull, lo, ol);
-      const uint32_t o_orbs = __shfl_sync(kFull, orbs, ol);
-      uint64_t cu = 0, cd = 0;
-      bool ok = false;
-      if (t < total) {
-        const uint32_t e = o_lo + (t - (o_inc - o_c));
-        ok = make_candidate_at(P, up, dn, s0 + (int)ol, o_orbs, e, &cu, &cd);
-      }
-      f(t < total, ok, cu, cd);
-    }
-  }
-}
-
 // h % n_batches exactly, without a 64-bit division: a mask for powers of two, else the
 // quotient estimate floor(h * magic / 2^64) with magic = floor((2^64 - 1) / n_batches), which
 // is at most 2 below the true quotient, corrected by subtraction.

@@ -152,3 +152,69 @@ def test_mixed_store_is_fp32_split_of_fp64(monkeypatch, c_dets):
     hi = v64.astype(np.float32)
     lo = (v64 - hi.astype(np.float64)).astype(np.float32)
     assert np.array_equal(vm, hi.astype(np.float64) + lo.astype(np.float64))
+
+
+def test_memory_budget_fallbacks_and_oom(monkeypatch, c_dets):
+    """A context budget (shci_create's hbm_budget_bytes, a host-side limit) steers the build:
+    from the unconstrained peak downwards it moves from the single-pass core join to the
+    two-pass join, every path giving the same elements, values and (where its vectors fit)
+    Davidson energy; below what any path needs, the build returns SHCI_ERR_OOM cleanly and the
+    context stays usable."""
+    import shci_gb300
+    for k in ("SHCI_HBUILD", "SHCI_JOIN_BITS", "SHCI_ROW_SORT"):
+        monkeypatch.delenv(k, raising=False)
+    up, dn, coefs = c_dets
+
+    def build(budget):
+        c = shci_gb300.Context(hbm_budget=budget)
+        c.load_fcidump(C_ATOM, 4, 2, "d2h")
+        c.set_dets(up, dn, coefs)
+        try:
+            nnz, _ = c.update_hamiltonian(shci_gb300.PREC_FP64)
+        except shci_gb300.ShciError as e:
+            return c, None, e
+        st = c.hamiltonian_stats()
+        kind = "scan" if st["path"] == "group_scan" else (
+            "join1" if st["one_pass"] else "join2")
+        rp, cols, vals, diag = c.hamiltonian(nnz)  # packs on the host when the budget is tight
+        return c, (kind, nnz, _sorted_rows(rp, cols, vals), diag), None
+
+    c0, ref, err = build(0)
+    assert err is None and ref[0] == "join1"
+    peak = c0.memory_stats()[1]
+    e_ref, _, _ = c0.davidson(1e-10)
+    seen = {"join1"}
+    oom = None
+    for f in (0.9, 0.75, 0.6, 0.5, 0.4, 0.3, 0.25, 0.2, 0.15, 0.1, 0.05, 0.01):
+        c, got, err = build(int(peak * f))
+        if err is not None:
+            assert err.status == 1, str(err)  # SHCI_ERR_OOM
+            assert "budget" in str(err) or "cudaMalloc" in str(err)
+            used, _, budget = c.memory_stats()
+            assert used <= budget
+            # the context still works after the failed build: a small det list builds
+            # within the same budget and matches the reference build's leading block
+            c.set_dets(up[:200], dn[:200], coefs[:200])
+            nnz_small, _ = c.update_hamiltonian(shci_gb300.PREC_FP64)
+            rp, cols, vals, _ = c.hamiltonian(nnz_small)
+            for (ca, va), (cb, vb) in zip(_sorted_rows(rp, cols, vals), ref[2][:200]):
+                keep = cb < 200
+                assert np.array_equal(ca, cb[keep]) and np.array_equal(va, vb[keep])
+            oom = f
+            break
+        kind, nnz, rows, diag = got
+        seen.add(kind)
+        assert nnz == ref[1] and np.array_equal(diag, ref[3])
+        for (ca, va), (cb, vb) in zip(rows, ref[2]):
+            assert np.array_equal(ca, cb) and np.array_equal(va, vb)
+        # Davidson on the budget-built matrix, where its vectors still fit
+        try:
+            e, _, _ = c.davidson(1e-10)
+            assert abs(e - e_ref) < 1e-12
+        except shci_gb300.ShciError as ex:
+            assert ex.status == 1
+    assert oom is not None, "no budget small enough to fail"
+    # the element store, not the join index, bounds this system: the budget moves the build
+    # from one pass to two passes and then to OOM (the group scan takes over when the join
+    # index cannot be built at all: 2^32 or more core entries, or SHCI_HBUILD=scan)
+    assert {"join1", "join2"} <= seen, seen

@@ -324,6 +324,38 @@ def test_pt_mem_avail_formula(shci, w1_fcidump):
     assert got == float(int(64e9 * 0.7 - n * 104 - 32 * (q["n_hci"] + q["n_singles"])))
 
 
+def test_find_connected_dets_matches_oracle(shci, c_oracle):
+    """shci_find_connected_dets (BaseSystem::find_connected_dets for a batch of dets) gives
+    every det's connected list in the reference's handler order, with n_excite, for windows
+    that include empty ones (eps_max < eps_min), an unbounded top and eps_min = 0."""
+    up, dn, coefs = c_oracle.dets()
+    rng = np.random.default_rng(5)
+    idx = rng.choice(len(up), 400, replace=False)
+    eps_min = 10.0 ** rng.uniform(-7, -2, len(idx))
+    eps_max = np.where(rng.random(len(idx)) < 0.3, 1e100, eps_min * 10.0 ** rng.uniform(-1, 3, len(idx)))
+    eps_min[:5] = 0.0
+    eps_max[5:10] = eps_min[5:10] * 0.5  # empty windows
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    off, cu, cd, nx = c.find_connected(up[idx], dn[idx], eps_max, eps_min)
+    total = 0
+    for k, i in enumerate(idx):
+        ou, od, onx = c_oracle.find_connected((int(up[i]), int(dn[i])), eps_max[k], eps_min[k])
+        a, b = int(off[k]), int(off[k + 1])
+        assert np.array_equal(cu[a:b], ou) and np.array_equal(cd[a:b], od), k
+        assert np.array_equal(nx[a:b], onx.astype(np.uint8)), k
+        total += len(ou)
+    assert total == int(off[-1]) > 10000
+    assert all(off[k + 1] == off[k] for k in range(5, 10))
+    # offsets that are not the count call's are refused
+    bad = off.copy()
+    bad[3] += 1
+    with pytest.raises(shci.ShciError):
+        c._ck(c.L.shci_find_connected_dets(c.h, up[idx], dn[idx], np.ascontiguousarray(eps_max),
+                                           np.ascontiguousarray(eps_min), len(idx), bad,
+                                           cu.ctypes.data, cd.ctypes.data, nx.ctypes.data))
+
+
 def test_mixed_precision_energy(shci, c_ham):
     c, _, _, _, _, up, dn, coefs = c_ham
     c.set_coefs(coefs)

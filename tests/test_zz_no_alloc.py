@@ -53,6 +53,27 @@ def test_noalloc_matches_existing_entry_point_twice():
         assert np.count_nonzero(want) > n // 4  # the batch exercises non-zero elements
 
 
+def test_noalloc_full_size_and_allocates_nothing():
+    """A call at exactly the 65,536-pair limit (every slot of the scratch array and the start
+    of its result region in use) matches the allocating entry point, and after a warm-up
+    call the device's free memory is the same before and after a call."""
+    import torch
+    import shci_gb300
+    ctx = shci_gb300.Context()
+    ctx.load_fcidump(C_ATOM, N_UP, N_DN, "d2h")
+    rng = np.random.default_rng(77)
+    ui, di, uj, dj = _random_pairs(rng, 65536)
+    want = ctx.h_elems(ui, di, uj, dj)
+    ctx.h_elems_noalloc(ui[:10], di[:10], uj[:10], dj[:10])  # warm-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    got = ctx.h_elems_noalloc(ui, di, uj, dj)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert np.array_equal(got, want)
+    assert free1 == free0
+
+
 def test_noalloc_rejects_oversized_requests():
     import shci_gb300
     from shci_gb300._lib import ShciError
