@@ -60,6 +60,7 @@ void after_integrals(shci_ctx* c) {
   c->dets_dirty = true;
   c->eps_tried.clear();
   c->H.valid = false;
+  c->H.prefix_ok = false;
   c->H.build_id++;
 }
 
@@ -250,6 +251,7 @@ shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
     c->dets_dirty = false;
     c->eps_tried.clear();
     c->H.valid = false;
+    c->H.prefix_ok = false;
     c->H.build_id++;
   });
 }
@@ -366,6 +368,16 @@ shci_status shci_get_hamiltonian(shci_ctx* c, uint64_t* row_ptr, uint32_t* cols,
     if (!H.valid) throw ArgError("no Hamiltonian built");
     cudaStream_t s = c->stream;
     const size_t n = H.n, nnz = H.nnz;
+    if (!H.older.empty()) {
+      // several segments (incremental updates): each row merged, in increasing column order
+      std::vector<uint64_t> all(n), off(n + 1);
+      for (size_t i = 0; i < n; i++) all[i] = i;
+      get_rows(c, all.data(), n, off.data(), cols, vals);
+      if (row_ptr) std::memcpy(row_ptr, off.data(), (n + 1) * 8);
+      if (diag) SHCI_CUDA(cudaMemcpyAsync(diag, H.diag.p, n * 8, cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      return;
+    }
     if (!H.packed) {
       // rows sized by an upper bound: hand out a packed copy, made on the device when there is
       // room for it and on the host otherwise (no device memory needed)
@@ -499,8 +511,11 @@ shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
     auto& H = c->H;
     cudaStream_t s = c->stream;
     const size_t nnz = row_ptr[n];
+    H.older.clear();
+    H.prefix_ok = false;
     H.n = n;
     H.nnz = nnz;
+    H.nnz_current = nnz;
     H.precision = SHCI_PREC_FP64;
     H.row_ptr.resize(n + 1);
     H.col.resize(nnz ? nnz : 1);
@@ -529,6 +544,8 @@ shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
     *eval = r.eval;
     if (converged) *converged = r.converged ? 1 : 0;
     H.valid = false;  // the context's own Hamiltonian is gone
+    H.prefix_ok = false;
+    H.older.clear();
     H.build_id++;
     c->dets_dirty = true;  // coefficients were overwritten
   });

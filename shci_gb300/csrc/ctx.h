@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -50,7 +51,37 @@ struct JoinIndex {
   DevBuf<uint64_t> span;        // [m] per entry (in det order): sorted position | bucket end << 32
 };
 
-// Upper-triangle Hamiltonian (strict upper part in CSR; FP64 diagonal kept apart).
+// Segments an incremental update may leave before the next update rebuilds the whole matrix.
+constexpr size_t kMaxSegments = 12;
+
+// A store segment kept from an earlier build: rows [0, n) of the strict upper part, row i at
+// [row_ptr[i], row_ptr[i] + row_cnt[i]).
+struct HSeg {
+  size_t n = 0, nnz = 0;
+  bool packed = true;
+  DevBuf<uint64_t> row_ptr;
+  DevBuf<uint32_t> row_cnt, col;
+  DevBuf<double> val64;
+  DevBuf<float> val32, res32;
+};
+
+// Read-only view of one segment (older segments first, then the current build's).
+struct SegView {
+  size_t n, nnz;
+  size_t len;  // entries allocated in col / values (row_ptr indexes into them)
+  bool packed;
+  const uint64_t* row_ptr;
+  const uint32_t* row_cnt;
+  const uint32_t* col;
+  const double* val64;
+  const float* val32;
+  const float* res32;
+};
+
+// Upper-triangle Hamiltonian (strict upper part in CSR; FP64 diagonal kept apart).  An
+// incremental update (Hamiltonian<S>::update with n_dets_prev > 0, hamiltonian.h:421-428)
+// moves the current store into `older` and builds a new segment with the new rows and the
+// new columns of the old rows; every consumer walks all segments.
 struct DevHamiltonian {
   size_t n = 0;
   size_t nnz = 0;
@@ -69,6 +100,12 @@ struct DevHamiltonian {
   DevBuf<double> diag;        // [n]
   DevBuf<uint32_t> row_cnt;   // [n+1] elements of each row
   bool valid = false;
+  // the stored matrix is that of the first n dets of the current list (dets were only
+  // appended since the build): an update can be incremental
+  bool prefix_ok = false;
+  std::vector<std::unique_ptr<HSeg>> older;  // segments of earlier (incremental) builds
+  size_t nnz_current = 0;                    // elements of the current segment
+  size_t n_prev = 0;                         // rows built before the last update (0: full)
   // mixed-storage H*v (spmv.cu): row abs-sum bound and fixed-point scratch
   bool bound_valid = false;
   DevBuf<double> scal;        // [0] max row abs sum, [1] max |x| (bits), [2] spare
@@ -76,6 +113,17 @@ struct DevHamiltonian {
   DevBuf<unsigned long long> yfix;  // [n] y in 64-bit fixed point
   DevBuf<float> rowabs;       // [n] scratch for the bound
 };
+
+// All segments of H: older ones, then the current build's.
+inline std::vector<SegView> segments(const DevHamiltonian& H) {
+  std::vector<SegView> v;
+  for (const auto& s : H.older)
+    v.push_back(SegView{s->n, s->nnz, s->col.n, s->packed, s->row_ptr.p, s->row_cnt.p,
+                        s->col.p, s->val64.p, s->val32.p, s->res32.p});
+  v.push_back(SegView{H.n, H.nnz_current, H.col.n, H.packed, H.row_ptr.p, H.row_cnt.p, H.col.p,
+                      H.val64.p, H.val32.p, H.res32.p});
+  return v;
+}
 
 struct DevQueues {
   size_t n_pairs = 0;

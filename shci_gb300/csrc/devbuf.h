@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 namespace shci {
 
@@ -103,6 +104,13 @@ struct DevBuf {
     n = k;
   }
   size_t bytes() const { return n * sizeof(T); }
+  // Exchanges the buffers (and their tracker) of two DevBufs.
+  void swap(DevBuf& o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    std::swap(cap, o.cap);
+    std::swap(mt, o.mt);
+  }
 };
 
 inline unsigned grid_for(size_t n, unsigned block, unsigned max_blocks = 152u * 64u) {

@@ -441,15 +441,48 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   const size_t n = c->up.size();
   cudaStream_t s = c->stream;
   if (n >= 0xffffffffull) throw ArgError("more than 2^32-1 dets");
-  H.n = n;
-  H.precision = precision;
-  H.valid = false;
-  H.build_id++;
-  H.bound_valid = false;
   const char* force = std::getenv("SHCI_HBUILD");
   const bool scan_only = force && std::strcmp(force, "scan") == 0;
   const bool two_pass = force && std::strcmp(force, "join2") == 0;
+  // Incremental update (Hamiltonian<S>::update with n_dets_prev, hamiltonian.h:89-93,
+  // 421-428): when the stored matrix is that of the first H.n dets of the list and dets were
+  // only appended, the new segment holds the new rows and the old rows' new columns.
+  // SHCI_HBUILD_INCREMENTAL=0 forces full rebuilds.
+  const char* inc_env = std::getenv("SHCI_HBUILD_INCREMENTAL");
+  const bool inc_ok = !(inc_env && std::strcmp(inc_env, "0") == 0);
+  size_t n_prev = 0;
+  if (inc_ok && H.prefix_ok && H.join && H.n > 0 && H.n < n && H.precision == precision &&
+      H.older.size() + 1 < kMaxSegments &&
+      (precision == SHCI_PREC_FP64 || H.rowabs.n == H.n))
+    n_prev = H.n;
+  H.prefix_ok = false;
+  H.valid = false;
+  H.build_id++;
+  H.bound_valid = false;
   H.join = !scan_only && join_prepare(c);
+  if (!H.join) n_prev = 0;  // the group scan builds whole matrices only
+  if (n_prev) {
+    // keep the current store as an older segment
+    auto seg = std::make_unique<HSeg>();
+    seg->row_ptr.mt = seg->col.mt = &c->mem;
+    seg->row_cnt.mt = &c->mem;
+    seg->val64.mt = seg->val32.mt = seg->res32.mt = &c->mem;
+    seg->n = H.n;
+    seg->nnz = H.nnz_current;
+    seg->packed = H.packed;
+    seg->row_ptr.swap(H.row_ptr);
+    seg->row_cnt.swap(H.row_cnt);
+    seg->col.swap(H.col);
+    seg->val64.swap(H.val64);
+    seg->val32.swap(H.val32);
+    seg->res32.swap(H.res32);
+    H.older.push_back(std::move(seg));
+  } else {
+    H.older.clear();
+  }
+  H.n_prev = n_prev;
+  H.n = n;
+  H.precision = precision;
   if (!H.join) build_index(c);
   H.row_ptr.resize(n + 1, 1.25);
   H.row_cnt.resize(n + 1, 1.25);
@@ -464,12 +497,20 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
   SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
-  // a mixed build also sums |H_ij| per det (the H*v fixed-point bound)
+  // a mixed build also sums |H_ij| per det (the H*v fixed-point bound); an incremental one
+  // adds to the sums of the older segments
   float* absacc = nullptr;
   if (precision == SHCI_PREC_MIXED) {
-    H.rowabs.resize(n, 1.1);
-    SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
+    if (n_prev) {
+      H.rowabs.grow_keep(n, s, 1.1);
+      SHCI_CUDA(cudaMemsetAsync(H.rowabs.p + n_prev, 0, (n - n_prev) * sizeof(float), s));
+    } else {
+      H.rowabs.resize(n, 1.1);
+      SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
+    }
     absacc = H.rowabs.p;
+  } else {
+    H.rowabs.release();
   }
   k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, H.diag.p);
   SHCI_LAUNCH_CHECK();
@@ -477,14 +518,14 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   uint64_t nnz = 0;
   bool one_pass = false;
   if (H.join && !two_pass) {
-    const uint64_t cap = join_row_caps(c, H.row_ptr.p);
+    const uint64_t cap = join_row_caps(c, H.row_ptr.p, static_cast<uint32_t>(n_prev));
     one_pass = static_cast<double>(cap) * 12.0 * 1.1 < 0.9 * static_cast<double>(store_room(c));
     if (one_pass) {
       alloc_store(c, precision, cap);
       {
         ProfScope ps(c->prof, s, "hbuild_fill");
         join_rows(c, fill_mode, H.row_cnt.p, H.row_ptr.p, H.col.p, H.val64.p, H.val32.p,
-                  H.res32.p, work, grid, absacc);
+                  H.res32.p, work, grid, absacc, static_cast<uint32_t>(n_prev));
       }
       c->k0.resize(n, 1.25);
       widen_u32_u64(H.row_cnt.p, c->k0.p, n, s);
@@ -497,7 +538,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
       ProfScope ps(c->prof, s, "hbuild_count");
       if (H.join) {
         join_rows(c, 0, H.row_cnt.p, nullptr, nullptr, nullptr, nullptr, nullptr, work, grid,
-                  absacc);
+                  absacc, static_cast<uint32_t>(n_prev));
       } else {
         k_hbuild<0><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                  H.row_cnt.p, nullptr, nullptr, nullptr,
@@ -514,7 +555,9 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   SHCI_CUDA(cudaMemcpyAsync(cand, work + 2, 24, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
   if (absacc) finish_mixed_bound(c);
+  H.nnz_current = nnz;
   H.nnz = nnz;
+  for (const auto& sg : H.older) H.nnz += sg->nnz;
   H.candidates = cand[0] + cand[1] + cand[2];
   for (int k = 0; k < 3; k++) H.cand_parts[k] = cand[k];
   if (H.join) {
@@ -528,7 +571,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
       ProfScope ps(c->prof, s, "hbuild_fill");
       if (H.join) {
         join_rows(c, fill_mode, nullptr, H.row_ptr.p, H.col.p, H.val64.p, H.val32.p, H.res32.p,
-                  work, grid, nullptr);
+                  work, grid, nullptr, static_cast<uint32_t>(n_prev));
       } else if (precision == SHCI_PREC_FP64) {
         k_hbuild<1><<<grid, kWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, v,
                                                  nullptr, H.row_ptr.p, H.col.p, H.val64.p,
@@ -547,6 +590,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   if (row_sort_enabled()) sort_rows(c);
   c->prof.flush();
   H.valid = true;
+  H.prefix_ok = true;
   H.build_id++;
   c->launches += 5;
   return nnz;

@@ -128,7 +128,26 @@ struct JoinView {
   const uint32_t* pairs;
   const uint64_t* span;
   const uint32_t* jdet;
+  uint32_t n_prev;  // incremental update: rows < n_prev take only members >= n_prev
 };
+
+// Members of entry sp = (position p | bucket end << 32) of row i: positions (p', end) with
+// p' = p, or, for a row built before (i < n_prev), the last position whose det precedes
+// n_prev (a bucket lists its dets in increasing id order, so the members >= n_prev follow).
+__device__ __forceinline__ uint32_t member_start(const uint32_t* __restrict__ jdet, uint64_t sp,
+                                                 uint32_t i, uint32_t n_prev) {
+  uint32_t p = static_cast<uint32_t>(sp);
+  if (i < n_prev) {
+    uint32_t lo = p + 1u, hi = static_cast<uint32_t>(sp >> 32);
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (jdet[mid] < n_prev) lo = mid + 1u;
+      else hi = mid;
+    }
+    p = lo - 1u;
+  }
+  return p;
+}
 
 // Row kernel of the join (MODE as in RowSink).  A warp per row: lanes take the row's entries
 // 32 at a time, the members after each entry are flattened over the lanes, and every member
@@ -159,7 +178,7 @@ __global__ void __launch_bounds__(kJoinWarps * 32, 5)
       uint64_t ru = 0, rd = 0;
       if (k < K) {
         const uint64_t sp = jv.span[(size_t)i * K + k];
-        p = static_cast<uint32_t>(sp);
+        p = member_start(jv.jdet, sp, i, jv.n_prev);
         len = static_cast<uint32_t>(sp >> 32) - p - 1u;
         pair_masks(jv.pairs[k], ui, di, jv.n_up, &ru, &rd);
       }
@@ -213,15 +232,15 @@ __global__ void __launch_bounds__(kJoinWarps * 32, 5)
 
 // Row capacity of a single-pass build: the candidates of row i (members after each of its
 // entries), an upper bound on the elements it keeps.
-__global__ void k_join_caps(const uint64_t* __restrict__ span, uint32_t n, uint32_t K,
-                            uint64_t* caps) {
+__global__ void k_join_caps(const uint64_t* __restrict__ span, const uint32_t* __restrict__ jdet,
+                            uint32_t n, uint32_t K, uint32_t n_prev, uint64_t* caps) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     uint64_t c = 0;
     for (uint32_t k = lane; k < K; k += 32) {
       const uint64_t sp = span[(size_t)i * K + k];
-      c += static_cast<uint32_t>(sp >> 32) - static_cast<uint32_t>(sp) - 1u;
+      c += static_cast<uint32_t>(sp >> 32) - member_start(jdet, sp, i, n_prev) - 1u;
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
@@ -339,10 +358,10 @@ bool join_prepare(shci_ctx* c) {
 
 void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
                uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
-               unsigned grid, float* absacc) {
+               unsigned grid, float* absacc, uint32_t n_prev) {
   const auto& J = c->join;
   const uint32_t n = static_cast<uint32_t>(c->up.size());
-  JoinView v{J.K, J.n_up, J.pairs.p, J.span.p, J.jdet.p};
+  JoinView v{J.K, J.n_up, J.pairs.p, J.span.p, J.jdet.p, n_prev};
   cudaStream_t s = c->stream;
   if (mode == 0)
     k_hjoin<0><<<grid, kJoinWarps * 32, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, n, v, row_cnt,
@@ -360,11 +379,12 @@ void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr
   c->launches += 1;
 }
 
-uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start) {
+uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start, uint32_t n_prev) {
   const auto& J = c->join;
   const uint32_t n = static_cast<uint32_t>(c->up.size());
   cudaStream_t s = c->stream;
-  k_join_caps<<<grid_for((size_t)n * 32, 256), 256, 0, s>>>(J.span.p, n, J.K, row_start);
+  k_join_caps<<<grid_for((size_t)n * 32, 256), 256, 0, s>>>(J.span.p, J.jdet.p, n, J.K, n_prev,
+                                                           row_start);
   SHCI_LAUNCH_CHECK();
   const uint64_t tot = exclusive_scan_u64(row_start, row_start, n, s, c->sort);
   SHCI_CUDA(cudaMemcpyAsync(row_start + n, &tot, 8, cudaMemcpyHostToDevice, s));

@@ -41,13 +41,14 @@ size_t build_hamiltonian(shci_ctx* c, int precision);
 // cannot be used for the current dets; join_rows runs one pass (mode as the row kernels;
 // every mode writes each row's kept count to row_cnt when given).
 bool join_prepare(shci_ctx* c);
+// n_prev > 0 (incremental update): rows < n_prev take only columns >= n_prev.
 void join_rows(shci_ctx* c, int mode, uint32_t* row_cnt, const uint64_t* row_ptr,
                uint32_t* col, double* v64, float* v32, float* r32, unsigned* work,
-               unsigned grid, float* absacc);
+               unsigned grid, float* absacc, uint32_t n_prev);
 void join_release(shci_ctx* c);
 // Row starts of a single-pass build: row_start[i] = sum of the candidate counts of rows < i
 // (row_start has n + 1 entries); returns the total capacity.
-uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start);
+uint64_t join_row_caps(shci_ctx* c, uint64_t* row_start, uint32_t n_prev);
 
 // rowsort.cu: sorts each row of the element store by column (tiles of 2048 elements), so
 // that H*v's scattered accesses share sectors; SHCI_ROW_SORT=0 turns the pass off.

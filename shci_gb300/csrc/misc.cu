@@ -110,49 +110,77 @@ void get_rows(shci_ctx* c, const uint64_t* rows, size_t m, uint64_t* offsets, ui
   for (size_t k = 0; k < m; k++)
     if (rows[k] >= n) throw ArgError("row index out of range");
   cudaStream_t s = c->stream;
-  std::vector<uint32_t> len(n);
-  if (n) SHCI_CUDA(cudaMemcpyAsync(len.data(), H.row_cnt.p, n * 4, cudaMemcpyDeviceToHost, s));
-  SHCI_CUDA(cudaStreamSynchronize(s));
-  offsets[0] = 0;
-  for (size_t k = 0; k < m; k++) offsets[k + 1] = offsets[k] + len[rows[k]];
-  if (!cols && !vals) return;
-  const uint64_t tot = offsets[m];
-  if (m == 0 || tot == 0) return;
-  std::vector<uint32_t> r32(rows, rows + m);
-  DevBuf<uint32_t> d_rows, o_col;
-  DevBuf<uint64_t> d_off;
-  DevBuf<double> o_val;
-  d_rows.mt = o_col.mt = &c->mem;
-  d_off.mt = &c->mem;
-  o_val.mt = &c->mem;
-  d_rows.resize(m);
-  d_off.resize(m + 1);
-  o_col.resize(tot);
-  o_val.resize(tot);
-  SHCI_CUDA(cudaMemcpyAsync(d_rows.p, r32.data(), m * 4, cudaMemcpyHostToDevice, s));
-  SHCI_CUDA(cudaMemcpyAsync(d_off.p, offsets, (m + 1) * 8, cudaMemcpyHostToDevice, s));
+  const auto segs = segments(H);
   const bool fp64 = H.precision == SHCI_PREC_FP64;
-  k_gather_rows<<<grid_for(m * 32, 256), 256, 0, s>>>(
-      H.row_ptr.p, H.row_cnt.p, d_rows.p, static_cast<uint32_t>(m), d_off.p, H.col.p,
-      fp64 ? H.val64.p : nullptr, fp64 ? nullptr : H.val32.p, fp64 ? nullptr : H.res32.p,
-      o_col.p, o_val.p);
-  SHCI_LAUNCH_CHECK();
-  std::vector<uint32_t> hc(tot);
-  std::vector<double> hv(tot);
-  SHCI_CUDA(cudaMemcpyAsync(hc.data(), o_col.p, tot * 4, cudaMemcpyDeviceToHost, s));
-  SHCI_CUDA(cudaMemcpyAsync(hv.data(), o_val.p, tot * 8, cudaMemcpyDeviceToHost, s));
-  SHCI_CUDA(cudaStreamSynchronize(s));
-  c->launches += 1;
-  // each row in increasing column order
-  std::vector<uint64_t> idx;
+  // per segment: the requested rows' lengths (rows beyond a segment's range are empty)
+  std::vector<std::vector<uint64_t>> soff(segs.size(), std::vector<uint64_t>(m + 1, 0));
+  for (size_t g = 0; g < segs.size(); g++) {
+    std::vector<uint32_t> len(segs[g].n);
+    if (segs[g].n)
+      SHCI_CUDA(cudaMemcpyAsync(len.data(), segs[g].row_cnt, segs[g].n * 4,
+                                cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < m; k++)
+      soff[g][k + 1] = soff[g][k] + (rows[k] < segs[g].n ? len[rows[k]] : 0u);
+  }
+  offsets[0] = 0;
   for (size_t k = 0; k < m; k++) {
-    const uint64_t a = offsets[k], b = offsets[k + 1];
-    idx.resize(b - a);
-    for (uint64_t t = a; t < b; t++) idx[t - a] = t;
-    std::sort(idx.begin(), idx.end(), [&](uint64_t x, uint64_t y) { return hc[x] < hc[y]; });
-    for (uint64_t t = a; t < b; t++) {
-      if (cols) cols[t] = hc[idx[t - a]];
-      if (vals) vals[t] = hv[idx[t - a]];
+    uint64_t l = 0;
+    for (size_t g = 0; g < segs.size(); g++) l += soff[g][k + 1] - soff[g][k];
+    offsets[k + 1] = offsets[k] + l;
+  }
+  if (!cols && !vals) return;
+  if (m == 0 || offsets[m] == 0) return;
+  // gather each segment's part of the rows, then merge per row in increasing column order
+  std::vector<std::vector<uint32_t>> hc(segs.size());
+  std::vector<std::vector<double>> hv(segs.size());
+  for (size_t g = 0; g < segs.size(); g++) {
+    const uint64_t tot = soff[g][m];
+    if (tot == 0) continue;
+    std::vector<uint32_t> r32;
+    std::vector<uint64_t> o;
+    for (size_t k = 0; k < m; k++)
+      if (rows[k] < segs[g].n) {
+        r32.push_back(static_cast<uint32_t>(rows[k]));
+        o.push_back(soff[g][k]);
+      }
+    o.push_back(tot);
+    DevBuf<uint32_t> d_rows, o_col;
+    DevBuf<uint64_t> d_off;
+    DevBuf<double> o_val;
+    d_rows.mt = o_col.mt = &c->mem;
+    d_off.mt = &c->mem;
+    o_val.mt = &c->mem;
+    d_rows.resize(r32.size());
+    d_off.resize(o.size());
+    o_col.resize(tot);
+    o_val.resize(tot);
+    SHCI_CUDA(cudaMemcpyAsync(d_rows.p, r32.data(), r32.size() * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_off.p, o.data(), o.size() * 8, cudaMemcpyHostToDevice, s));
+    k_gather_rows<<<grid_for(r32.size() * 32, 256), 256, 0, s>>>(
+        segs[g].row_ptr, segs[g].row_cnt, d_rows.p, static_cast<uint32_t>(r32.size()), d_off.p,
+        segs[g].col, fp64 ? segs[g].val64 : nullptr, fp64 ? nullptr : segs[g].val32,
+        fp64 ? nullptr : segs[g].res32, o_col.p, o_val.p);
+    SHCI_LAUNCH_CHECK();
+    hc[g].resize(tot);
+    hv[g].resize(tot);
+    SHCI_CUDA(cudaMemcpyAsync(hc[g].data(), o_col.p, tot * 4, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaMemcpyAsync(hv[g].data(), o_val.p, tot * 8, cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    c->launches += 1;
+  }
+  std::vector<std::pair<uint32_t, double>> row;
+  for (size_t k = 0; k < m; k++) {
+    row.clear();
+    for (size_t g = 0; g < segs.size(); g++)
+      for (uint64_t t = soff[g][k]; t < soff[g][k + 1]; t++) row.emplace_back(hc[g][t], hv[g][t]);
+    std::sort(row.begin(), row.end(),
+              [](const std::pair<uint32_t, double>& a, const std::pair<uint32_t, double>& b) {
+                return a.first < b.first;
+              });
+    for (size_t t = 0; t < row.size(); t++) {
+      if (cols) cols[offsets[k] + t] = row[t].first;
+      if (vals) vals[offsets[k] + t] = row[t].second;
     }
   }
 }

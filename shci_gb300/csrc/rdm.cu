@@ -264,13 +264,13 @@ __device__ void rdm2_elements(uint64_t cu, uint64_t cd, uint64_t tu, uint64_t td
 __global__ void __launch_bounds__(256)
     k_rdm2(const uint64_t* up, const uint64_t* dn, const double* coef, uint32_t n_dets,
            const uint64_t* row_ptr, const uint32_t* row_len, const uint32_t* col, int n,
-           double* half) {
+           bool with_diag, double* half) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_dets; i += warps) {
     const uint64_t tu = up[i], td = dn[i];
     const double ci = coef[i];
-    if (lane == 0) rdm2_elements(tu, td, tu, td, Rdm2Writer{half, n, ci * ci});
+    if (with_diag && lane == 0) rdm2_elements(tu, td, tu, td, Rdm2Writer{half, n, ci * ci});
     for (uint64_t k = row_ptr[i] + lane; k < row_ptr[i] + row_len[i]; k += 32) {
       const uint32_t j = col[k];
       rdm2_elements(up[j], dn[j], tu, td, Rdm2Writer{half, n, ci * coef[j]});
@@ -348,10 +348,16 @@ void rdm2(shci_ctx* c, double* out_half) {
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   {
     ProfScope ps(c->prof, s, "rdm2");
-    k_rdm2<<<static_cast<unsigned>(sms) * 8u, 256, 0, s>>>(c->d_up.p, c->d_dn.p, c->d_coef.p,
-                                                           (uint32_t)H.n, H.row_ptr.p, H.row_cnt.p, H.col.p, n,
-                                                           half.p);
-    SHCI_LAUNCH_CHECK();
+    const auto segs = segments(H);
+    for (size_t k = 0; k < segs.size(); k++) {
+      const SegView& g = segs[k];
+      // diagonal terms once, with the current segment (which covers every row)
+      k_rdm2<<<static_cast<unsigned>(sms) * 8u, 256, 0, s>>>(
+          c->d_up.p, c->d_dn.p, c->d_coef.p, (uint32_t)g.n, g.row_ptr, g.row_cnt, g.col, n,
+          k + 1 == segs.size(), half.p);
+      SHCI_LAUNCH_CHECK();
+      c->launches += 1;
+    }
   }
   SHCI_CUDA(cudaMemcpyAsync(out_half, half.p, size * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));

@@ -309,7 +309,7 @@ bool row_sort_enabled() {
 void sort_rows(shci_ctx* c) {
   auto& H = c->H;
   const uint32_t n = static_cast<uint32_t>(H.n);
-  if (n == 0 || H.nnz == 0) return;
+  if (n == 0 || H.nnz_current == 0) return;
   cudaStream_t s = c->stream;
   int dev_sms = 0, per_sm = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    if (lane == 0) atomicAdd(&y[i], acc + diag[i] * xi);
+    if (lane == 0) atomicAdd(&y[i], diag ? acc + diag[i] * xi : acc);
   }
 }
 
@@ -208,7 +208,7 @@ __global__ void k_fix_out(const unsigned long long* __restrict__ yfix,
 }  // namespace
 
 // H.scal[0] = bound on max_i sum_j |H_ij| from the off-diagonal sums in H.rowabs and the
-// diagonal; releases H.rowabs.
+// diagonal; H.rowabs stays (an incremental update adds to it).
 void finish_mixed_bound(shci_ctx* c) {
   auto& H = c->H;
   cudaStream_t s = c->stream;
@@ -227,7 +227,6 @@ void finish_mixed_bound(shci_ctx* c) {
   const double bound = 1.05 * static_cast<double>(fm) + 1e-300;
   SHCI_CUDA(cudaMemcpyAsync(H.scal.p, &bound, 8, cudaMemcpyHostToDevice, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
-  H.rowabs.release();
   H.bound_valid = true;
   c->launches += 1;
 }
@@ -241,14 +240,16 @@ void mixed_bound(shci_ctx* c, unsigned grid) {
   const uint32_t n = static_cast<uint32_t>(H.n);
   H.rowabs.resize(n, 1.1);
   SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, (size_t)n * 4, s));
-  k_rowabs<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, H.res32.p, H.diag.p,
-                                      H.rowabs.p, n);
-  SHCI_LAUNCH_CHECK();
-  c->launches += 1;
+  for (const SegView& g : segments(H)) {
+    k_rowabs<true><<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.val32, g.res32, H.diag.p,
+                                        H.rowabs.p, static_cast<uint32_t>(g.n));
+    SHCI_LAUNCH_CHECK();
+    c->launches += 1;
+  }
   finish_mixed_bound(c);
 }
 
-// t_i = sum over row i's stored elements of residual_ij * w_j (no atomics: the FP64 energy
+// t_i += sum over row i's stored elements of residual_ij * w_j (no atomics: the FP64 energy
 // correction needs only w^T R w = 2 sum_i w_i t_i of the residual store R).  w comes split
 // into float pairs and the products and sums are float pairs, as in the mixed H*v (about
 // 2^-44 relative): the FP64 form spent two FP64 operations per element (conversion and FMA),
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(256)
       ah = s2;
       al = al + bl + se;
     }
-    if (lane == 0) t[i] = static_cast<double>(ah) + static_cast<double>(al);
+    if (lane == 0) t[i] += static_cast<double>(ah) + static_cast<double>(al);
   }
 }
 
@@ -299,9 +300,14 @@ void residual_rows(shci_ctx* c, const double* w, double* t) {
   k_split_x<<<grid_for(n, 256), 256, 0, s>>>(w, n, ws,
                                              reinterpret_cast<unsigned long long*>(H.scal.p + 1));
   SHCI_LAUNCH_CHECK();
-  k_res_rows<<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.res32.p, ws, t, n);
-  SHCI_LAUNCH_CHECK();
-  c->launches += 2;
+  SHCI_CUDA(cudaMemsetAsync(t, 0, (size_t)n * 8, s));
+  for (const SegView& g : segments(H)) {
+    k_res_rows<<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.res32, ws, t,
+                                    static_cast<uint32_t>(g.n));
+    SHCI_LAUNCH_CHECK();
+    c->launches += 1;
+  }
+  c->launches += 1;
 }
 
 void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
@@ -315,9 +321,16 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   if (H.precision == SHCI_PREC_FP64) {
     ProfScope ps(c->prof, s, "spmv");
     SHCI_CUDA(cudaMemsetAsync(y, 0, H.n * sizeof(double), s));
-    k_spmv<<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val64.p, H.diag.p, x, y, n);
-    SHCI_LAUNCH_CHECK();
-    c->launches += 1;
+    const auto segs = segments(H);
+    for (size_t k = 0; k < segs.size(); k++) {
+      const SegView& g = segs[k];
+      // the diagonal goes in with the current segment, which covers every row
+      k_spmv<<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.val64,
+                                  k + 1 == segs.size() ? H.diag.p : nullptr, x, y,
+                                  static_cast<uint32_t>(g.n));
+      SHCI_LAUNCH_CHECK();
+      c->launches += 1;
+    }
     return;
   }
   if (!H.bound_valid) mixed_bound(c, grid);
@@ -330,16 +343,20 @@ void spmv(shci_ctx* c, const double* x, double* y, bool residual) {
   k_split_x<<<grid_for(n, 256), 256, 0, s>>>(
       x, n, xs, reinterpret_cast<unsigned long long*>(H.scal.p + 1));
   SHCI_LAUNCH_CHECK();
-  if (residual)
-    k_spmv_fix<true><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, H.res32.p, xs,
-                                           H.scal.p, H.yfix.p, n);
-  else
-    k_spmv_fix<false><<<grid, 256, 0, s>>>(H.row_ptr.p, H.row_cnt.p, H.col.p, H.val32.p, nullptr, xs,
-                                            H.scal.p, H.yfix.p, n);
-  SHCI_LAUNCH_CHECK();
+  for (const SegView& g : segments(H)) {
+    const uint32_t gn = static_cast<uint32_t>(g.n);
+    if (residual)
+      k_spmv_fix<true><<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.val32, g.res32, xs,
+                                             H.scal.p, H.yfix.p, gn);
+    else
+      k_spmv_fix<false><<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.val32, nullptr, xs,
+                                              H.scal.p, H.yfix.p, gn);
+    SHCI_LAUNCH_CHECK();
+    c->launches += 1;
+  }
   k_fix_out<<<grid_for(n, 256), 256, 0, s>>>(H.yfix.p, H.diag.p, x, H.scal.p, y, n);
   SHCI_LAUNCH_CHECK();
-  c->launches += 3;
+  c->launches += 2;
 }
 
 }  // namespace shci
