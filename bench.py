@@ -264,7 +264,7 @@ def run_pt2_timed(ctx, stream, e_var, warmup, steps):
     return out
 
 
-def parity_n40(fcidump, w, up, dn, ctx, rows_mixed):
+def parity_n40(fcidump, w, up, dn):
     """The oracle's own selection schedule on the CPU gives the step's det list independently;
     it must equal the device's bit for bit.  The oracle's rows of a strided sample (the CPU
     baseline's) must equal the device store's rows: columns exactly, FP64 values exactly for
@@ -340,11 +340,14 @@ def run_converged(fcidump, w, device, warmup, steps):
         step()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.profile(True)
     ev0.record(stream)
     for _ in range(steps):
         e_step = step()
     ev1.record(stream)
     torch.cuda.synchronize()
+    prof = ctx.profile_get()
+    ctx.profile(False)
     st = ctx.hamiltonian_stats()
     peak = ctx.memory_stats()[1]
     ctx.close()
@@ -352,7 +355,9 @@ def run_converged(fcidump, w, device, warmup, steps):
             "iterations": [{"n_dets": int(a), "nnz_sym": int(b), "energy": float(c)}
                            for a, b, c in zip(nd, nz, en)],
             "n_dets": n, "nnz_upper": st["nnz"], "ms_per_step": ev0.elapsed_time(ev1) / steps,
-            "steps": steps, "warmup": warmup, "energy_step": e_step, "peak_device_bytes": peak}
+            "steps": steps, "warmup": warmup, "energy_step": e_step, "peak_device_bytes": peak,
+            "build": {"one_pass": st.get("one_pass"), "path": st["path"]},
+            "stage_ms_per_step": {k: round(v[0] / steps, 2) for k, v in prof.items()}}
 
 
 def run_small_configs(data_dir, device, repeats=3):
@@ -527,6 +532,12 @@ def run_ours(args):
             e2e_ms.append((tb - ta) * 1e3)
     e2e = statistics.median(e2e_ms)
     rows_mixed = ctx.hamiltonian_rows(sample) if args.parity else None
+    # the whole variational stage, and the step on its converged det list (after the headline
+    # context has released its memory, before the host-side oracle work)
+    converged = None
+    if args.converged:
+        ctx.close()
+        converged = run_converged(fcidump, w, local, 1, args.steps)
 
     if rank != 0:
         return
@@ -582,7 +593,7 @@ def run_ours(args):
         _, cpu = cpu_sample(fcidump, w, up, dn, keep=keep)
     parity = None
     if args.parity:
-        parity = parity_n40(fcidump, w, up, dn, ctx, rows_mixed)
+        parity = parity_n40(fcidump, w, up, dn)
         o_rows = keep["rows"]
         parity["sample_rows"] = int(len(sample))
         parity["sample_elements"] = int(len(o_rows[2]))
@@ -594,12 +605,6 @@ def run_ours(args):
     if args.no_cpu_baseline:
         cpu = None
     small = run_small_configs(args.data, local) if args.small else None
-    # the whole variational stage, and the step on its converged det list (after the headline
-    # context has released its memory)
-    converged = None
-    if args.converged:
-        ctx.close()
-        converged = run_converged(fcidump, w, local, 1, args.steps)
     pt2_total = None
     if pt2 and pt2_fp64 and "error" not in pt2 and "error" not in pt2_fp64:
         pt2_total = {"energy_total_mixed": e_mixed + pt2["correction"],

@@ -159,6 +159,10 @@ struct shci_ctx {
   bool have_integrals = false;
   shci::HostIntegrals I;
   shci::DevBuf<double> h1, g2, dtab, xtab, jtab, ktab;
+  // PT2 diagonals in 64-bit fixed point (pt2.cu): h_oo, J - K (same spin), J (opposite spin)
+  shci::DevBuf<long long> dfix;
+  int dfix_scale = 0;
+  bool dfix_valid = false;
   shci::DevIntegrals dI{};
   double energy_hf = 0.0;
 

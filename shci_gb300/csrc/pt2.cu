@@ -249,13 +249,50 @@ __global__ void __launch_bounds__(kPtWarps * 32, 4)
   }
 }
 
+// Diagonal H_aa of the PT dets in 64-bit fixed point.  The diagonal is a sum of about
+// n_e^2 / 2 table entries (h_pp, J - K for same-spin pairs, J for opposite-spin pairs,
+// chem_system.cc:495-542); on GB300 the FP64 pipe retires about two operations per SM cycle,
+// so ~300 FP64 additions per PT det made the contribution kernel FP64-bound.  Here every
+// entry is rounded once to a multiple of 2^-s (s chosen so that no sum can reach 2^62) and the
+// sum is an exact integer sum on the integer pipe: |error| <= (number of terms) * 2^-(s+1),
+// about 1e-13 Ha at n = 40 (s = 51), where the FP64 sum carries a comparable rounding error.
+struct DiagFix {
+  const long long* tab;  // [n] h_pp, [n*n] J - K, [n*n] J
+  int n;
+  double inv_scale;      // 2^-s
+  double e_core;
+};
+
+__device__ __forceinline__ double h_diag_fix(const DiagFix& F, uint64_t up, uint64_t dn) {
+  const int n = F.n;
+  const long long* h1 = F.tab;
+  const long long* jk = F.tab + n;
+  const long long* jj = F.tab + n + n * n;
+  long long acc = 0;
+  for (uint64_t m = up; m; m &= m - 1) {
+    const int a = ctz64(m);
+    acc += __ldg(h1 + a);
+    const long long* row = jk + a * n;
+    for (uint64_t m2 = m & (m - 1); m2; m2 &= m2 - 1) acc += __ldg(row + ctz64(m2));
+    const long long* row2 = jj + a * n;
+    for (uint64_t m3 = dn; m3; m3 &= m3 - 1) acc += __ldg(row2 + ctz64(m3));
+  }
+  for (uint64_t m = dn; m; m &= m - 1) {
+    const int a = ctz64(m);
+    acc += __ldg(h1 + a);
+    const long long* row = jk + a * n;
+    for (uint64_t m2 = m & (m - 1); m2; m2 &= m2 - 1) acc += __ldg(row + ctz64(m2));
+  }
+  return static_cast<double>(acc) * F.inv_scale + F.e_core;
+}
+
 // x[k] = contribution of unique PT det k (mapper of solver.h:727-732, 856-862, 1117-1124)
 template <int MODE>
-__global__ void k_pt_x(DevIntegrals I, const uint64_t* au, const uint64_t* ad, OutCols S,
+__global__ void k_pt_x(DiagFix D, const uint64_t* au, const uint64_t* ad, OutCols S,
                        size_t m, double e_var, double n_batches, uint64_t orb_mask, double* x) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m;
        k += (size_t)gridDim.x * blockDim.x) {
-    const double haa = h_diag(I, au[k] & orb_mask, ad[k]);
+    const double haa = h_diag_fix(D, au[k] & orb_mask, ad[k]);
     double v;
     if (MODE == kDtm) {
       v = S.v[0][k] * S.v[0][k] / (e_var - haa);
@@ -383,6 +420,38 @@ __global__ void k_iter_starts(const uint64_t* au, size_t m, int shift, uint32_t 
     else hi = mid;
   }
   starts[it] = lo;
+}
+
+// Fixed-point diagonal tables of the context's integrals (built once per set of integrals).
+DiagFix diag_fix(shci_ctx* c) {
+  const auto& I = c->I;
+  const int n = static_cast<int>(I.n);
+  if (!c->dfix_valid) {
+    std::vector<double> v(n + 2 * (size_t)n * n, 0.0);
+    for (int p = 0; p < n; p++) v[p] = I.h(p, p);
+    for (int a = 0; a < n; a++)
+      for (int b = 0; b < n; b++) {
+        const double J = I.g(a, a, b, b), K = I.g(a, b, b, a);
+        v[n + (size_t)a * n + b] = J - K;
+        v[n + (size_t)n * n + (size_t)a * n + b] = J;
+      }
+    double mx = 0.0;
+    for (double x : v) mx = std::max(mx, std::fabs(x));
+    const int n_e = static_cast<int>(I.n_up + I.n_dn);
+    const double bound = (static_cast<double>(n_e) + static_cast<double>(n_e) * n_e) * mx;
+    int s = 60;
+    while (s > 0 && bound * std::ldexp(1.0, s) >= std::ldexp(1.0, 62)) s--;
+    std::vector<long long> t(v.size());
+    for (size_t k = 0; k < v.size(); k++) t[k] = std::llround(std::ldexp(v[k], s));
+    c->dfix.mt = &c->mem;
+    c->dfix.resize(t.size());
+    SHCI_CUDA(cudaMemcpyAsync(c->dfix.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice,
+                              c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    c->dfix_scale = s;
+    c->dfix_valid = true;
+  }
+  return DiagFix{c->dfix.p, n, std::ldexp(1.0, -c->dfix_scale), I.e_core};
 }
 
 struct PtSetup {
@@ -601,8 +670,8 @@ void pt_batch_sums(shci_ctx* c, DevBuf<uint64_t>& bu, DevBuf<uint64_t>& bd, DevB
   for (int v = 0; v < n_cols<MODE>(); v++) oc.v[v] = bv[v].p;
   {
     ProfScope ps(c->prof, s, "pt2_contrib");
-    k_pt_x<MODE><<<grid_for(bn, 256), 256, 0, s>>>(c->dI, bu.p, bd.p, oc, bn, e_var, 1.0, ~0ull,
-                                                   x.p);
+    k_pt_x<MODE><<<grid_for(bn, 256), 256, 0, s>>>(diag_fix(c), bu.p, bd.p, oc, bn, e_var, 1.0,
+                                                   ~0ull, x.p);
     SHCI_LAUNCH_CHECK();
     const uint64_t st2[2] = {0, bn};
     SHCI_CUDA(cudaMemcpyAsync(starts.p, st2, 16, cudaMemcpyHostToDevice, s));
@@ -1002,8 +1071,9 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
       const uint64_t mask = shift == 64 ? ~0ull : ((1ull << shift) - 1ull);
       {
         ProfScope ps(c->prof, s, "pt2_contrib");
-        k_pt_x<kSto><<<grid_for(bn, 256), 256, 0, s>>>(c->dI, bu.p, bd.p, oc, bn, energy_var,
-                                                       static_cast<double>(n_batches), mask, x.p);
+        k_pt_x<kSto><<<grid_for(bn, 256), 256, 0, s>>>(diag_fix(c), bu.p, bd.p, oc, bn,
+                                                       energy_var, static_cast<double>(n_batches),
+                                                       mask, x.p);
         SHCI_LAUNCH_CHECK();
         k_iter_starts<<<1, 128, 0, s>>>(bu.p, bn, shift, n_it, starts.p);
         SHCI_LAUNCH_CHECK();
