@@ -266,10 +266,7 @@ def run_pt2_timed(ctx, stream, e_var, warmup, steps):
 
 def parity_n40(fcidump, w, up, dn):
     """The oracle's own selection schedule on the CPU gives the step's det list independently;
-    it must equal the device's bit for bit.  The oracle's rows of a strided sample (the CPU
-    baseline's) must equal the device store's rows: columns exactly, FP64 values exactly for
-    the FP64 build (rows_fp64) and, for the mixed build (rows_mixed), the FP32 value and FP32
-    residual of the oracle's FP64 value."""
+    it must equal the device's bit for bit (the sampled rows are compared by compare_rows)."""
     import numpy as np
     from oracle.oracle import Oracle
     t0 = time.time()
