@@ -14,6 +14,13 @@ Ritz vector (a pass over the FP32 residual store).  value = device seconds per s
 (inputs resident in HBM); e2e = the same through the public API with the det list and start
 vector copied from pinned host memory each step and the energy read back.
 
+Also in the line: the three PT2 stages on the step's wavefunction, timed over the same
+warm-up and step counts (`pt2`), the all-FP64 step and its PT2 (`fp64`,
+`pt2_fp64_wavefunction`, `totals`), the whole variational stage to the converged eps_var =
+2e-5 space and a step on it (`converged`), the oracle checks (`parity`: the oracle's own det
+list and sampled rows), full device and oracle runs of the n = 16 and n = 26 configurations
+(`small_configs`) and the 256-instance batched workload (`batched`).
+
 --impl reference times the CPU restatement of the reference's algorithm (oracle/) on a
 strided sample of the same step's rows with every host thread, scaled to the full step.
 """
@@ -654,8 +661,8 @@ def main():
                     help="skip the full device and oracle runs of the two small configurations")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the oracle checks (independent det list, sampled rows)")
-    ap.add_argument("--batched", action="store_true",
-                    help="also time workload 5 (256 small instances, concurrent batch runner)")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip workload 5 (256 small instances, concurrent batch runner)")
     args = ap.parse_args()
     global WORKLOAD, SCHEDULE, EPS_VAR
     WORKLOAD = args.workload
