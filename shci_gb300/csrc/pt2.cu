@@ -869,10 +869,11 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   // probabilities and their running sums (solver.h:921-933)
   double sum_w = 0.0;
   for (size_t i = 0; i < n_var; i++) sum_w += std::abs(coefs[i]);
-  std::vector<double> probs(n_var), cum(n_var);
-  for (size_t i = 0; i < n_var; i++) {
-    probs[i] = std::abs(coefs[i]) / sum_w;
-    cum[i] = i > 0 ? probs[i] + cum[i - 1] : probs[i];
+  std::vector<double> probs(n_var), cum;
+  for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(coefs[i]) / sum_w;
+  if (n_dets_in_sample == 0) {  // the pilot draws by inverse CDF
+    cum.resize(n_var);
+    for (size_t i = 0; i < n_var; i++) cum[i] = i > 0 ? probs[i] + cum[i - 1] : probs[i];
   }
   std::default_random_engine gen(random_seed);
   std::uniform_real_distribution<double> ur(0., 1.);
@@ -989,17 +990,24 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
         // sample counts per det, and the dets in order of first draw (the reference's
         // unordered_map counts and insertion-ordered list); cnt is cleared after use.
         // The draws come first, in the reference's order; the alias lookups, independent of
-        // one another, then run as one loop whose cache misses overlap.
+        // one another, then run as one loop whose cache misses overlap, with the table entries
+        // of a later draw prefetched (the tables are far larger than the host caches).
+        constexpr size_t kAhead = 32;
         for (size_t k = 0; k < n_draw; k++) {
           r1s[k] = ui_var(gen);
           r2s[k] = ur(gen);
         }
         for (size_t k = 0; k < n_draw; k++) {
+          if (k + kAhead < n_draw) {
+            __builtin_prefetch(&aprob[r1s[k + kAhead]]);
+            __builtin_prefetch(&alias[r1s[k + kAhead]]);
+          }
           const size_t r1 = r1s[k];
           ids[k] = static_cast<uint32_t>(r2s[k] < aprob[r1] ? r1 : alias[r1]);
         }
         std::vector<size_t> list;
         for (size_t k = 0; k < n_draw; k++) {
+          if (k + kAhead < n_draw) __builtin_prefetch(&cnt[ids[k + kAhead]], 1);
           const uint32_t id = ids[k];
           if (cnt[id]++ == 0) list.push_back(id);
         }
