@@ -52,7 +52,10 @@ struct PtParams {
   int pilot;         // sto: sample-size pilot (only single excitations face the |H c| test)
 };
 
-// Stochastic sources: entry k = (det, iteration, count, weight, batch, deterministic?)
+// Stochastic sources: entry e = (det, iteration, count, weight, batch, deterministic?).  With
+// ent_off, source m groups the entries [ent_off[m], ent_off[m+1]) of one det (its draws in the
+// iterations of one device pass): the det's window is walked and each candidate hashed once,
+// then tested against every entry's batch.  Without it, source m is entry m.
 struct StoSources {
   const uint32_t* det;
   const uint32_t* iter;
@@ -60,15 +63,23 @@ struct StoSources {
   const double* weight;
   const uint32_t* batch;
   const uint8_t* is_dtm;
-  const uint32_t* remap;  // optional: launch source k' is source remap[k'] (re-runs)
+  const uint32_t* remap;    // optional: launch source k' is source remap[k'] (re-runs)
+  const uint32_t* ent_off;  // optional: entries of each source
 };
 
 __device__ __forceinline__ uint32_t src_index(const StoSources& S, uint32_t k) {
   return S.remap ? S.remap[k] : k;
 }
 
+__device__ __forceinline__ uint32_t ent_begin(const StoSources& S, uint32_t k) {
+  return S.ent_off ? S.ent_off[k] : k;
+}
+__device__ __forceinline__ uint32_t ent_end(const StoSources& S, uint32_t k) {
+  return S.ent_off ? S.ent_off[k + 1] : k + 1;
+}
+
 __device__ __forceinline__ uint32_t src_det(const StoSources& S, uint32_t k, int mode) {
-  return mode == kSto ? S.det[k] : k;
+  return mode == kSto ? S.det[ent_begin(S, k)] : k;
 }
 
 // h % n_batches exactly, without a 64-bit division: a mask for powers of two, else the
@@ -125,6 +136,15 @@ __global__ void __launch_bounds__(kPtWarps * 32, 4)
         for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(kFull, cc, o);
         tot += cc;
       }
+    } else if (MODE == kSto) {
+      // every entry of the source whose batch the candidate falls in
+      const uint32_t e0 = ent_begin(S, kk), e1 = ent_end(S, kk);
+      pt_walk(P, up, dn, eps_min, eps_max, [&](bool, bool ok, uint64_t cu, uint64_t cd) {
+        const uint64_t b = ok ? batch_of(Q, rehash(det_hash(cu, cd))) : ~0ull;
+        uint32_t m = 0;
+        for (uint32_t e = e0; e < e1; e++) m += b == S.batch[e] ? 1u : 0u;
+        tot += __reduce_add_sync(kFull, m);
+      });
     } else {
       const uint64_t batch = src_batch(Q, S, kk, MODE);
       pt_walk(P, up, dn, eps_min, eps_max, [&](bool, bool ok, uint64_t cu, uint64_t cd) {
@@ -143,16 +163,22 @@ constexpr uint32_t kPtQ = 64;  // per-warp queue of batch members (< 32 waiting 
 struct PtQueue {
   uint64_t u[kPtQ];
   uint64_t d[kPtQ];
+  uint64_t pos[kPtQ];  // output slot of the member
+  uint32_t src[kPtQ];  // its source (launch-relative index k - k_begin)
+  uint8_t ent[kPtQ];   // stochastic stage: its entry within the source
 };
 
 // Emits the batch members of each source into its region [off[k], off[k + 1]) (one batch:
-// every index entry of the window, as counted by slot ranges).  Members wait in a per-warp
-// queue and are finished 32 at a time (variational-set test, H_ai c_i, the value columns), so
-// the set search and the FP64 element run with full warps; slots of members rejected there,
-// of entries that make no valid candidate, and the unused tail of the region are written
-// invalid.  Members keep their walk order.  A region may be sized by an estimate (several
-// batches): when the members do not fit, the whole region is written invalid and
-// overflow[k] is set, and the caller emits that source again with an exact count.
+// every index entry of the window, as counted by slot ranges).  A warp walks its sources one
+// after the other; members wait in a per-warp queue that carries them across sources (with
+// their source and output slot) and are finished 32 at a time (variational-set test,
+// H_ai c_i, the value columns), so the set search and the FP64 element run with full warps
+// even when most sources have only a few members.  Slots of members rejected there, of
+// entries that make no valid candidate, and the unused tail of a region are written invalid.
+// Members keep their walk order within their source's region.  A region may be sized by an
+// estimate (several batches): when the members do not fit, the queue is drained, the whole
+// region is written invalid and overflow[k] is set, and the caller emits that source again
+// with an exact count.
 template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32, 4)
     k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
@@ -163,90 +189,117 @@ __global__ void __launch_bounds__(kPtWarps * 32, 4)
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t wpg = gridDim.x * kPtWarps;
+  uint32_t qh = 0, qn = 0;  // warp-uniform ring state, kept across sources
+  auto drain = [&](uint32_t m) {
+    __syncwarp();
+    if (lane < m) {
+      const uint32_t sl = (qh + lane) & (kPtQ - 1);
+      const uint64_t cu = q.u[sl], cd = q.d[sl], pos = q.pos[sl];
+      const uint32_t kk = src_index(S, k_begin + q.src[sl]);
+      const uint32_t i = src_det(S, kk, MODE);
+      const uint64_t up = P.up[i], dn = P.dn[i];
+      const double coef = P.coef[i];
+      double count = 1.0, weight = 1.0;
+      bool dtm_src = true;
+      uint64_t iter_tag = 0;
+      if (MODE == kSto) {
+        const uint32_t e = ent_begin(S, kk) + q.ent[sl];
+        dtm_src = S.is_dtm[e] != 0;
+        count = dtm_src ? 1.0 : S.count[e];
+        weight = dtm_src ? 1.0 : S.weight[e];
+        iter_tag = static_cast<uint64_t>(S.iter[e]) << Q.iter_shift;
+      }
+      // handler order of solver.h:703-713: batch (done), variational set, |H_ai c_i|
+      bool ok = cu != kInvalid && !in_set(P, cu, cd);
+      double hc = 0.0;
+      // the pilot's handler tests |H_ai c_i| for single excitations only (solver.h:958-962)
+      const bool test = MODE != kSto || !Q.pilot || popc64(up ^ cu) + popc64(dn ^ cd) == 2;
+      if (ok && test) {
+        hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
+        if (fabs(hc) < Q.eps) ok = false;
+      }
+      out_up[pos] = ok ? (cu | iter_tag) : kInvalid;
+      out_dn[pos] = ok ? cd : kInvalid;
+      if (MODE == kDtm) {
+        out.v[0][pos] = hc;
+      } else if (MODE == kPsto) {
+        out.v[0][pos] = hc;
+        out.v[1][pos] = fabs(hc) >= Q.eps_dtm ? hc : 0.0;
+      } else {
+        // solver.h:1093-1103
+        const double x = count * hc / weight;
+        const bool above = fabs(hc) > Q.eps_psto;
+        double v2 = 0.0, v3 = 0.0, v4 = 0.0;
+        if (!dtm_src) {
+          v2 = count * hc / weight * sqrt(Q.factor);
+          if (above) v3 = v2;
+          else v4 = x * x * (1. - weight / count + Q.factor);
+        }
+        out.v[0][pos] = x;
+        out.v[1][pos] = above ? x : 0.0;
+        out.v[2][pos] = v2;
+        out.v[3][pos] = v3;
+        out.v[4][pos] = v4;
+      }
+    }
+    __syncwarp();
+    qh += m;
+    qn -= m;
+  };
   for (uint32_t k = k_begin + blockIdx.x * kPtWarps + (threadIdx.x >> 5); k < k_end; k += wpg) {
+    const uint32_t kl = k - k_begin;
     const uint32_t kk = src_index(S, k);
     const uint32_t i = src_det(S, kk, MODE);
-    const double coef = P.coef[i];
-    const double ac = fabs(coef);
+    const double ac = fabs(P.coef[i]);
     const double eps_min = Q.eps / ac;
     const double eps_max = 1.0e100 / ac;
     const uint64_t up = P.up[i], dn = P.dn[i];
-    const uint64_t batch = src_batch(Q, S, kk, MODE);
-    double count = 1.0, weight = 1.0;
-    bool dtm_src = true;
-    uint64_t iter_tag = 0;
-    if (MODE == kSto) {
-      dtm_src = S.is_dtm[kk] != 0;
-      count = dtm_src ? 1.0 : S.count[kk];
-      weight = dtm_src ? 1.0 : S.weight[kk];
-      iter_tag = static_cast<uint64_t>(S.iter[kk]) << Q.iter_shift;
-    }
-    const uint64_t start = off[k - k_begin], limit = off[k - k_begin + 1];
-    uint64_t base = start;
+    const uint64_t batch = MODE == kSto ? 0 : src_batch(Q, S, kk, MODE);
+    const uint32_t e0 = MODE == kSto ? ent_begin(S, kk) : 0u;
+    const uint32_t e1 = MODE == kSto ? ent_end(S, kk) : 1u;
+    const uint64_t start = off[kl], limit = off[kl + 1];
+    uint64_t cnt = 0;   // members of this source so far (warp-uniform)
     bool over = false;  // warp-uniform
-    uint32_t qh = 0, qn = 0;
-    auto drain = [&](uint32_t m) {
-      __syncwarp();
-      if (base + m > limit) over = true;
-      if (lane < m && !over) {
-        const uint32_t sl = (qh + lane) & (kPtQ - 1);
-        const uint64_t cu = q.u[sl], cd = q.d[sl];
-        // handler order of solver.h:703-713: batch (done), variational set, |H_ai c_i|
-        bool ok = cu != kInvalid && !in_set(P, cu, cd);
-        double hc = 0.0;
-        // the pilot's handler tests |H_ai c_i| for single excitations only (solver.h:958-962)
-        const bool test = MODE != kSto || !Q.pilot ||
-                          popc64(up ^ cu) + popc64(dn ^ cd) == 2;
-        if (ok && test) {
-          hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
-          if (fabs(hc) < Q.eps) ok = false;
-        }
-        const uint64_t pos = base + lane;
-        out_up[pos] = ok ? (cu | iter_tag) : kInvalid;
-        out_dn[pos] = ok ? cd : kInvalid;
-        if (MODE == kDtm) {
-          out.v[0][pos] = hc;
-        } else if (MODE == kPsto) {
-          out.v[0][pos] = hc;
-          out.v[1][pos] = fabs(hc) >= Q.eps_dtm ? hc : 0.0;
-        } else {
-          // solver.h:1093-1103
-          const double x = count * hc / weight;
-          const bool above = fabs(hc) > Q.eps_psto;
-          double v2 = 0.0, v3 = 0.0, v4 = 0.0;
-          if (!dtm_src) {
-            v2 = count * hc / weight * sqrt(Q.factor);
-            if (above) v3 = v2;
-            else v4 = x * x * (1. - weight / count + Q.factor);
-          }
-          out.v[0][pos] = x;
-          out.v[1][pos] = above ? x : 0.0;
-          out.v[2][pos] = v2;
-          out.v[3][pos] = v3;
-          out.v[4][pos] = v4;
-        }
-      }
-      __syncwarp();
-      qh += m;
-      qn -= m;
-      base += m;
-    };
-    pt_walk(P, up, dn, eps_min, eps_max, [&](bool slot, bool ok, uint64_t cu, uint64_t cd) {
-      const bool mine = Q.n_batches <= 1 ? slot : (ok && in_batch(Q, batch, cu, cd));
+    // queue the lanes with mine set (members of entry ent), each with its output slot
+    auto push = [&](bool mine, bool ok, uint64_t cu, uint64_t cd, uint32_t ent) {
       const unsigned bal = __ballot_sync(kFull, mine);
-      if (mine) {
+      if (!bal) return;
+      const uint32_t nb = __popc(bal);
+      if (start + cnt + nb > limit) over = true;
+      if (!over && mine) {
         const uint32_t sl = (qh + qn + __popc(bal & lt)) & (kPtQ - 1);
         q.u[sl] = ok ? cu : kInvalid;
         q.d[sl] = ok ? cd : kInvalid;
+        q.pos[sl] = start + cnt + __popc(bal & lt);
+        q.src[sl] = kl;
+        q.ent[sl] = static_cast<uint8_t>(ent);
       }
-      qn += __popc(bal);
+      if (!over) qn += nb;
+      cnt += nb;
       if (qn >= 32u) drain(32u);
+    };
+    pt_walk(P, up, dn, eps_min, eps_max, [&](bool slot, bool ok, uint64_t cu, uint64_t cd) {
+      if (MODE == kSto) {
+        // hash once, then one member per entry whose batch the candidate falls in
+        const uint64_t b =
+            (ok && Q.n_batches > 1) ? batch_of(Q, rehash(det_hash(cu, cd))) : 0ull;
+        for (uint32_t e = e0; e < e1; e++)
+          push(Q.n_batches <= 1 ? slot : (ok && b == S.batch[e]), ok, cu, cd, e - e0);
+        return;
+      }
+      push(Q.n_batches <= 1 ? slot : (ok && in_batch(Q, batch, cu, cd)), ok, cu, cd, 0u);
     });
-    if (qn) drain(qn);
-    // invalid tail, or (overflow) the whole region
-    for (uint64_t p = (over ? start : base) + lane; p < limit; p += 32) out_up[p] = kInvalid;
-    if (over && lane == 0) overflow[k - k_begin] = 1;
+    if (over) {
+      // members of this source may still wait in the queue: finish them, then void the region
+      while (qn) drain(qn < 32u ? qn : 32u);
+      for (uint64_t p = start + lane; p < limit; p += 32) out_up[p] = kInvalid;
+      if (lane == 0) overflow[kl] = 1;
+    } else {
+      // the region's unused tail (the members' slots are below start + cnt)
+      for (uint64_t p = start + cnt + lane; p < limit; p += 32) out_up[p] = kInvalid;
+    }
   }
+  while (qn) drain(qn < 32u ? qn : 32u);
 }
 
 // Diagonal H_aa of the PT dets in 64-bit fixed point.  The diagonal is a sum of about
@@ -620,14 +673,20 @@ size_t pt_emit_reduce(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSour
 // with several batches a source's members are a binomial(bound, 1 / n_batches) count, and
 // bound / n_batches * 1.3 + 64 exceeds its mean by many standard deviations (overflowing
 // sources are re-run exactly).  SHCI_PT_SLOTS="slack,pad" replaces 1.3 and 64.
-std::vector<uint64_t> region_slots(const std::vector<uint64_t>& bound, uint64_t n_batches) {
-  if (n_batches <= 1) return bound;
+std::vector<uint64_t> region_slots(const std::vector<uint64_t>& bound, uint64_t n_batches,
+                                   const std::vector<uint32_t>* mult = nullptr) {
+  // mult[k]: entries of source k (a det walked once for several iterations)
   double slack = 1.3, pad = 64.0;
   if (const char* e = std::getenv("SHCI_PT_SLOTS")) std::sscanf(e, "%lf,%lf", &slack, &pad);
   std::vector<uint64_t> r(bound.size());
   for (size_t k = 0; k < bound.size(); k++) {
-    const double est = std::ceil(static_cast<double>(bound[k]) / n_batches * slack + pad);
-    r[k] = std::min<uint64_t>(bound[k], static_cast<uint64_t>(std::max(0.0, est)));
+    const uint64_t full = bound[k] * (mult ? (*mult)[k] : 1u);
+    if (n_batches <= 1) {
+      r[k] = full;
+      continue;
+    }
+    const double est = std::ceil(static_cast<double>(full) / n_batches * slack + pad);
+    r[k] = std::min<uint64_t>(full, static_cast<uint64_t>(std::max(0.0, est)));
   }
   return r;
 }
@@ -839,6 +898,29 @@ size_t pilot_pt_dets(shci_ctx* c, PtSetup& st, const std::vector<size_t>& src, d
   return pt_emit_reduce<kSto>(c, st, Q, S, n_src, hc, bu, bd, bv, shift + 5);
 }
 
+// Entry indices ordered by key (< key_end), stable: an LSD radix sort in two passes of up to
+// 16 bits over the key's bit width.
+std::vector<uint32_t> stable_order_by_key(const std::vector<uint32_t>& key, size_t key_end) {
+  const size_t n = key.size();
+  int bits = 1;
+  while (bits < 32 && (size_t{1} << bits) < key_end) bits++;
+  const int lo_bits = (bits + 1) / 2, hi_bits = bits - lo_bits;
+  std::vector<uint32_t> a(n), b(n);
+  std::iota(a.begin(), a.end(), 0u);
+  const int shifts[2] = {0, lo_bits};
+  const int widths[2] = {lo_bits, hi_bits};
+  for (int pass = 0; pass < 2; pass++) {
+    if (widths[pass] == 0) continue;
+    const uint32_t nb = 1u << widths[pass], mask = nb - 1u;
+    std::vector<uint32_t> cnt(nb + 1, 0u);
+    for (size_t k = 0; k < n; k++) cnt[((key[a[k]] >> shifts[pass]) & mask) + 1]++;
+    for (uint32_t d = 0; d < nb; d++) cnt[d + 1] += cnt[d];
+    for (size_t k = 0; k < n; k++) b[cnt[(key[a[k]] >> shifts[pass]) & mask]++] = a[k];
+    a.swap(b);
+  }
+  return a;
+}
+
 // Stochastic stage (solver.h:898-1153).  n_dets_in_sample = 0: the sample size comes from
 // the reference's 1,000-draw pilot and the PT memory pt_mem_avail (solver.h:942-1006);
 // semisto: the variational dets above the quantile of the top quarter of the unique-sample
@@ -977,7 +1059,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     // draw the samples of the next chunk of iterations (solver.h:1048-1072)
     const uint32_t chunk = iteration == 0 ? kFirstChunk : kNextChunk;
     const uint32_t n_it = static_cast<uint32_t>(std::min<size_t>(chunk, max_iterations - iteration));
-    std::vector<uint32_t> h_det, h_iter, h_batch;
+    std::vector<uint32_t> h_det, h_iter, h_batch, h_off;
     std::vector<double> h_count, h_weight;
     std::vector<uint8_t> h_dtm;
     {
@@ -1032,25 +1114,52 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
         }
         for (size_t i : list) cnt[i] = 0;
       }
+      // group the pass's entries by det (iteration order kept within a det): a det drawn in
+      // several iterations is walked once (the heaviest dets, with the widest windows, are
+      // drawn in nearly every iteration)
+      std::vector<uint32_t> order = stable_order_by_key(h_det, n_var);
+      auto permute = [&](auto& v) {
+        auto w = v;
+        for (size_t k = 0; k < order.size(); k++) w[k] = v[order[k]];
+        v.swap(w);
+      };
+      permute(h_det);
+      permute(h_iter);
+      permute(h_batch);
+      permute(h_count);
+      permute(h_weight);
+      permute(h_dtm);
+      h_off.clear();
+      for (size_t k = 0; k < h_det.size(); k++)
+        if (k == 0 || h_det[k] != h_det[k - 1]) h_off.push_back(static_cast<uint32_t>(k));
+      h_off.push_back(static_cast<uint32_t>(h_det.size()));
+      for (size_t g = 0; g + 1 < h_off.size(); g++)
+        if (h_off[g + 1] - h_off[g] > 255)
+          throw std::logic_error("stochastic PT2: more than 255 draws of one det in a pass");
     }
-    const uint32_t n_src = static_cast<uint32_t>(h_det.size());
+    const uint32_t n_ent = static_cast<uint32_t>(h_det.size());
+    const uint32_t n_src = static_cast<uint32_t>(h_off.size() - 1);  // dets of the pass
     DevBuf<uint32_t> d_det, d_iter, d_batch;
     DevBuf<double> d_count, d_weight;
     DevBuf<uint8_t> d_dtm;
+    DevBuf<uint32_t> d_off;
     d_det.mt = d_iter.mt = d_batch.mt = d_count.mt = d_weight.mt = d_dtm.mt = &c->mem;
-    d_det.resize(n_src);
-    d_iter.resize(n_src);
-    d_batch.resize(n_src);
-    d_count.resize(n_src);
-    d_weight.resize(n_src);
-    d_dtm.resize(n_src);
-    SHCI_CUDA(cudaMemcpyAsync(d_det.p, h_det.data(), n_src * 4, cudaMemcpyHostToDevice, s));
-    SHCI_CUDA(cudaMemcpyAsync(d_iter.p, h_iter.data(), n_src * 4, cudaMemcpyHostToDevice, s));
-    SHCI_CUDA(cudaMemcpyAsync(d_batch.p, h_batch.data(), n_src * 4, cudaMemcpyHostToDevice, s));
-    SHCI_CUDA(cudaMemcpyAsync(d_count.p, h_count.data(), n_src * 8, cudaMemcpyHostToDevice, s));
-    SHCI_CUDA(cudaMemcpyAsync(d_weight.p, h_weight.data(), n_src * 8, cudaMemcpyHostToDevice, s));
-    SHCI_CUDA(cudaMemcpyAsync(d_dtm.p, h_dtm.data(), n_src, cudaMemcpyHostToDevice, s));
-    StoSources S{d_det.p, d_iter.p, d_count.p, d_weight.p, d_batch.p, d_dtm.p};
+    d_off.mt = &c->mem;
+    d_off.resize(n_src + 1);
+    SHCI_CUDA(cudaMemcpyAsync(d_off.p, h_off.data(), (n_src + 1) * 4, cudaMemcpyHostToDevice, s));
+    d_det.resize(n_ent);
+    d_iter.resize(n_ent);
+    d_batch.resize(n_ent);
+    d_count.resize(n_ent);
+    d_weight.resize(n_ent);
+    d_dtm.resize(n_ent);
+    SHCI_CUDA(cudaMemcpyAsync(d_det.p, h_det.data(), n_ent * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_iter.p, h_iter.data(), n_ent * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_batch.p, h_batch.data(), n_ent * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_count.p, h_count.data(), n_ent * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_weight.p, h_weight.data(), n_ent * 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(d_dtm.p, h_dtm.data(), n_ent, cudaMemcpyHostToDevice, s));
+    StoSources S{d_det.p, d_iter.p, d_count.p, d_weight.p, d_batch.p, d_dtm.p, nullptr, d_off.p};
     PtParams Q{};
     Q.eps = eps_pt;
     Q.eps_psto = eps_pt_psto;
@@ -1059,7 +1168,10 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     Q.iter_shift = shift;
     PtParams Q1 = Q;
     set_batches(Q1, 1);
-    const std::vector<uint64_t> hc = region_slots(pt_counts<kSto>(c, st, Q1, S, n_src), n_batches);
+    std::vector<uint32_t> mult(n_src);
+    for (uint32_t g = 0; g < n_src; g++) mult[g] = h_off[g + 1] - h_off[g];
+    const std::vector<uint64_t> hc =
+        region_slots(pt_counts<kSto>(c, st, Q1, S, n_src), n_batches, &mult);
     DevBuf<uint64_t> bu, bd;
     DevBuf<double> bv[5];
     bu.mt = bd.mt = &c->mem;
