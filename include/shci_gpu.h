@@ -62,13 +62,19 @@ void* shci_stream(shci_ctx* ctx);
  * (src/chem/integrals.cc:17-35, 37-114, 155-384): |v| < 1e-9 dropped, duplicates keep the
  * larger |v|, HF det filled lowest (or from occs_up/occs_dn when both non-NULL), orbitals
  * reordered by HF orbital energy when reorder = -1 (default: unless occs given) or 1.
- * point_group: "C1", "C2", "Cs", "Ci", "C2v", "C2h", "D2", "D2h" (case-insensitive). */
+ * point_group: "C1", "C2", "Cs", "Ci", "C2v", "C2h", "D2", "D2h", or a linear group "Dooh" /
+ * "Dih" / "Coov" / "Civ" (case-insensitive; chem_system.cc:198-221).  ORBSYM labels with
+ * negative entries are converted to the reference's linear-group labels (integrals.cc:
+ * 116-153).  For a linear group every (pq|rs) with lz_p + lz_r != lz_q + lz_s is zero, as
+ * Integrals::get_2b returns it (integrals.cc:394-406), and the heat-bath queues pair r with
+ * the conjugate irrep (chem_system.cc:133-135). */
 shci_status shci_load_fcidump(shci_ctx* ctx, const char* path, unsigned n_up, unsigned n_dn,
                               const char* point_group, int reorder, const unsigned* occs_up,
                               const unsigned* occs_dn);
 
 /* Set already-prepared integrals: h1[n*n] (h_pq), g2[n^4] (chemists' (pq|rs) at
- * ((p*n+q)*n+r)*n+s), orb_sym[n] (irreps 1..8, NULL = all 1).  The HF det is given. */
+ * ((p*n+q)*n+r)*n+s), orb_sym[n] (irreps 1..8, or linear-group labels; NULL = all 1).  The
+ * HF det is given.  Linear groups screen g2 by Lz as shci_load_fcidump does. */
 shci_status shci_set_integrals(shci_ctx* ctx, int n_orbs, unsigned n_up, unsigned n_dn,
                                double e_core, const double* h1, const double* g2,
                                const unsigned* orb_sym, const char* point_group,
@@ -196,12 +202,60 @@ shci_status shci_davidson_csr(shci_ctx* ctx, size_t n, const uint64_t* row_ptr,
                               const double* init, double tol, double* eval, double* evec,
                               int* converged);
 
+/* Several-state Davidson (davidson.cc:8-196 with n_states initial vectors, as a Solver with
+ * n_states > 1 calls it) on a caller-supplied CSR: init[n_states * n] in, evecs[n_states * n]
+ * and evals[n_states] out.  1 <= n_states <= 8. */
+shci_status shci_davidson_csr_states(shci_ctx* ctx, size_t n, const uint64_t* row_ptr,
+                                     const uint32_t* cols, const double* vals,
+                                     const double* diag, unsigned n_states, const double* init,
+                                     double tol, double* evals, double* evecs, int* converged);
+
+/* ---- several states (config "n_states", chem_system.cc:24, 52-56) ------------------------ */
+
+/* Number of states of the variational stage (1 <= n_states <= 8).  States 1.. start at 1e-16
+ * on every current det.  With n_states > 1 the selection uses the coefficient of largest
+ * magnitude over the states (solver.h:440-444); while the det list is small (<= 50 dets when a
+ * step begins) new det k starts as state k's unit vector (solver.h:479-486); Davidson runs
+ * with all states (davidson.cc); the RDMs sum over the states (rdm.cc:222-231, 648-657).  The
+ * coefficients of state 0 are the context's coefficients (shci_get_dets / shci_set_coefs).
+ * PT2 of state s: shci_set_coefs with state s's coefficients, then the PT2 calls with state
+ * s's energy (solver.h:620-632). */
+shci_status shci_set_n_states(shci_ctx* ctx, unsigned n_states);
+shci_status shci_get_state_coefs(shci_ctx* ctx, unsigned state, double* coefs, size_t cap);
+shci_status shci_set_state_coefs(shci_ctx* ctx, unsigned state, const double* coefs, size_t n);
+/* ---- time-reversal symmetry (config "time_sym", needs n_up == n_dn) -------------------- */
+
+/* With on != 0 the det list holds one det of each time-reversal pair, the one with up <= dn
+ * (every current det must be in that form); an open det stands for (|up,dn> + |dn,up>)/sqrt(2).
+ * Selection multiplies an open source's eps_min by sqrt(2) and stores candidates in that form
+ * (solver.h:447-455); the Hamiltonian is the packed one of Hamiltonian<S>::update_matrix with
+ * time_sym (hamiltonian.h:415-598; elements get_hamiltonian_elem_time_sym, base_system.h:
+ * 86-101); updates rebuild it whole. */
+shci_status shci_set_time_sym(shci_ctx* ctx, int on);
+/* unpack_time_sym (base_system.h:108-123), as Solver::run_perturbation does before PT2: every
+ * det with up < dn gets its reverse appended, both coefficients (all states) times 1/sqrt(2);
+ * the context leaves time_sym mode. */
+shci_status shci_unpack_time_sym(shci_ctx* ctx);
+
+/* Energies of the states after the last variational iteration (FP64-corrected in mixed mode). */
+shci_status shci_get_state_energies(shci_ctx* ctx, double* energies, size_t cap);
+/* Per-iteration energies of every state of the last shci_run_variation:
+ * energies[iteration * n_states + state]; *n = number of iterations. */
+shci_status shci_get_var_trace_states(shci_ctx* ctx, double* energies, size_t cap, size_t* n);
+
 /* ---- heat-bath selection (Solver<S>::run_variation, solver.h:435-495) ---------------- */
 
 /* One selection step with the context's coefficients: five passes over var dets i = j mod 5,
  * each pass's new dets appended in ascending Det order with coefficient 1e-16.  Keeps the
  * eps_tried_prev memo (solver.h:445-448, 465-468) across calls.  n_new = dets added. */
 shci_status shci_select(shci_ctx* ctx, double eps_var, int var_sd, size_t* n_new);
+
+/* Second rejection of the selection (config "second_rejection" / "second_rejection_factor",
+ * solver.h:426-428, 461-465; chem_system.cc:300-308, 318-324, 364-370): when enabled, window
+ * entries with |H|^2 / (one-body energy difference to HF) < factor * eps_min^2 are dropped and
+ * eps_tried_prev becomes 1.000000001 * max(largest dropped |H|, eps_min).  Off by default
+ * (factor 0.2).  Applies to shci_select and shci_run_variation of this context. */
+shci_status shci_set_second_rejection(shci_ctx* ctx, int enable, double factor);
 
 /* eps_tried_prev memo (length = n dets at the last selection). */
 shci_status shci_get_eps_tried(shci_ctx* ctx, double* out, size_t cap);
@@ -326,6 +380,23 @@ shci_status shci_rdm1(shci_ctx* ctx, double* rdm1);
  * rdm2_half has n^2 (n^2 + 1) / 2 entries.  E_var = E_core + sum_pq h_pq g1_pq +
  * 1/2 sum_pqrs Gamma(p,q,r,s) (ps|qr), with g1 the 2-RDM contraction (rdm.cc:707-753). */
 shci_status shci_rdm2(shci_ctx* ctx, double* rdm2_half);
+
+/* ---- orbital optimisation inputs (src/chem/optimization.cc) -------------------------- */
+
+/* Generalized Fock matrix F[n*n] (row m, column n) of Optimization::get_generalized_Fock /
+ * generalized_Fock_element (optimization.cc:620-650, Helgaker 10.8.24) from the device RDMs of
+ * the current wavefunction (all states summed when n_states > 1):
+ * F(m,n) = sum_q gamma(m,q) h(n,q) + sum_qrs Gamma(m,r,s,q) (nq|rs) for orbitals of equal irrep,
+ * 0 otherwise.  Builds the Hamiltonian (FP64) if it is not current (the 2-RDM walks its
+ * connections). */
+shci_status shci_generalized_fock(shci_ctx* ctx, double* F);
+/* Optimization::parameter_indices (optimization.cc:500-522, no active space): the pairs
+ * p < q of equal irrep; *n = their count, up to cap written. */
+shci_status shci_orbital_parameters(shci_ctx* ctx, uint32_t* p, uint32_t* q, size_t cap,
+                                    size_t* n);
+/* Optimization::gradient (optimization.cc:565-578): grad[k] = 2 (F(p_k,q_k) - F(q_k,p_k)). */
+shci_status shci_orbital_gradient(shci_ctx* ctx, const uint32_t* p, const uint32_t* q,
+                                  size_t n_param, double* grad);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,16 @@ def lib():
             "orc_hv": (None, [vp, _f64p, _f64p]),
             "orc_davidson": (i, [vp, _f64p, d, ctypes.POINTER(d), _f64p, sz, ctypes.POINTER(sz)]),
             "orc_davidson_csr": (i, [sz, _u64p, _u32p, _f64p, _f64p, d, ctypes.POINTER(d)]),
+            "orc_davidson_csr_states": (i, [sz, _u64p, _u32p, _f64p, u, _f64p, d, _f64p, _f64p]),
+            "orc_set_n_states": (None, [vp, u]),
+            "orc_set_time_sym": (None, [vp, i]),
+            "orc_set_second_rejection": (None, [vp, i]),
+            "orc_unpack_time_sym": (None, [vp]),
+            "orc_generalized_fock": (None, [vp, _f64p, _f64p, _f64p]),
+            "orc_orbital_parameters": (sz, [vp, vp, vp, sz]),
+            "orc_get_state_coefs": (None, [vp, u, _f64p]),
+            "orc_set_state_coefs": (None, [vp, u, _f64p]),
+            "orc_state_energies": (None, [vp, _f64p, vp]),
             "orc_select": (sz, [vp, d, i]),
             "orc_eps_tried": (None, [vp, _f64p]),
             "orc_run_all_variations": (None, [vp, _f64p, sz, _f64p, sz, d, i, _f64p]),
@@ -203,6 +213,48 @@ class Oracle:
     def set_coefs(self, c):
         self.L.orc_set_coefs(self.h, np.ascontiguousarray(c, np.float64))
 
+    def generalized_fock(self, g1, half):
+        """Optimization::get_generalized_Fock from the given RDMs (n x n)."""
+        n = self.n_orbs
+        F = np.zeros(n * n)
+        self.L.orc_generalized_fock(self.h, np.ascontiguousarray(g1, np.float64).ravel(),
+                                    np.ascontiguousarray(half, np.float64), F)
+        return F.reshape(n, n)
+
+    def orbital_parameters(self):
+        k = self.L.orc_orbital_parameters(self.h, None, None, 0)
+        p = np.zeros(k, np.uint32)
+        q = np.zeros(k, np.uint32)
+        self.L.orc_orbital_parameters(self.h, p.ctypes.data, q.ctypes.data, k)
+        return p, q
+
+    def set_time_sym(self, on=True):
+        self.L.orc_set_time_sym(self.h, int(on))
+
+    def unpack_time_sym(self):
+        self.L.orc_unpack_time_sym(self.h)
+
+    def set_n_states(self, n):
+        self.n_states = n
+        self.L.orc_set_n_states(self.h, n)
+
+    def state_coefs(self, s):
+        out = np.zeros(self.L.orc_n_dets(self.h))
+        self.L.orc_get_state_coefs(self.h, s, out)
+        return out
+
+    def set_state_coefs(self, s, c):
+        self.L.orc_set_state_coefs(self.h, s, np.ascontiguousarray(c, np.float64))
+
+    def state_energies(self):
+        """(energies of the states after the last run, per-iteration energies (n_iter, n_states))"""
+        ns = getattr(self, "n_states", 1)
+        e = np.zeros(ns)
+        n_it = self.L.orc_n_iterations(self.h)
+        per = np.zeros((max(n_it, 1), ns))
+        self.L.orc_state_energies(self.h, e, per.ctypes.data)
+        return e, per[:n_it]
+
     def update_hamiltonian(self):
         return self.L.orc_update_hamiltonian(self.h)
 
@@ -328,6 +380,19 @@ class Oracle:
         out = np.zeros(n * n * (n * n + 1) // 2)
         self.L.orc_rdm2(self.h, out)
         return out
+
+
+def davidson_csr_states(row_ptr, cols, vals, init, tol):
+    """Several-state Davidson (davidson.cc) on an upper-triangle CSR; init is (n_states, n)."""
+    init = np.ascontiguousarray(init, np.float64)
+    ns, n = init.shape
+    ev = np.zeros(ns)
+    vecs = np.zeros((ns, n))
+    conv = lib().orc_davidson_csr_states(n, np.ascontiguousarray(row_ptr, np.uint64),
+                                         np.ascontiguousarray(cols, np.uint32),
+                                         np.ascontiguousarray(vals, np.float64), ns, init, tol,
+                                         ev, vecs)
+    return ev, vecs, bool(conv)
 
 
 def davidson_csr(row_ptr, cols, vals, init, tol):

@@ -42,6 +42,9 @@ constexpr double EPS = 1.0e-12;   // src/util.h:50
 constexpr double INF = 1.0e100;   // src/util.h:52
 
 static inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+constexpr double kSqrt2 = 1.4142135623730951;     // src/util.h:58
+constexpr double kSqrt2Inv = 0.7071067811865475;  // src/util.h:60
 static inline int ctz(uint64_t x) { return __builtin_ctzll(x); }
 
 // ---------------------------------------------------------------- determinants (C1)
@@ -170,8 +173,15 @@ struct Integrals {
   Det det_hf{0, 0};
   bool explicit_orbs = false;
 
+  // Linear point groups: Lz of each (reordered) orbital, and whether lookups screen by it
+  // (set once the system's point group is known, after loading: chem_system.cc:33-34).
+  bool lz_screen = false;
+  std::vector<int> lz;
+
   double get_1b(unsigned p, unsigned q) const { return h1[combine2(p, q)]; }
+  // src/chem/integrals.cc:394-406
   double get_2b(unsigned p, unsigned q, unsigned r, unsigned s) const {
+    if (lz_screen && lz[p] + lz[r] != lz[q] + lz[s]) return 0.;
     return g2[combine4(p, q, r, s)];
   }
   // Reducer used on duplicate keys: the larger |v| wins (src/chem/integrals.cc:104-111).
@@ -344,16 +354,52 @@ static void load_integrals(Integrals& I, const std::string& path, unsigned n_up,
 }
 
 // ---------------------------------------------------------------- symmetry (C3)
-// src/chem/product_table.cc:5-35: the C1..D2h tables are the XOR group on (irrep-1).
-static unsigned sym_product(unsigned a, unsigned b) { return ((a - 1) ^ (b - 1)) + 1; }
+// src/chem/dooh_util.cc:5-45: linear-group labels.  1, 2: Lz = 0 (g, u); label >= 3:
+// |Lz| = 1 + (label - 3) / 4, the sign from bit 1 of (label - 1), g/u from the parity.
+static int dooh_lz(int ind, int& gu) {
+  if (ind <= 2) {
+    gu = ind - 1;
+    return 0;
+  }
+  int lz = 1 + ((ind - 3) >> 2);
+  if ((((ind - 1) >> 1) & 1) == 0) lz = -lz;
+  gu = (ind + 1) & 1;
+  return lz;
+}
+static int dooh_ind(int lz, int gu) {
+  if (lz == 0) return gu + 1;
+  int ind = (std::abs(lz) << 2) - 1 + gu;
+  if (lz < 0) ind += 2;
+  return ind;
+}
+static unsigned dooh_inverse(unsigned i) {
+  int gu;
+  const int lz = dooh_lz(static_cast<int>(i), gu);
+  return lz > 0 ? i + 2 : lz < 0 ? i - 2 : i;
+}
 
-static unsigned point_group_order(const std::string& pg) {
+// src/chem/product_table.cc:5-47: the C1..D2h tables are the XOR group on (irrep-1); the
+// linear groups add Lz and combine g/u.
+static unsigned sym_product(bool dooh, unsigned a, unsigned b) {
+  if (!dooh) return ((a - 1) ^ (b - 1)) + 1;
+  int ga, gb;
+  const int la = dooh_lz(static_cast<int>(a), ga), lb = dooh_lz(static_cast<int>(b), gb);
+  return static_cast<unsigned>(dooh_ind(la + lb, (ga + gb) & 1));
+}
+
+// src/chem/chem_system.cc:198-221 and product_table.cc:43-47 (128 irreps for Dooh)
+static unsigned point_group_order(const std::string& pg, bool& dooh) {
   std::string s;
   for (char c : pg) s.push_back(std::tolower(c));
+  dooh = false;
   if (s == "c1") return 1;
   if (s == "c2" || s == "cs" || s == "ci") return 2;
   if (s == "c2v" || s == "c2h" || s == "d2") return 4;
   if (s == "d2h") return 8;
+  if (s == "coov" || s == "civ" || s == "dooh" || s == "dih") {
+    dooh = true;
+    return 128;
+  }
   throw std::invalid_argument("point group not supported by the oracle: " + pg);
 }
 
@@ -371,6 +417,7 @@ struct System {
   Integrals I;
   unsigned n_orbs = 0, n_up = 0, n_dn = 0, n_elecs = 0;
   unsigned n_syms = 1;
+  bool dooh = false;
   std::vector<std::vector<unsigned>> sym_orbs;
   std::vector<std::vector<Hrs>> hci_queue;
   std::vector<std::vector<Sr>> singles_queue;
@@ -382,8 +429,16 @@ struct System {
   bool has_double_excitation = true;
 
   std::vector<Det> dets;
-  std::vector<double> coefs;  // one state
-  double energy_var = 0.0;
+  std::vector<double> coefs;  // state 0
+  double energy_var = 0.0;    // state 0
+  // n_states > 1 (config "n_states", chem_system.cc:24, 52-56): the coefficients and
+  // variational energies of states 1 .. n_states - 1
+  unsigned n_states = 1;
+  std::vector<std::vector<double>> xcoefs;
+  std::vector<double> xenergy_var;
+  // time-reversal symmetry (config "time_sym"): a det with up != dn stands for
+  // (|up,dn> + |dn,up>) / sqrt(2); the list holds the form with up <= dn
+  bool time_sym = false;
 
   // ------------------------------------------------ Slater-Condon (C6)
   // src/chem/chem_system.cc:444-457
@@ -469,6 +524,41 @@ struct System {
     return e;
   }
   // src/chem/chem_system.cc:409-442
+  // src/base_system.h:86-101 (SQRT2 = src/util.h:58)
+  double hamiltonian_elem_time_sym(const Det& di, const Det& dj, int n_excite) const {
+    double h = hamiltonian_elem(di, dj, n_excite);
+    if (di.up == di.dn) {
+      if (dj.up != dj.dn) h *= kSqrt2;
+    } else {
+      if (dj.up == dj.dn) {
+        h *= kSqrt2;
+      } else {
+        const Det r{di.dn, di.up};
+        h += hamiltonian_elem(r, dj, -1);
+      }
+    }
+    return h;
+  }
+
+  // src/base_system.h:108-123: every det with up < dn gets its reverse appended, both
+  // coefficients divided by sqrt(2) (SQRT2_INV = src/util.h:60)
+  void unpack_time_sym() {
+    const size_t n_old = dets.size();
+    for (size_t i = 0; i < n_old; i++) {
+      const Det det = dets[i];
+      if (det.up < det.dn) {
+        auto half = [&](std::vector<double>& c) {
+          const double v = c[i] * kSqrt2Inv;
+          c[i] = v;
+          c.push_back(v);
+        };
+        half(coefs);
+        for (auto& xc : xcoefs) half(xc);
+        dets.push_back(Det{det.dn, det.up});
+      }
+    }
+  }
+
   double hamiltonian_elem(const Det& di, const Det& dj, int n_excite) const {
     Diff du, dd;
     if (n_excite < 0) {
@@ -545,7 +635,15 @@ struct System {
     n_up = nu;
     n_dn = nd;
     n_elecs = nu + nd;
-    n_syms = point_group_order(pg);
+    n_syms = point_group_order(pg, dooh);
+    if (dooh) {  // Integrals::set_point_group after load (chem_system.cc:33-34)
+      I.lz.resize(n_orbs);
+      for (unsigned o = 0; o < n_orbs; o++) {
+        int gu;
+        I.lz[o] = dooh_lz(static_cast<int>(I.orb_sym[o]), gu);
+      }
+      I.lz_screen = true;
+    }
     // src/chem/chem_system.cc:65-72
     sym_orbs.assign(n_syms + 1, {});
     for (unsigned o = 0; o < n_orbs; o++) {
@@ -592,9 +690,11 @@ struct System {
       const unsigned sp = I.orb_sym[p];
       for (unsigned q = p + 1; q < n_orbs; q++) {
         const size_t pq = combine2(p, q);
-        const unsigned sq = sym_product(sp, I.orb_sym[q]);
+        const unsigned sq = sym_product(dooh, sp, I.orb_sym[q]);
         for (unsigned r = 0; r < n_orbs; r++) {
-          const unsigned sr = sym_product(sq, I.orb_sym[r]);
+          unsigned sr = I.orb_sym[r];
+          if (dooh) sr = dooh_inverse(sr);
+          sr = sym_product(dooh, sq, sr);
           if (sr >= sym_orbs.size()) continue;
           for (unsigned s : sym_orbs[sr]) {
             if (s < r) continue;
@@ -612,9 +712,11 @@ struct System {
       const unsigned sp = I.orb_sym[p];
       for (unsigned q = n_orbs + p; q < 2 * n_orbs; q++) {
         const size_t pq = combine2(p, q);
-        const unsigned sq = sym_product(sp, I.orb_sym[q - n_orbs]);
+        const unsigned sq = sym_product(dooh, sp, I.orb_sym[q - n_orbs]);
         for (unsigned r = 0; r < n_orbs; r++) {
-          const unsigned sr = sym_product(sq, I.orb_sym[r]);
+          unsigned sr = I.orb_sym[r];
+          if (dooh) sr = dooh_inverse(sr);
+          sr = sym_product(dooh, sq, sr);
           if (sr >= sym_orbs.size()) continue;
           for (unsigned s : sym_orbs[sr]) {
             const double H = hci_queue_elem(p, q, r, s + n_orbs);
@@ -821,6 +923,7 @@ struct Hamiltonian {
 
   // src/solver/hamiltonian.h:157-254
   void update_abdet(const System& sys) {
+    const bool ts = sys.time_sym;
     std::unordered_set<size_t> ua, ub;
     for (size_t i = n_dets_prev; i < n_dets; i++) {
       const Det& d = sys.dets[i];
@@ -836,17 +939,38 @@ struct Hamiltonian {
         aid = ita->second;
       }
       ua.insert(aid);
-      auto itb = beta_to_id.find(d.dn);
-      if (itb == beta_to_id.end()) {
-        bid = beta_to_id.size();
-        beta_to_id[d.dn] = bid;
-        unique_betas.push_back(d.dn);
-        b2a.resize(bid + 1);
-        b2d.resize(bid + 1);
+      if (ts) {  // time_sym: beta strings take ids in the alpha id space (:182-198, 219-228)
+        auto itb2 = alpha_to_id.find(d.dn);
+        if (itb2 == alpha_to_id.end()) {
+          bid = alpha_to_id.size();
+          alpha_to_id[d.dn] = bid;
+          unique_alphas.push_back(d.dn);
+        } else {
+          bid = itb2->second;
+        }
+        const size_t m = alpha_to_id.size();
+        if (a2b.size() < m) {
+          a2b.resize(m);
+          a2d.resize(m);
+        }
+        if (b2a.size() < m) {
+          b2a.resize(m);
+          b2d.resize(m);
+        }
+        ub.insert(bid);
       } else {
-        bid = itb->second;
+        auto itb = beta_to_id.find(d.dn);
+        if (itb == beta_to_id.end()) {
+          bid = beta_to_id.size();
+          beta_to_id[d.dn] = bid;
+          unique_betas.push_back(d.dn);
+          b2a.resize(bid + 1);
+          b2d.resize(bid + 1);
+        } else {
+          bid = itb->second;
+        }
+        ub.insert(bid);
       }
-      ub.insert(bid);
       a2b[aid].push_back(bid);
       a2d[aid].push_back(i);
       b2a[bid].push_back(aid);
@@ -871,6 +995,14 @@ struct Hamiltonian {
         for (unsigned o : occ(d.up)) abm1[d.up & ~(1ull << o)].first.push_back(aid);
         ua.insert(aid);
       }
+      if (sys.time_sym) {  // beta strings join the alpha lists (:277-287)
+        const size_t bid = alpha_to_id[d.dn];
+        if (!ua.count(bid)) {
+          for (unsigned o : occ(d.dn)) abm1[d.dn & ~(1ull << o)].first.push_back(bid);
+          ua.insert(bid);
+        }
+        continue;
+      }
       const size_t bid = beta_to_id[d.dn];
       if (!ub.count(bid)) {
         for (unsigned o : occ(d.dn)) abm1[d.dn & ~(1ull << o)].second.push_back(bid);
@@ -886,7 +1018,8 @@ struct Hamiltonian {
     beta_singles.resize(beta_to_id.size());
     for (size_t i = n_dets_prev; i < n_dets; i++) {
       ua.insert(alpha_to_id[sys.dets[i].up]);
-      ub.insert(beta_to_id[sys.dets[i].dn]);
+      if (sys.time_sym) ua.insert(alpha_to_id[sys.dets[i].dn]);  // (:316-325)
+      else ub.insert(beta_to_id[sys.dets[i].dn]);
     }
     for (size_t aid = 0; aid < unique_alphas.size(); aid++) {
       const uint64_t a = unique_alphas[aid];
@@ -918,40 +1051,68 @@ struct Hamiltonian {
     for (auto& v : beta_singles) std::sort(v.begin(), v.end());
   }
 
-  // src/solver/hamiltonian.h:415-598 (time_sym = false)
+  // src/solver/hamiltonian.h:415-598.  With time_sym the elements are
+  // get_hamiltonian_elem_time_sym and each open det also meets the dets connected to its
+  // reverse: same-string partners of the reversed strings (:448-459, 473-484) and mixed
+  // doubles of the reverse (:535-590).
   void update_matrix(const System& sys) {
     matrix.set_dim(n_dets);
     const auto& dets = sys.dets;
+    const bool ts = sys.time_sym;
+    auto elem = [&](const Det& a, const Det& b, int nx) {
+      return ts ? sys.hamiltonian_elem_time_sym(a, b, nx) : sys.hamiltonian_elem(a, b, nx);
+    };
 #pragma omp parallel for schedule(dynamic, 16)
     for (size_t det_id = 0; det_id < n_dets; det_id++) {
       const Det& det = dets[det_id];
       auto& row = matrix.rows[det_id];
       const bool is_new = det_id >= n_dets_prev;
       if (is_new) {
-        const double H = sys.hamiltonian_elem(det, det, 0);
+        const double H = elem(det, det, 0);
         row.emplace_back(static_cast<uint32_t>(det_id), H);
         matrix.diag[det_id] = H;
       }
       const size_t start_id = is_new ? det_id + 1 : n_dets_prev;
-      const size_t bid = beta_to_id.at(det.dn);
+      const bool open = det.up != det.dn;
+      auto take = [&](size_t j, double H) {
+        if (std::abs(H) < EPS) return;
+        row.emplace_back(static_cast<uint32_t>(j), H);
+      };
+      // alpha excitations: same beta string (:436-447), then the reverse's (:448-459)
+      const size_t bid = ts ? alpha_to_id.at(det.dn) : beta_to_id.at(det.dn);
       for (size_t j : b2d[bid]) {
         if (j < start_id) continue;
-        const double H = sys.hamiltonian_elem(det, dets[j], -1);
-        if (std::abs(H) < EPS) continue;
-        row.emplace_back(static_cast<uint32_t>(j), H);
+        take(j, elem(det, dets[j], -1));
       }
+      if (ts && open && a2d.size() > bid) {
+        for (size_t j : a2d[bid]) {
+          if (j < start_id) continue;
+          const Det& c = dets[j];
+          if (c.up == c.dn) continue;
+          take(j, sys.hamiltonian_elem_time_sym(det, c, -1));
+        }
+      }
+      // beta excitations: same alpha string (:461-472), then the reverse's (:473-484)
       const size_t aid = alpha_to_id.at(det.up);
       for (size_t j : a2d[aid]) {
         if (j < start_id) continue;
-        const double H = sys.hamiltonian_elem(det, dets[j], -1);
-        if (std::abs(H) < EPS) continue;
-        row.emplace_back(static_cast<uint32_t>(j), H);
+        take(j, elem(det, dets[j], -1));
       }
-      if (!sys.has_double_excitation) continue;
+      if (ts && open && b2d.size() > aid) {
+        for (size_t j : b2d[aid]) {
+          if (j < start_id) continue;
+          const Det& c = dets[j];
+          if (c.up == c.dn) continue;
+          take(j, sys.hamiltonian_elem_time_sym(det, c, -1));
+        }
+      }
+      if (!sys.has_double_excitation && !ts) continue;
+      // mixed doubles (:487-533)
       const auto& as_list = alpha_singles[aid];
-      const auto& bs_list = beta_singles[bid];
+      const auto& bs_list = ts ? alpha_singles[bid] : beta_singles[bid];
       for (size_t as : as_list) {
         if (a2b.size() <= as) continue;
+        if (ts && as == bid) continue;
         const auto& rel_b = a2b[as];
         const auto& rel_d = a2d[as];
         const size_t nrel = rel_b.size();
@@ -959,25 +1120,60 @@ struct Hamiltonian {
           const size_t st =
               std::lower_bound(rel_d.begin(), rel_d.end(), start_id) - rel_d.begin();
           for (size_t k = st; k < nrel; k++) {
+            if (ts && rel_b[k] == aid) continue;
             if (std::binary_search(bs_list.begin(), bs_list.end(), rel_b[k])) {
               const size_t j = rel_d[k];
-              const double H = sys.hamiltonian_elem(det, dets[j], 2);
-              if (std::abs(H) < EPS) continue;
-              row.emplace_back(static_cast<uint32_t>(j), H);
+              take(j, elem(det, dets[j], 2));
             }
           }
         } else {
           size_t ptr = 0;
           for (size_t bs : bs_list) {
+            if (ts && bs == aid) continue;
             while (ptr < nrel && rel_b[ptr] < bs) ptr++;
             if (ptr == nrel) break;
             if (rel_b[ptr] == bs) {
               const size_t j = rel_d[ptr];
               ptr++;
               if (j < start_id) continue;
-              const double H = sys.hamiltonian_elem(det, dets[j], 2);
-              if (std::abs(H) < EPS) continue;
-              row.emplace_back(static_cast<uint32_t>(j), H);
+              take(j, elem(det, dets[j], 2));
+            }
+          }
+        }
+      }
+      if (!(ts && open)) continue;
+      // mixed doubles of the reverse (:535-590)
+      const Det rev{det.dn, det.up};
+      for (size_t as : as_list) {
+        if (as == bid) continue;
+        if (b2a.size() <= as) continue;
+        const auto& rel_b = b2a[as];
+        const auto& rel_d = b2d[as];
+        const size_t nrel = rel_b.size();
+        auto visit = [&](size_t j) {
+          const Det& c = dets[j];
+          if (c.up == c.dn) return;
+          if (popc(c.up ^ det.up) == 2 && popc(c.dn ^ det.dn) == 2) return;
+          take(j, sys.hamiltonian_elem_time_sym(rev, c, 2));
+        };
+        if (sort_by_det_id) {
+          const size_t st =
+              std::lower_bound(rel_d.begin(), rel_d.end(), start_id) - rel_d.begin();
+          for (size_t k = st; k < nrel; k++) {
+            if (rel_b[k] == aid) continue;
+            if (std::binary_search(bs_list.begin(), bs_list.end(), rel_b[k])) visit(rel_d[k]);
+          }
+        } else {
+          size_t ptr = 0;
+          for (size_t bs : bs_list) {
+            if (bs == aid) continue;
+            while (ptr < nrel && rel_b[ptr] < bs) ptr++;
+            if (ptr == nrel) break;
+            if (rel_b[ptr] == bs) {
+              const size_t j = rel_d[ptr];
+              ptr++;
+              if (j < start_id) continue;
+              visit(j);
             }
           }
         }
@@ -1135,6 +1331,142 @@ static DavidsonResult davidson(const SparseMatrix& H, const std::vector<double>&
   return res;
 }
 
+// ---------------------------------------------------------------- Davidson, several states
+// src/solver/davidson.cc:8-196 for any n_states: n_states * 5 stored vectors, the initial
+// vectors normalised and orthogonalised in order, a subspace matrix that starts with only its
+// diagonal set (:62-77), one preconditioned vector per step for state i_state_precond (cycling
+// over the unconverged states), a subspace solve after the last state's vector, restarts that
+// collapse onto the Ritz vectors (:86-103), and convergence state by state (:174-186).
+struct DavidsonStates {
+  std::vector<double> evals;
+  std::vector<std::vector<double>> evecs;
+  bool converged = false;
+};
+
+static DavidsonStates davidson_states(const SparseMatrix& H,
+                                      const std::vector<std::vector<double>>& init, double tol,
+                                      std::vector<std::vector<double>>* trace = nullptr) {
+  DavidsonStates res;
+  const size_t dim = init[0].size();
+  const unsigned ns = static_cast<unsigned>(std::min(dim, init.size()));
+  res.evals.assign(init.size(), 0.0);
+  res.evecs.assign(init.size(), std::vector<double>(dim, 0.0));
+  if (dim == 1) {
+    res.evals[0] = H.diag[0];
+    res.evecs[0] = {1.0};
+    res.converged = true;
+    return res;
+  }
+  const size_t nis = std::min<size_t>(dim, 5);
+  const size_t m = ns * nis;
+  std::vector<std::vector<double>> v(m, std::vector<double>(dim)), Hv(m), w(ns), Hw(ns);
+  for (unsigned i = 0; i < ns; i++) {
+    double norm = std::sqrt(dot(init[i], init[i]));
+    for (size_t j = 0; j < dim; j++) v[i][j] = init[i][j] / norm;
+    if (i > 0) {
+      for (unsigned k = 0; k < i; k++) {
+        const double ip = dot(v[i], v[k]);
+        for (size_t j = 0; j < dim; j++) v[i][j] -= ip * v[k][j];
+      }
+      norm = std::sqrt(dot(v[i], v[i]));
+      for (size_t j = 0; j < dim; j++) v[i][j] /= norm;
+    }
+  }
+  std::vector<double> hk(m * m, 0.0);
+  std::vector<double> lam(ns), lam_prev(ns);
+  for (unsigned i = 0; i < ns; i++) {
+    Hv[i] = H.mul(v[i]);
+    lam[i] = dot(v[i], Hv[i]);
+    hk[i * m + i] = lam[i];
+    w[i] = v[i];
+    Hw[i] = Hv[i];
+  }
+  if (trace) trace->push_back(lam);
+  lam_prev = lam;
+  bool converged = false;
+  size_t n_conv = 0, precond = 0;
+  for (size_t it = ns; it < m * 2; it++) {
+    const size_t ic = it % m;
+    if (it >= m) {
+      if (ic < ns - 1) continue;
+      if (ic == ns - 1) {
+        for (unsigned i = 0; i < ns; i++) {
+          v[i] = w[i];
+          Hv[i] = Hw[i];
+        }
+        for (unsigned i = 0; i < ns; i++) {
+          lam[i] = dot(v[i], Hv[i]);
+          hk[i * m + i] = lam[i];
+          for (unsigned k = i + 1; k < ns; k++) {
+            const double e = dot(v[i], Hv[k]);
+            hk[i * m + k] = e;
+            hk[k * m + i] = e;
+          }
+        }
+        continue;
+      }
+    }
+    const double l = lam[precond];
+    for (size_t j = 0; j < dim; j++) {
+      const double d = l - H.diag[j];
+      v[ic][j] = std::abs(d) < 1.0e-8 ? 0.0 : (Hw[precond][j] - l * w[precond][j]) / d;
+    }
+    for (size_t i = 0; i < ic; i++) {
+      const double nrm = dot(v[ic], v[i]);
+      for (size_t j = 0; j < dim; j++) v[ic][j] -= nrm * v[i][j];
+    }
+    const double norm = std::sqrt(dot(v[ic], v[ic]));
+    if (norm < 1e-12) {
+      converged = true;
+      break;
+    }
+    for (size_t j = 0; j < dim; j++) v[ic][j] /= norm;
+    Hv[ic] = H.mul(v[ic]);
+    for (size_t i = 0; i <= ic; i++) hk[ic * m + i] = dot(v[i], Hv[ic]);
+    if (precond + 1 == ns) {
+      const int k = static_cast<int>(ic + 1);
+      std::vector<double> lower(k * k, 0.0), ev, evec;
+      for (int i = 0; i < k; i++)
+        for (int j = 0; j <= i; j++) lower[i * k + j] = hk[i * m + j];
+      jacobi_eig(k, lower, ev, evec);
+      for (unsigned s = 0; s < ns; s++) {
+        lam[s] = ev[s];
+        const double factor = evec[0 * k + s] < 0 ? -1.0 : 1.0;
+        std::vector<double> ek(k);
+        for (int i = 0; i < k; i++) ek[i] = evec[i * k + s] * factor;
+        w[s].assign(dim, 0.0);
+        Hw[s].assign(dim, 0.0);
+        for (size_t j = 0; j < dim; j++) {
+          double wj = 0.0, hwj = 0.0;
+          for (int i = 0; i < k; i++) {
+            wj += v[i][j] * ek[i];
+            hwj += Hv[i][j] * ek[i];
+          }
+          w[s][j] = wj;
+          Hw[s][j] = hwj;
+        }
+      }
+      if (trace) trace->push_back(lam);
+      for (unsigned s = static_cast<unsigned>(n_conv); s < ns; s++) {
+        if (std::abs(lam[s] - lam_prev[s]) > tol) break;
+        n_conv++;
+      }
+      if (n_conv == ns) converged = true;
+      if (!converged) lam_prev = lam;
+      if (converged) break;
+    }
+    precond++;
+    if (precond >= ns) precond = n_conv;
+  }
+  for (unsigned s = 0; s < ns; s++) {
+    res.evals[s] = lam[s];
+    res.evecs[s] = w[s];
+  }
+  for (size_t s = ns; s < init.size(); s++) res.evecs[s] = init[s];  // (:191-195)
+  res.converged = converged;
+  return res;
+}
+
 // ---------------------------------------------------------------- solver (C10, C11)
 struct Solver {
   System sys;
@@ -1146,6 +1478,7 @@ struct Solver {
   bool second_rejection = false;
   std::vector<size_t> iter_ndets, iter_nnz;
   std::vector<double> iter_energy;
+  std::vector<std::vector<double>> iter_xenergy;  // states 1.. per iteration (n_states > 1)
   bool last_davidson_converged = false;
 
   // One selection step (src/solver/solver.h:435-495): five passes over i = j mod 5, each
@@ -1161,17 +1494,22 @@ struct Solver {
       for (size_t i = j; i < n_dets; i += 5) {
         auto& out = found[omp_get_thread_num()];
         const Det& det = sys.dets[i];
-        const double max_coef = sys.coefs[i];
+        double max_coef = sys.coefs[i];  // the largest |c| over the states (solver.h:440-444)
+        for (const auto& xc : sys.xcoefs)
+          if (std::abs(xc[i]) > std::abs(max_coef)) max_coef = xc[i];
         double eps_min = eps_var / std::abs(max_coef);
         if (i == 0 && var_sd) eps_min = 0.0;
+        if (sys.time_sym && det.up != det.dn) eps_min *= kSqrt2;  // (:451)
         if (eps_min >= eps_tried_prev[i]) continue;
         auto handler = [&](const Det& c, int n_excite) {
-          if (var_dets.count(c)) return;
+          Det reg = c;  // the stored form up <= dn (:453-455)
+          if (sys.time_sym && c.up > c.dn) reg = Det{c.dn, c.up};
+          if (var_dets.count(reg)) return;
           if (n_excite == 1) {
             const double h_ai = sys.hamiltonian_elem(det, c, 1);
             if (std::abs(h_ai) < eps_min) return;
           }
-          out.push_back(c);
+          out.push_back(reg);
         };
         if (second_rejection) {
           const double mr = sys.find_connected_dets(det, eps_tried_prev[i], eps_min, handler, true);
@@ -1189,6 +1527,11 @@ struct Solver {
         var_dets.insert(d);
         sys.dets.push_back(d);
         sys.coefs.push_back(1e-16);
+        // solver.h:479-486: while the list is small, det k starts as state k's unit vector
+        for (unsigned s = 1; s < sys.n_states; s++) {
+          auto& xc = sys.xcoefs[s - 1];
+          xc.push_back(n_dets <= 50 && xc.size() == s ? 1.0 : 1e-16);
+        }
       }
       n_new_total += all.size();
     }
@@ -1203,8 +1546,11 @@ struct Solver {
     bool converged = false, dets_converged = false;
     sys.energy_hf_1b = 0.0;
     if (second_rejection) {
+      // ChemSystem::get_e_hf_1b (chem_system.cc:812-823)
       for (unsigned p : occ(sys.dets[0].up)) sys.energy_hf_1b += sys.I.get_1b(p, p);
-      for (unsigned p : occ(sys.dets[0].dn)) sys.energy_hf_1b += sys.I.get_1b(p, p);
+      if (sys.time_sym) sys.energy_hf_1b *= 2.;
+      else
+        for (unsigned p : occ(sys.dets[0].dn)) sys.energy_hf_1b += sys.I.get_1b(p, p);
     }
     while (!converged) {
       if (!dets_converged) {
@@ -1212,7 +1558,22 @@ struct Solver {
         ham.update(sys);
       }
       const double tol = until_converged ? target_error / 500000 : target_error / 50;
-      DavidsonResult dr = davidson(ham.matrix, sys.coefs, tol);
+      DavidsonResult dr;
+      if (sys.n_states == 1) {
+        dr = davidson(ham.matrix, sys.coefs, tol);
+      } else {  // davidson.cc with n_states initial vectors
+        std::vector<std::vector<double>> init(1, sys.coefs);
+        init.insert(init.end(), sys.xcoefs.begin(), sys.xcoefs.end());
+        DavidsonStates ds = davidson_states(ham.matrix, init, tol);
+        dr.eval = ds.evals[0];
+        dr.evec = ds.evecs[0];
+        dr.converged = ds.converged;
+        for (unsigned s = 1; s < sys.n_states; s++) {
+          sys.xcoefs[s - 1] = ds.evecs[s];
+          sys.xenergy_var[s - 1] = ds.evals[s];
+        }
+        iter_xenergy.push_back(std::vector<double>(ds.evals.begin() + 1, ds.evals.end()));
+      }
       sys.coefs = dr.evec;
       last_davidson_converged = dr.converged;
       iter_ndets.push_back(n_dets_new);
@@ -1897,6 +2258,7 @@ void orc_set_dets(void* h, const uint64_t* up, const uint64_t* dn, const double*
     s.sys.dets[i] = Det{up[i], dn[i]};
     s.sys.coefs[i] = coefs ? coefs[i] : (i == 0 ? 1.0 : 1e-16);
   }
+  for (auto& xc : s.sys.xcoefs) xc.assign(n, 1e-16);
   s.var_dets.clear();
   for (const auto& d : s.sys.dets) s.var_dets.insert(d);
   s.ham.clear();
@@ -1966,6 +2328,79 @@ int orc_davidson(void* h, double* coefs, double tol, double* eval, double* trace
   return r.converged ? 1 : 0;
 }
 
+// Time-reversal symmetry (config "time_sym"; needs n_up == n_dn).  Set before any variation.
+void orc_set_time_sym(void* h, int on) {
+  auto& s = S(h);
+  s.sys.time_sym = on != 0;
+  s.ham.clear();
+}
+
+// Solver::run_perturbation's unpack_time_sym (solver.h:593, base_system.h:108-123).
+void orc_unpack_time_sym(void* h) {
+  auto& s = S(h);
+  s.sys.unpack_time_sym();
+  s.var_dets.clear();
+  for (const auto& d : s.sys.dets) s.var_dets.insert(d);
+  s.ham.clear();
+  s.eps_tried_prev.clear();
+}
+
+// Number of states (ChemSystem::setup, chem_system.cc:24, 52-56): states 1.. start at 1e-16 on
+// every current det.
+void orc_set_n_states(void* h, unsigned ns) {
+  auto& s = S(h).sys;
+  s.n_states = ns < 1 ? 1 : ns;
+  s.xcoefs.assign(s.n_states - 1, std::vector<double>(s.dets.size(), 1e-16));
+  s.xenergy_var.assign(s.n_states - 1, 0.0);
+}
+
+// Coefficients of state st (0 = the main vector).
+void orc_get_state_coefs(void* h, unsigned st, double* out) {
+  auto& s = S(h).sys;
+  const auto& v = st == 0 ? s.coefs : s.xcoefs.at(st - 1);
+  std::copy(v.begin(), v.end(), out);
+}
+
+void orc_set_state_coefs(void* h, unsigned st, const double* c) {
+  auto& s = S(h).sys;
+  auto& v = st == 0 ? s.coefs : s.xcoefs.at(st - 1);
+  std::copy(c, c + s.dets.size(), v.begin());
+}
+
+// energies[n_states] of the last variational run; per_iter[n_iter * n_states] if non-null
+void orc_state_energies(void* h, double* energies, double* per_iter) {
+  auto& S_ = S(h);
+  auto& s = S_.sys;
+  energies[0] = s.energy_var;
+  for (unsigned k = 1; k < s.n_states; k++) energies[k] = s.xenergy_var[k - 1];
+  if (per_iter)
+    for (size_t it = 0; it < S_.iter_energy.size(); it++) {
+      per_iter[it * s.n_states] = S_.iter_energy[it];
+      for (unsigned k = 1; k < s.n_states; k++)
+        per_iter[it * s.n_states + k] =
+            it < S_.iter_xenergy.size() ? S_.iter_xenergy[it][k - 1] : 0.0;
+    }
+}
+
+// Several-state Davidson on an explicit upper-triangle CSR: init[ns * n] in, evecs[ns * n] and
+// evals[ns] out.  Returns 1 when converged.
+int orc_davidson_csr_states(size_t n, const uint64_t* row_ptr, const uint32_t* cols,
+                            const double* vals, unsigned ns, const double* init, double tol,
+                            double* evals, double* evecs) {
+  SparseMatrix m;
+  m.set_dim(n);
+  for (size_t i = 0; i < n; i++)
+    for (uint64_t k = row_ptr[i]; k < row_ptr[i + 1]; k++) m.append(i, cols[k], vals[k]);
+  std::vector<std::vector<double>> iv(ns);
+  for (unsigned s = 0; s < ns; s++) iv[s].assign(init + s * n, init + (s + 1) * n);
+  auto r = davidson_states(m, iv, tol);
+  for (unsigned s = 0; s < ns; s++) {
+    evals[s] = r.evals[s];
+    std::copy(r.evecs[s].begin(), r.evecs[s].end(), evecs + s * n);
+  }
+  return r.converged ? 1 : 0;
+}
+
 // Davidson on an explicit upper-triangle CSR (for the Hilbert-matrix golden test).
 int orc_davidson_csr(size_t n, const uint64_t* row_ptr, const uint32_t* cols, const double* vals,
                      double* coefs, double tol, double* eval) {
@@ -2005,6 +2440,20 @@ void orc_run_all_variations(void* h, const double* eps_vars, size_t n_eps, const
   std::vector<double> ev(eps_vars, eps_vars + n_eps), sc(sched, sched + n_sched);
   auto e = s.run_all_variations(ev, sc);
   std::copy(e.begin(), e.end(), energies);
+}
+
+// Second rejection for single selection steps (orc_select): the flag and energy_hf_1b as
+// run_variation sets them (solver.h:426-428, chem_system.cc:812-823).
+void orc_set_second_rejection(void* h, int on) {
+  auto& s = S(h);
+  s.second_rejection = on != 0;
+  s.sys.energy_hf_1b = 0.0;
+  if (s.second_rejection) {
+    for (unsigned p : occ(s.sys.dets[0].up)) s.sys.energy_hf_1b += s.sys.I.get_1b(p, p);
+    if (s.sys.time_sym) s.sys.energy_hf_1b *= 2.;
+    else
+      for (unsigned p : occ(s.sys.dets[0].dn)) s.sys.energy_hf_1b += s.sys.I.get_1b(p, p);
+  }
 }
 
 // One run_variation call (solver.h:413-539); returns the energy.
@@ -2221,6 +2670,48 @@ void orc_rdm2(void* h, double* out) {
     for (const auto& e : m.rows[i])
       R.elements(s.sys.dets[e.first], e.first, s.sys.dets[i], i, 1.0, s.sys.n_up, s.sys.n_dn);
   std::copy(R.half.begin(), R.half.end(), out);
+}
+
+// Generalized Fock matrix (src/chem/optimization.cc:620-650) from given RDMs: g1[n*n] (one_rdm
+// (p, q) at p*n+q) and half (two_rdm in the half storage of rdm.cc:233-241).
+void orc_generalized_fock(void* h, const double* g1, const double* half, double* F) {
+  const auto& sys = S(h).sys;
+  const unsigned n = sys.n_orbs;
+  auto two = [&](unsigned p, unsigned q, unsigned r, unsigned s) {
+    const size_t a = (size_t)p * n + s, b = (size_t)q * n + r;
+    return a > b ? half[a * (a + 1) / 2 + b] : half[b * (b + 1) / 2 + a];
+  };
+#pragma omp parallel for collapse(2) schedule(dynamic)
+  for (unsigned i = 0; i < n; i++)
+    for (unsigned j = 0; j < n; j++) {
+      if (sys.I.orb_sym[i] != sys.I.orb_sym[j]) {
+        F[i * n + j] = 0.;
+        continue;
+      }
+      double elem = 0.;  // generalized_Fock_element (:635-650)
+      for (unsigned q = 0; q < n; q++) elem += g1[i * n + q] * sys.I.get_1b(j, q);
+      for (unsigned q = 0; q < n; q++)
+        for (unsigned r = 0; r < n; r++)
+          for (unsigned s = 0; s < n; s++) elem += two(i, r, s, q) * sys.I.get_2b(j, q, r, s);
+      F[i * n + j] = elem;
+    }
+}
+
+// Optimization::parameter_indices (optimization.cc:500-522) without an active space: pairs
+// i < j of equal irrep.  Returns the count; writes up to cap pairs.
+size_t orc_orbital_parameters(void* h, unsigned* p, unsigned* q, size_t cap) {
+  const auto& sys = S(h).sys;
+  size_t k = 0;
+  for (unsigned i = 0; i < sys.n_orbs; i++)
+    for (unsigned j = i + 1; j < sys.n_orbs; j++)
+      if (sys.I.orb_sym[i] == sys.I.orb_sym[j]) {
+        if (k < cap) {
+          p[k] = i;
+          q[k] = j;
+        }
+        k++;
+      }
+  return k;
 }
 
 }  // extern "C"

@@ -68,6 +68,19 @@ def load():
         "shci_davidson_csr": [vp, sz, _u64p, _u32p, _f64p, _f64p, _f64p, d, P(d), _f64p, P(i)],
         "shci_select": [vp, d, i, P(sz)],
         "shci_get_eps_tried": [vp, _f64p, sz],
+        "shci_set_second_rejection": [vp, i, d],
+        "shci_set_n_states": [vp, u],
+        "shci_set_time_sym": [vp, i],
+        "shci_unpack_time_sym": [vp],
+        "shci_generalized_fock": [vp, _f64p],
+        "shci_orbital_parameters": [vp, vp, vp, sz, P(sz)],
+        "shci_orbital_gradient": [vp, vp, vp, sz, _f64p],
+        "shci_get_state_coefs": [vp, u, _f64p, sz],
+        "shci_set_state_coefs": [vp, u, _f64p, sz],
+        "shci_get_state_energies": [vp, _f64p, sz],
+        "shci_get_var_trace_states": [vp, vp, sz, P(sz)],
+        "shci_davidson_csr_states": [vp, sz, _u64p, _u32p, _f64p, _f64p, u, _f64p, d, _f64p,
+                                     _f64p, P(i)],
         "shci_run_variation": [vp, _f64p, sz, vp, sz, d, i, _f64p],
         "shci_get_var_trace": [vp, _u64p, _u64p, _f64p, sz, P(sz)],
         "shci_get_launch_count": [vp, P(u64)],
@@ -358,6 +371,78 @@ class Context:
         n = ctypes.c_size_t()
         self._ck(self.L.shci_select(self.h, eps_var, int(var_sd), ctypes.byref(n)))
         return n.value
+
+    def generalized_fock(self):
+        n = self.n_orbs
+        F = np.zeros(n * n)
+        self._ck(self.L.shci_generalized_fock(self.h, F))
+        return F.reshape(n, n)
+
+    def orbital_parameters(self):
+        k = ctypes.c_size_t()
+        self._ck(self.L.shci_orbital_parameters(self.h, None, None, 0, ctypes.byref(k)))
+        p = np.zeros(k.value, np.uint32)
+        q = np.zeros(k.value, np.uint32)
+        self._ck(self.L.shci_orbital_parameters(self.h, p.ctypes.data, q.ctypes.data, k.value,
+                                                ctypes.byref(k)))
+        return p, q
+
+    def orbital_gradient(self, p, q):
+        p = np.ascontiguousarray(p, np.uint32)
+        q = np.ascontiguousarray(q, np.uint32)
+        g = np.zeros(len(p))
+        self._ck(self.L.shci_orbital_gradient(self.h, p.ctypes.data, q.ctypes.data, len(p), g))
+        return g
+
+    def set_time_sym(self, on=True):
+        self._ck(self.L.shci_set_time_sym(self.h, int(on)))
+
+    def unpack_time_sym(self):
+        self._ck(self.L.shci_unpack_time_sym(self.h))
+
+    def set_n_states(self, n):
+        self._ck(self.L.shci_set_n_states(self.h, n))
+        self.n_states = n
+
+    def state_coefs(self, s):
+        n = self.n_dets()
+        out = np.zeros(n)
+        self._ck(self.L.shci_get_state_coefs(self.h, s, out, n))
+        return out
+
+    def set_state_coefs(self, s, c):
+        c = np.ascontiguousarray(c, np.float64)
+        self._ck(self.L.shci_set_state_coefs(self.h, s, c, len(c)))
+
+    def state_energies(self):
+        ns = getattr(self, "n_states", 1)
+        out = np.zeros(ns)
+        self._ck(self.L.shci_get_state_energies(self.h, out, ns))
+        return out
+
+    def var_trace_states(self):
+        ns = getattr(self, "n_states", 1)
+        n = ctypes.c_size_t()
+        self._ck(self.L.shci_get_var_trace_states(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), ns))
+        self._ck(self.L.shci_get_var_trace_states(self.h, out.ctypes.data, out.size,
+                                                  ctypes.byref(n)))
+        return out[: n.value]
+
+    def davidson_csr_states(self, row_ptr, cols, vals, diag, init, tol):
+        init = np.ascontiguousarray(init, np.float64)
+        ns, n = init.shape
+        ev = np.zeros(ns)
+        vecs = np.zeros((ns, n))
+        conv = ctypes.c_int()
+        self._ck(self.L.shci_davidson_csr_states(
+            self.h, n, np.ascontiguousarray(row_ptr, np.uint64),
+            np.ascontiguousarray(cols, np.uint32), np.ascontiguousarray(vals, np.float64),
+            np.ascontiguousarray(diag, np.float64), ns, init, tol, ev, vecs, ctypes.byref(conv)))
+        return ev, vecs, bool(conv.value)
+
+    def set_second_rejection(self, enable=True, factor=0.2):
+        self._ck(self.L.shci_set_second_rejection(self.h, int(enable), factor))
 
     def eps_tried(self):
         n = self.n_dets()

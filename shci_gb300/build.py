@@ -76,7 +76,8 @@ CLI = os.path.join(HERE, "bin", "shci_gpu")
 def build_cli():
     """The drop-in driver: links only the C ABI of libshci_gpu.so."""
     os.makedirs(os.path.dirname(CLI), exist_ok=True)
-    deps = [CLI_SRC, os.path.join(HERE, "cli", "json.h"), LIB]
+    deps = [CLI_SRC, os.path.join(HERE, "cli", "json.h"), os.path.join(HERE, "cli", "wf_file.h"),
+            LIB]
     if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(d) for d in deps):
         return CLI
     cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"), CLI_SRC,

@@ -8,7 +8,13 @@
 // (energy_hf, n_elecs, config, energy_var/<eps>, energy_total/<eps_var>/<eps_pt>/{value,
 // uncert}) and printing the reference's grep-able lines ("Final iteration ... energy=",
 // "Total energy: ...").  All computation goes through the C ABI of include/shci_gpu.h.
+// After each eps_var the wavefunction is saved to wf_eps1_<eps_var>.dat, and an eps_var whose
+// file exists is loaded instead of computed (force_var recomputes); the PT2 stage takes its
+// wavefunctions from those files under skip_var (solver.h:348-397, 571-575; format in
+// wf_file.h).
 //
+// Also honoured as the reference does: n_states (several states, state-suffixed result keys),
+// second_rejection / second_rejection_factor, the linear point groups.
 // GPU-specific keys (ignored by the reference): gpu/device (default 0), gpu/precision
 // ("mixed" default, or "fp64").
 #include <shci_gpu.h>
@@ -25,6 +31,7 @@
 #include <unistd.h>
 
 #include "json.h"
+#include "wf_file.h"
 
 using shci_cli::Json;
 
@@ -116,11 +123,110 @@ void result_put(const std::string& k, double v) {
 
 std::string key_eps(double e) { return fmt("%#.2e", e); }
 
+std::string wf_filename(double eps_var) { return fmt("wf_eps1_%#.2e.dat", eps_var); }
+
 struct Wavefunction {
-  double eps_var = 0.0, energy = 0.0;
+  double eps_var = 0.0, energy = 0.0;  // energy of state 0
   std::vector<uint64_t> up, dn;
-  std::vector<double> coefs;
+  std::vector<double> coefs;                // state 0
+  std::vector<std::vector<double>> xcoefs;  // states 1..
+  std::vector<double> xenergy;              // states 1..
+  size_t n_states() const { return 1 + xcoefs.size(); }
+  double energy_of(size_t k) const { return k == 0 ? energy : xenergy[k - 1]; }
+  const std::vector<double>& coefs_of(size_t k) const { return k == 0 ? coefs : xcoefs[k - 1]; }
 };
+
+// "" for state 0, "_<k>" otherwise (Solver::get_state_suffix, solver.h:1406-1412)
+std::string state_suffix(size_t k) { return k == 0 ? "" : "_" + std::to_string(k); }
+
+// unpack_time_sym (base_system.h:108-123): each det with up < dn gets its reverse appended,
+// both coefficients (every state) times 1/sqrt(2) (Util::SQRT2_INV, src/util.h:60).
+Wavefunction unpacked(const Wavefunction& wf) {
+  constexpr double kSqrt2Inv = 0.7071067811865475;
+  Wavefunction u = wf;
+  const size_t n = wf.up.size();
+  for (size_t i = 0; i < n; i++)
+    if (wf.up[i] < wf.dn[i]) {
+      auto half = [&](std::vector<double>& v) {
+        const double h = v[i] * kSqrt2Inv;
+        v[i] = h;
+        v.push_back(h);
+      };
+      half(u.coefs);
+      for (auto& xc : u.xcoefs) half(xc);
+      u.up.push_back(wf.dn[i]);
+      u.dn.push_back(wf.up[i]);
+    }
+  return u;
+}
+
+// The context's det list and every state's coefficients become wf's.
+void put_wf(shci_ctx* c, const Wavefunction& wf) {
+  ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), wf.up.size()), "dets");
+  for (size_t k = 1; k < wf.n_states(); k++)
+    ck(c, shci_set_state_coefs(c, (unsigned)k, wf.xcoefs[k - 1].data(), wf.up.size()),
+       "state coefficients");
+}
+
+// load_variation_result (solver.h:1179-1211) for this build's files; prints what the
+// reference prints on success.  A file of another format is reported and left alone.
+bool load_wf(const std::string& fn, unsigned n_up, unsigned n_dn, unsigned n_states,
+             bool time_sym, double eps_var, Wavefunction* wf) {
+  shci_cli::WfFile w;
+  const auto st = shci_cli::wf_load(fn, &w);
+  if (st == shci_cli::WfStatus::kForeign || st == shci_cli::WfStatus::kBad) {
+    std::printf("%s is not a wavefunction file of this build; not loaded\n", fn.c_str());
+    return false;
+  }
+  if (st != shci_cli::WfStatus::kOk) return false;
+  if (w.n_up != n_up || w.n_dn != n_dn || w.n_states != n_states ||
+      w.time_sym != (time_sym ? 1u : 0u)) {
+    std::printf("%s holds %u/%u electrons, %u states, time_sym %u; not loaded\n", fn.c_str(),
+                w.n_up, w.n_dn, w.n_states, w.time_sym);
+    return false;
+  }
+  std::printf("Loaded %'zu dets from: %s\n", w.up.size(), fn.c_str());
+  std::printf("HF energy: %.10f Ha\n", w.energy_hf);
+  std::printf("Variational energy: ");
+  for (double e : w.energy_var) std::printf("%.10f\t", e);
+  std::printf("\n");
+  const size_t n = w.up.size();
+  wf->eps_var = eps_var;
+  wf->energy = w.energy_var[0];
+  wf->up = std::move(w.up);
+  wf->dn = std::move(w.dn);
+  wf->coefs.assign(w.coefs.begin(), w.coefs.begin() + n);
+  wf->xcoefs.clear();
+  wf->xenergy.clear();
+  for (unsigned k = 1; k < w.n_states; k++) {
+    wf->xcoefs.emplace_back(w.coefs.begin() + k * n, w.coefs.begin() + (k + 1) * n);
+    wf->xenergy.push_back(w.energy_var[k]);
+  }
+  return true;
+}
+
+// save_variation_result (solver.h:1213-1221); a file of another format is not overwritten
+void save_wf(const std::string& fn, unsigned n_up, unsigned n_dn, bool time_sym, double e_hf,
+             const Wavefunction& wf) {
+  if (shci_cli::wf_probe(fn) == shci_cli::WfStatus::kForeign) {
+    std::printf("%s exists in another format; not overwritten\n", fn.c_str());
+    return;
+  }
+  shci_cli::WfFile w;
+  w.n_up = n_up;
+  w.n_dn = n_dn;
+  w.energy_hf = e_hf;
+  w.time_sym = time_sym ? 1u : 0u;
+  w.n_states = static_cast<unsigned>(wf.n_states());
+  w.up = wf.up;
+  w.dn = wf.dn;
+  for (size_t k = 0; k < wf.n_states(); k++) {
+    w.energy_var.push_back(wf.energy_of(k));
+    w.coefs.insert(w.coefs.end(), wf.coefs_of(k).begin(), wf.coefs_of(k).end());
+  }
+  if (shci_cli::wf_save(fn, w)) std::printf("Variational results saved to: %s\n", fn.c_str());
+  else std::printf("cannot write %s\n", fn.c_str());
+}
 
 }  // namespace
 
@@ -156,8 +262,8 @@ int main(int, char* argv[]) {
   std::printf("Configuration:\n%s\n", shci_cli::dump(g_config).c_str());
   const std::string system = cfg_s("system", "", true);
   if (system != "chem") die("system '" + system + "' is not supported.");
-  if (cfg_d("n_states", 1) != 1) die("n_states > 1 is not supported by this build");
-  if (cfg_b("time_sym", false)) die("time_sym is not supported by this build");
+  const unsigned n_states = static_cast<unsigned>(cfg_d("n_states", 1));
+  const bool time_sym = cfg_b("time_sym", false);
   const unsigned n_up = static_cast<unsigned>(cfg_d("n_up", 0, true));
   const unsigned n_dn = static_cast<unsigned>(cfg_d("n_dn", 0, true));
   const std::string pg = cfg_s("chem/point_group", "", true);
@@ -180,6 +286,11 @@ int main(int, char* argv[]) {
   ck(c, shci_get_hf(c, &hf_up, &hf_dn, &e_hf), "HF det");
   int n_orbs = 0;
   ck(c, shci_get_integrals(c, &n_orbs, nullptr, nullptr, nullptr, nullptr, nullptr), "integrals");
+  ck(c, shci_set_n_states(c, n_states), "n_states");
+  if (time_sym) ck(c, shci_set_time_sym(c, 1), "time_sym");
+  ck(c, shci_set_second_rejection(c, cfg_b("second_rejection", false) ? 1 : 0,
+                                  cfg_d("second_rejection_factor", 0.2)),
+     "second rejection");
   double qinfo[4];
   ck(c, shci_build_queues(c, qinfo), "heat-bath queues");
   std::printf("Max hci queue elem: %.10f Ha\nNumber of entries in hci queue: %'zu\n", qinfo[0],
@@ -203,6 +314,19 @@ int main(int, char* argv[]) {
     size_t it_s = 0;
     size_t it_global = 0;
     for (double eps_var : eps_vars) {
+      const std::string fn = wf_filename(eps_var);
+      std::printf("Try Loading Wavefunction %s\n", fn.c_str());
+      Wavefunction lw;
+      if (!cfg_b("force_var", false) &&
+          load_wf(fn, n_up, n_dn, n_states, time_sym, eps_var, &lw)) {
+        // solver.h:381-388: continue from the loaded wavefunction, memo cleared
+        put_wf(c, lw);
+        for (size_t k = 0; k < lw.n_states(); k++)
+          result_put("energy_var" + state_suffix(k) + "/" + key_eps(eps_var), lw.energy_of(k));
+        wfs.push_back(std::move(lw));
+        eps_prev = eps_var;
+        continue;
+      }
       std::vector<double> sched;
       while (it_s < schedule.size() && schedule[it_s] >= eps_prev) it_s++;
       while (it_s < schedule.size() && schedule[it_s] > eps_var) sched.push_back(schedule[it_s++]);
@@ -215,11 +339,15 @@ int main(int, char* argv[]) {
       std::vector<uint64_t> nd(n_it), nz(n_it);
       std::vector<double> en(n_it);
       ck(c, shci_get_var_trace(c, nd.data(), nz.data(), en.data(), n_it, &n_it), "trace");
+      std::vector<double> es(n_it * n_states);
+      ck(c, shci_get_var_trace_states(c, es.data(), es.size(), &n_it), "trace");
       for (size_t k = 0; k < n_it; k++) {
         const double eps_k = k < sched.size() ? sched[k] : eps_var;
         std::printf("Number of nonzero elems: %'zu\n", (size_t)nz[k]);
-        std::printf("Iteration %zu eps1= %#.2e ndets= %'zu energy= %.8f\n", ++it_global, eps_k,
-                    (size_t)nd[k], en[k]);
+        std::printf("Iteration %zu eps1= %#.2e ndets= %'zu energy=", ++it_global, eps_k,
+                    (size_t)nd[k]);
+        for (unsigned st = 0; st < n_states; st++) std::printf(" %.8f", es[k * n_states + st]);
+        std::printf("\n");
       }
       Wavefunction wf;
       wf.eps_var = eps_var;
@@ -230,9 +358,19 @@ int main(int, char* argv[]) {
       wf.dn.resize(n);
       wf.coefs.resize(n);
       ck(c, shci_get_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), n), "dets");
-      std::printf("Final iteration %zu eps1= %#.2e ndets= %'zu energy=  %.8f\n", it_global, eps_var,
-                  n, e);
-      result_put("energy_var/" + key_eps(eps_var), e);
+      std::vector<double> se(n_states);
+      ck(c, shci_get_state_energies(c, se.data(), n_states), "state energies");
+      for (unsigned st = 1; st < n_states; st++) {
+        wf.xcoefs.emplace_back(n);
+        ck(c, shci_get_state_coefs(c, st, wf.xcoefs.back().data(), n), "state coefficients");
+        wf.xenergy.push_back(se[st]);
+      }
+      std::printf("Final iteration %zu eps1= %#.2e ndets= %'zu energy=", it_global, eps_var, n);
+      for (unsigned st = 0; st < n_states; st++) std::printf("  %.8f", wf.energy_of(st));
+      std::printf("\n");
+      for (unsigned st = 0; st < n_states; st++)
+        result_put("energy_var" + state_suffix(st) + "/" + key_eps(eps_var), wf.energy_of(st));
+      save_wf(fn, n_up, n_dn, time_sym, e_hf, wf);
       wfs.push_back(std::move(wf));
       eps_prev = eps_var;
     }
@@ -240,9 +378,12 @@ int main(int, char* argv[]) {
 
   const bool want_1rdm = cfg_b("get_1rdm_csv", false);
   const bool want_2rdm = cfg_b("2rdm", false) || cfg_b("get_2rdm_csv", false);
+  // from here on the wavefunctions are used unpacked (solver.h:593; the reference's RDM code
+  // reads packed time_sym dets with the same result)
+  if (time_sym) ck(c, shci_set_time_sym(c, 0), "time_sym");
   if ((want_1rdm || want_2rdm) && !wfs.empty()) {
-    const Wavefunction& wf = wfs.back();
-    ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), wf.up.size()), "dets");
+    const Wavefunction wf = time_sym ? unpacked(wfs.back()) : wfs.back();
+    put_wf(c, wf);  // the RDMs sum over the states (rdm.cc:222-231)
     std::vector<unsigned> order(n_orbs), inv(n_orbs);
     ck(c, shci_get_integrals(c, nullptr, nullptr, nullptr, nullptr, nullptr, order.data()), "order");
     for (int i = 0; i < n_orbs; i++) inv[order[i]] = i;
@@ -306,7 +447,18 @@ int main(int, char* argv[]) {
   }
 
   // Perturbation for each eps_var (solver.h:399-411, 541-634)
-  for (const Wavefunction& wf : wfs) {
+  for (const double eps_var_cfg : eps_vars) {
+    const Wavefunction* wp = nullptr;
+    for (const Wavefunction& w : wfs)
+      if (w.eps_var == eps_var_cfg) wp = &w;
+    Wavefunction lw;
+    if (!wp) {  // skip_var: the wavefunction comes from its file (solver.h:571-575)
+      if (!load_wf(wf_filename(eps_var_cfg), n_up, n_dn, n_states, time_sym, eps_var_cfg, &lw))
+        die("cannot load variation results from " + wf_filename(eps_var_cfg));
+      wp = &lw;
+    }
+    const Wavefunction uw = time_sym ? unpacked(*wp) : Wavefunction();
+    const Wavefunction& wf = time_sym ? uw : *wp;
     const double eps_var = wf.eps_var;
     double eps_pt_dtm = std::max(2.0e-6, cfg_d("eps_pt_dtm_ratio", 0.1) * eps_var);
     double eps_pt_psto = std::max(1.0e-7, cfg_d("eps_pt_psto_ratio", 0.01) * eps_var);
@@ -316,63 +468,77 @@ int main(int, char* argv[]) {
     eps_pt = cfg_d("eps_pt", eps_pt);
     if (eps_pt_psto < eps_pt) eps_pt_psto = eps_pt;
     if (eps_pt_dtm < eps_pt_psto) eps_pt_dtm = eps_pt_psto;
-    const std::string base = "energy_total/" + key_eps(eps_var) + "/" + key_eps(eps_pt);
-    const Json* have = g_result.get(base + "/value");
-    if (have && have->type == Json::Number && have->num != 0.0 && !cfg_b("force_pt", false)) {
-      const Json* hu = g_result.get(base + "/uncert");
-      std::printf("Total energy: %.10f +- %.10f (state 0, loaded from result file)\n", have->num,
-                  hu ? hu->num : 0.0);
-      continue;
-    }
-    ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs.data(), wf.up.size()), "dets");
-    double dtm = 0.0, u_dtm = 0.0;
-    size_t n_dtm = 0;
-    ck(c, shci_pt2_dtm(c, wf.energy, eps_pt_dtm, (size_t)cfg_d("n_batches_pt_dtm", 0), &dtm,
-                       &u_dtm, &n_dtm),
-       "PT2 dtm");
-    std::printf("Number of dtm pt dets: %'zu\n", n_dtm);
-    std::printf("PT dtm correction (eps1= %.2e, eps_pt_dtm= %.2e): %.10f +- %.10f Ha\n", eps_var,
-                eps_pt_dtm, dtm, u_dtm);
-    double value = wf.energy + dtm, uncert = 0.0;
-    double psto = 0.0, u_psto = 0.0;
-    if (eps_pt_psto < eps_pt_dtm) {
-      size_t n_psto = 0, nb = 0;
-      const size_t nb_psto = std::max<size_t>(16, (size_t)cfg_d("n_batches_pt_psto", 16));
-      ck(c, shci_pt2_psto(c, wf.energy, eps_pt_dtm, eps_pt_psto, nb_psto, target_error, eps_pt,
-                          &psto, &u_psto, &n_psto, &nb),
-         "PT2 psto");
-      std::printf("PT psto correction (eps1= %.2e, eps_pt_psto= %.2e): %.10f +- %.10f Ha\n",
-                  eps_var, eps_pt_psto, psto, u_psto);
-      value += psto;
-      uncert = u_psto;
-    }
-    if (eps_pt < eps_pt_psto) {
-      // solver.h:905-1036: the sample size comes from the pilot and the PT memory unless
-      // n_dets_in_sample_pt_sto is set; semisto_sto (default true) needs the pilot
-      const size_t n_samples = (size_t)cfg_d("n_dets_in_sample_pt_sto", 0);
-      const bool semisto = cfg_b("semisto_sto", true);
-      double pt_mem = 0.0;
-      ck(c, shci_pt_mem_avail(c, cfg_d("mem_total", machine_memory()), &pt_mem), "PT memory");
-      double sto = 0.0, u_sto = 0.0;
-      size_t iters = 0, info[3] = {0, 0, 0};
-      ck(c, shci_pt2_sto(c, wf.energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),
-                         n_samples, semisto ? 1 : 0, (unsigned)cfg_d("random_seed", 347634253),
-                         (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, pt_mem,
-                         cfg_d("pt_sto_mem_usage", 0.4), &sto, &u_sto, &iters, info, nullptr, 0),
-         "PT2 sto");
-      if (n_samples == 0) {
-        std::printf("Number of unique var dets in sample target: %'zu\n", info[2]);
-        std::printf("Number of dets chosen: %'zu\n", info[0]);
+    // solver.h:546-568: skipped when every state's total is in result.json
+    auto base_of = [&](size_t st) {
+      return "energy_total" + state_suffix(st) + "/" + key_eps(eps_var) + "/" + key_eps(eps_pt);
+    };
+    bool missing = false;
+    for (size_t st = 0; st < wf.n_states(); st++) {
+      const Json* have = g_result.get(base_of(st) + "/value");
+      if (have && have->type == Json::Number && have->num != 0.0) {
+        const Json* hu = g_result.get(base_of(st) + "/uncert");
+        std::printf("Total energy: %.10f +- %.10f (state %zu, loaded from result file)\n",
+                    have->num, hu ? hu->num : 0.0, st);
+      } else {
+        missing = true;
       }
-      if (semisto) std::printf("Number of deterministic var dets: %'zu\n", info[1]);
-      std::printf("PT sto correction (eps1= %.2e, eps_pt= %.2e): %.10f +- %.10f Ha\n", eps_var,
-                  eps_pt, sto, u_sto);
-      value += sto;
-      uncert = std::sqrt(uncert * uncert + u_sto * u_sto);
     }
-    std::printf("Total energy: %.10f +- %.10f Ha (state 0)\n", value, uncert);
-    result_put(base + "/value", value);
-    result_put(base + "/uncert", uncert);
+    if (!missing && !cfg_b("force_pt", false)) continue;
+    for (size_t st = 0; st < wf.n_states(); st++) {
+      // state st: its coefficients and energy (solver.h:620-632)
+      const std::string base = base_of(st);
+      const double energy = wf.energy_of(st);
+      ck(c, shci_set_dets(c, wf.up.data(), wf.dn.data(), wf.coefs_of(st).data(), wf.up.size()),
+         "dets");
+      double dtm = 0.0, u_dtm = 0.0;
+      size_t n_dtm = 0;
+      ck(c, shci_pt2_dtm(c, energy, eps_pt_dtm, (size_t)cfg_d("n_batches_pt_dtm", 0), &dtm,
+                         &u_dtm, &n_dtm),
+         "PT2 dtm");
+      std::printf("Number of dtm pt dets: %'zu\n", n_dtm);
+      std::printf("PT dtm correction (eps1= %.2e, eps_pt_dtm= %.2e): %.10f +- %.10f Ha\n", eps_var,
+                  eps_pt_dtm, dtm, u_dtm);
+      double value = energy + dtm, uncert = 0.0;
+      double psto = 0.0, u_psto = 0.0;
+      if (eps_pt_psto < eps_pt_dtm) {
+        size_t n_psto = 0, nb = 0;
+        const size_t nb_psto = std::max<size_t>(16, (size_t)cfg_d("n_batches_pt_psto", 16));
+        ck(c, shci_pt2_psto(c, energy, eps_pt_dtm, eps_pt_psto, nb_psto, target_error, eps_pt,
+                            &psto, &u_psto, &n_psto, &nb),
+           "PT2 psto");
+        std::printf("PT psto correction (eps1= %.2e, eps_pt_psto= %.2e): %.10f +- %.10f Ha\n",
+                    eps_var, eps_pt_psto, psto, u_psto);
+        value += psto;
+        uncert = u_psto;
+      }
+      if (eps_pt < eps_pt_psto) {
+        // solver.h:905-1036: the sample size comes from the pilot and the PT memory unless
+        // n_dets_in_sample_pt_sto is set; semisto_sto (default true) needs the pilot
+        const size_t n_samples = (size_t)cfg_d("n_dets_in_sample_pt_sto", 0);
+        const bool semisto = cfg_b("semisto_sto", true);
+        double pt_mem = 0.0;
+        ck(c, shci_pt_mem_avail(c, cfg_d("mem_total", machine_memory()), &pt_mem), "PT memory");
+        double sto = 0.0, u_sto = 0.0;
+        size_t iters = 0, info[3] = {0, 0, 0};
+        ck(c, shci_pt2_sto(c, energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),
+                           n_samples, semisto ? 1 : 0, (unsigned)cfg_d("random_seed", 347634253),
+                           (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, pt_mem,
+                           cfg_d("pt_sto_mem_usage", 0.4), &sto, &u_sto, &iters, info, nullptr, 0),
+           "PT2 sto");
+        if (n_samples == 0) {
+          std::printf("Number of unique var dets in sample target: %'zu\n", info[2]);
+          std::printf("Number of dets chosen: %'zu\n", info[0]);
+        }
+        if (semisto) std::printf("Number of deterministic var dets: %'zu\n", info[1]);
+        std::printf("PT sto correction (eps1= %.2e, eps_pt= %.2e): %.10f +- %.10f Ha\n", eps_var,
+                    eps_pt, sto, u_sto);
+        value += sto;
+        uncert = std::sqrt(uncert * uncert + u_sto * u_sto);
+      }
+      std::printf("Total energy: %.10f +- %.10f Ha (state %zu)\n", value, uncert, st);
+      result_put(base + "/value", value);
+      result_put(base + "/uncert", uncert);
+    }
   }
   shci_destroy(c);
   return 0;

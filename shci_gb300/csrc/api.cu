@@ -50,6 +50,19 @@ void need_dets(shci_ctx* c) {
   if (c->up.empty()) throw ArgError("no determinants set");
 }
 
+// States 1 .. n_states - 1 start at 1e-16 on each of the n current dets (chem_system.cc:52-56)
+void reset_states(shci_ctx* c, size_t n) {
+  const std::vector<double> tiny(n, 1e-16);
+  for (unsigned k = 1; k < c->n_states; k++) {
+    auto& xc = c->d_xcoef[k - 1];
+    xc.mt = &c->mem;
+    xc.resize(n, 1.1);
+    SHCI_CUDA(cudaMemcpyAsync(xc.p, tiny.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+  }
+  SHCI_CUDA(cudaStreamSynchronize(c->stream));
+  c->state_energy.assign(c->n_states, 0.0);
+}
+
 void after_integrals(shci_ctx* c) {
   upload_integrals(c);
   c->have_integrals = true;
@@ -62,7 +75,51 @@ void after_integrals(shci_ctx* c) {
   c->H.valid = false;
   c->H.prefix_ok = false;
   c->H.build_id++;
+  reset_states(c, 1);
 }
+
+// An explicit upper-triangle CSR (FP64) becomes the context's Hamiltonian (Davidson tests).
+void load_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr, const uint32_t* cols,
+              const double* vals, const double* diag) {
+  auto& H = c->H;
+  cudaStream_t s = c->stream;
+  const size_t nnz = row_ptr[n];
+  H.older.clear();
+  H.prefix_ok = false;
+  H.n = n;
+  H.nnz = nnz;
+  H.nnz_current = nnz;
+  H.precision = SHCI_PREC_FP64;
+  H.row_ptr.resize(n + 1);
+  H.col.resize(nnz ? nnz : 1);
+  H.val64.resize(nnz ? nnz : 1);
+  H.diag.resize(n);
+  SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p, row_ptr, (n + 1) * 8, cudaMemcpyHostToDevice, s));
+  std::vector<uint32_t> len(n);
+  for (size_t i = 0; i < n; i++) len[i] = static_cast<uint32_t>(row_ptr[i + 1] - row_ptr[i]);
+  H.row_cnt.resize(n + 1);
+  SHCI_CUDA(cudaMemcpyAsync(H.row_cnt.p, len.data(), n * 4, cudaMemcpyHostToDevice, s));
+  H.packed = true;
+  H.bound_valid = false;
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  if (nnz) {
+    SHCI_CUDA(cudaMemcpyAsync(H.col.p, cols, nnz * 4, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(H.val64.p, vals, nnz * 8, cudaMemcpyHostToDevice, s));
+  }
+  SHCI_CUDA(cudaMemcpyAsync(H.diag.p, diag, n * 8, cudaMemcpyHostToDevice, s));
+  H.valid = true;
+  H.build_id++;
+}
+
+// After a CSR Davidson the context's own Hamiltonian and coefficients are gone.
+void drop_csr(shci_ctx* c) {
+  c->H.valid = false;
+  c->H.prefix_ok = false;
+  c->H.older.clear();
+  c->H.build_id++;
+  c->dets_dirty = true;
+}
+
 
 }  // namespace
 
@@ -160,7 +217,7 @@ shci_status shci_set_integrals(shci_ctx* c, int n_orbs, unsigned n_up, unsigned 
     I.n_up = n_up;
     I.n_dn = n_dn;
     I.e_core = e_core;
-    I.n_syms = point_group_order(point_group ? point_group : "C1");
+    I.n_syms = point_group_order(point_group ? point_group : "C1", &I.linear);
     I.h1.assign(h1, h1 + n * n);
     I.g2.assign(g2, g2 + n * n * n * n);
     I.orb_sym.resize(n);
@@ -171,6 +228,7 @@ shci_status shci_set_integrals(shci_ctx* c, int n_orbs, unsigned n_up, unsigned 
     }
     if (__builtin_popcountll(hf_up) != (int)n_up || __builtin_popcountll(hf_dn) != (int)n_dn)
       throw ArgError("HF det does not match n_up / n_dn");
+    screen_linear(I);
     I.hf_up = hf_up;
     I.hf_dn = hf_dn;
     c->I = std::move(I);
@@ -253,6 +311,110 @@ shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
     c->H.valid = false;
     c->H.prefix_ok = false;
     c->H.build_id++;
+    reset_states(c, n);
+  });
+}
+
+shci_status shci_set_n_states(shci_ctx* c, unsigned n_states) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (n_states < 1 || n_states > kMaxStates)
+      throw ArgError("n_states must be in [1, " + std::to_string(kMaxStates) + "]");
+    c->n_states = n_states;
+    reset_states(c, c->up.size());
+  });
+}
+
+shci_status shci_set_time_sym(shci_ctx* c, int on) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (on) {
+      if (c->I.n_up != c->I.n_dn) throw ArgError("time_sym needs n_up == n_dn");
+      for (size_t i = 0; i < c->up.size(); i++)
+        if (c->up[i] > c->dn[i])
+          throw ArgError("time_sym needs every det in the form up <= dn (det " +
+                         std::to_string(i) + ")");
+    }
+    c->time_sym = on != 0;
+    c->H.valid = false;
+    c->H.prefix_ok = false;
+    c->H.build_id++;
+    c->eps_tried.clear();
+  });
+}
+
+shci_status shci_unpack_time_sym(shci_ctx* c) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_dets(c);
+    if (!c->time_sym) throw ArgError("the context is not in time_sym mode");
+    const size_t n = c->up.size();
+    const unsigned ns = c->n_states;
+    std::vector<std::vector<double>> cs(ns, std::vector<double>(n));
+    sync_dets(c);
+    for (unsigned k = 0; k < ns; k++)
+      SHCI_CUDA(cudaMemcpyAsync(cs[k].data(), state_coef(c, k), n * 8, cudaMemcpyDeviceToHost,
+                                c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<uint64_t> up(c->up), dn(c->dn);
+    constexpr double kSqrt2Inv = 0.7071067811865475;  // Util::SQRT2_INV (src/util.h:60)
+    for (size_t i = 0; i < n; i++)  // base_system.h:108-123
+      if (up[i] < dn[i]) {
+        for (auto& v : cs) {
+          const double h = v[i] * kSqrt2Inv;
+          v[i] = h;
+          v.push_back(h);
+        }
+        up.push_back(dn[i]);
+        dn.push_back(up[i]);
+      }
+    c->time_sym = false;
+    const shci_status st = shci_set_dets(c, up.data(), dn.data(), cs[0].data(), up.size());
+    if (st != SHCI_OK) throw ArgError(c->err);
+    for (unsigned k = 1; k < ns; k++) {
+      const shci_status sk = shci_set_state_coefs(c, k, cs[k].data(), up.size());
+      if (sk != SHCI_OK) throw ArgError(c->err);
+    }
+  });
+}
+
+shci_status shci_get_state_coefs(shci_ctx* c, unsigned state, double* coefs, size_t cap) {
+  if (!c || !coefs) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_dets(c);
+    if (state >= c->n_states) throw ArgError("state index >= n_states");
+    const size_t n = c->up.size();
+    if (cap < n) throw ArgError("coefficient buffer too small");
+    sync_dets(c);
+    SHCI_CUDA(cudaMemcpyAsync(coefs, state_coef(c, state), n * 8, cudaMemcpyDeviceToHost,
+                              c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+shci_status shci_set_state_coefs(shci_ctx* c, unsigned state, const double* coefs, size_t n) {
+  if (!c || !coefs) return SHCI_ERR_ARG;
+  if (state == 0) return shci_set_coefs(c, coefs, n);
+  return guard(c, [&]() {
+    need_dets(c);
+    if (state >= c->n_states) throw ArgError("state index >= n_states");
+    if (n != c->up.size()) throw ArgError("coefficient count != det count");
+    SHCI_CUDA(cudaMemcpyAsync(state_coef(c, state), coefs, n * 8, cudaMemcpyHostToDevice,
+                              c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    c->dav.ritz = false;
+  });
+}
+
+shci_status shci_get_state_energies(shci_ctx* c, double* energies, size_t cap) {
+  if (!c || !energies) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    for (size_t k = 0; k < c->n_states && k < cap; k++)
+      energies[k] = k < c->state_energy.size() ? c->state_energy[k] : 0.0;
   });
 }
 
@@ -502,52 +664,81 @@ shci_status shci_energy_fp64(shci_ctx* c, double* energy) {
   });
 }
 
+
 shci_status shci_davidson_csr(shci_ctx* c, size_t n, const uint64_t* row_ptr,
                               const uint32_t* cols, const double* vals, const double* diag,
                               const double* init, double tol, double* eval, double* evec,
                               int* converged) {
   if (!c) return SHCI_ERR_ARG;
   return guard(c, [&]() {
-    auto& H = c->H;
     cudaStream_t s = c->stream;
-    const size_t nnz = row_ptr[n];
-    H.older.clear();
-    H.prefix_ok = false;
-    H.n = n;
-    H.nnz = nnz;
-    H.nnz_current = nnz;
-    H.precision = SHCI_PREC_FP64;
-    H.row_ptr.resize(n + 1);
-    H.col.resize(nnz ? nnz : 1);
-    H.val64.resize(nnz ? nnz : 1);
-    H.diag.resize(n);
-    SHCI_CUDA(cudaMemcpyAsync(H.row_ptr.p, row_ptr, (n + 1) * 8, cudaMemcpyHostToDevice, s));
-    std::vector<uint32_t> len(n);
-    for (size_t i = 0; i < n; i++) len[i] = static_cast<uint32_t>(row_ptr[i + 1] - row_ptr[i]);
-    H.row_cnt.resize(n + 1);
-    SHCI_CUDA(cudaMemcpyAsync(H.row_cnt.p, len.data(), n * 4, cudaMemcpyHostToDevice, s));
-    H.packed = true;
-    H.bound_valid = false;
-    SHCI_CUDA(cudaStreamSynchronize(s));
-    if (nnz) {
-      SHCI_CUDA(cudaMemcpyAsync(H.col.p, cols, nnz * 4, cudaMemcpyHostToDevice, s));
-      SHCI_CUDA(cudaMemcpyAsync(H.val64.p, vals, nnz * 8, cudaMemcpyHostToDevice, s));
-    }
-    SHCI_CUDA(cudaMemcpyAsync(H.diag.p, diag, n * 8, cudaMemcpyHostToDevice, s));
+    load_csr(c, n, row_ptr, cols, vals, diag);
     c->d_coef.resize(n);
     SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, init, n * 8, cudaMemcpyHostToDevice, s));
-    H.valid = true;
-    H.build_id++;
-    auto r = davidson(c, tol);
+    const unsigned ns = c->n_states;
+    c->n_states = 1;
+    DavidsonOut r;
+    try {
+      r = davidson(c, tol);
+    } catch (...) {
+      c->n_states = ns;
+      drop_csr(c);
+      throw;
+    }
+    c->n_states = ns;
     SHCI_CUDA(cudaMemcpyAsync(evec, c->d_coef.p, n * 8, cudaMemcpyDeviceToHost, s));
     SHCI_CUDA(cudaStreamSynchronize(s));
     *eval = r.eval;
     if (converged) *converged = r.converged ? 1 : 0;
-    H.valid = false;  // the context's own Hamiltonian is gone
-    H.prefix_ok = false;
-    H.older.clear();
-    H.build_id++;
-    c->dets_dirty = true;  // coefficients were overwritten
+    drop_csr(c);
+  });
+}
+
+shci_status shci_davidson_csr_states(shci_ctx* c, size_t n, const uint64_t* row_ptr,
+                                     const uint32_t* cols, const double* vals,
+                                     const double* diag, unsigned n_states, const double* init,
+                                     double tol, double* evals, double* evecs, int* converged) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (n_states < 1 || n_states > kMaxStates)
+      throw ArgError("n_states must be in [1, " + std::to_string(kMaxStates) + "]");
+    if (!init || !evals || !evecs || n == 0) throw ArgError("null or empty argument");
+    cudaStream_t s = c->stream;
+    load_csr(c, n, row_ptr, cols, vals, diag);
+    const unsigned ns_ctx = c->n_states;
+    c->n_states = n_states;
+    auto restore = [&]() {
+      c->n_states = ns_ctx;
+      drop_csr(c);
+      if (!c->up.empty()) reset_states(c, c->up.size());
+    };
+    try {
+      for (unsigned k = 0; k < n_states; k++) {
+        auto& b = k == 0 ? c->d_coef : c->d_xcoef[k - 1];
+        b.mt = &c->mem;
+        b.resize(n, 1.1);
+        SHCI_CUDA(cudaMemcpyAsync(b.p, init + k * n, n * 8, cudaMemcpyHostToDevice, s));
+      }
+      DavidsonStatesOut r;
+      if (n_states == 1) {
+        DavidsonOut r1 = davidson(c, tol);
+        r.evals.assign(1, r1.eval);
+        r.converged = r1.converged;
+      } else {
+        r = davidson_states(c, tol);
+      }
+      for (unsigned k = 0; k < n_states; k++) {
+        SHCI_CUDA(cudaMemcpyAsync(evecs + k * n, state_coef(c, k), n * 8, cudaMemcpyDeviceToHost,
+                                  s));
+        evals[k] = r.evals[k];
+      }
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      if (converged) *converged = r.converged ? 1 : 0;
+    } catch (...) {
+      restore();
+      throw;
+    }
+    restore();
   });
 }
 
@@ -560,6 +751,15 @@ shci_status shci_select(shci_ctx* c, double eps_var, int var_sd, size_t* n_new) 
     if (n_new) *n_new = k;
     c->H.valid = false;
     c->H.build_id++;
+  });
+}
+
+shci_status shci_set_second_rejection(shci_ctx* c, int enable, double factor) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!(factor >= 0.0)) throw ArgError("second_rejection_factor must be >= 0");
+    c->second_rejection = enable != 0;
+    c->second_rejection_factor = factor;
   });
 }
 
@@ -640,6 +840,20 @@ shci_status shci_get_var_trace(shci_ctx* c, uint64_t* n_dets, uint64_t* nnz, dou
   });
 }
 
+shci_status shci_get_var_trace_states(shci_ctx* c, double* energies, size_t cap, size_t* n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    const auto& t = c->var_trace;
+    const size_t ns = c->n_states;
+    if (n) *n = t.size();
+    if (!energies) return;
+    for (size_t i = 0; i < t.size() && (i + 1) * ns <= cap; i++)
+      for (size_t k = 0; k < ns; k++)
+        energies[i * ns + k] =
+            k < t[i].energies.size() ? t[i].energies[k] : (k == 0 ? t[i].energy : 0.0);
+  });
+}
+
 shci_status shci_pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches,
                          double* correction, double* uncert, size_t* n_pt_dets) {
   if (!c) return SHCI_ERR_ARG;
@@ -691,7 +905,21 @@ shci_status shci_rdm1(shci_ctx* c, double* out) {
   return guard(c, [&]() {
     need_integrals(c);
     need_dets(c);
-    rdm1(c, out);
+    if (c->n_states == 1) {
+      rdm1(c, out);
+      return;
+    }
+    // rdm.cc:222-231: the sum over the states of c_i c_j, formed state by state
+    const size_t nn = static_cast<size_t>(c->I.n) * c->I.n;
+    std::vector<double> acc(nn, 0.0), t(nn);
+    sync_dets(c);
+    for (unsigned k = 0; k < c->n_states; k++) {
+      if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
+      rdm1(c, t.data());
+      if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
+      for (size_t i = 0; i < nn; i++) acc[i] += t[i];
+    }
+    std::memcpy(out, acc.data(), nn * 8);
   });
 }
 
@@ -700,7 +928,69 @@ shci_status shci_rdm2(shci_ctx* c, double* out_half) {
   return guard(c, [&]() {
     need_integrals(c);
     need_dets(c);
-    rdm2(c, out_half);
+    if (c->n_states == 1) {
+      rdm2(c, out_half);
+      return;
+    }
+    const size_t nn = static_cast<size_t>(c->I.n) * c->I.n, m = nn * (nn + 1) / 2;
+    std::vector<double> acc(m, 0.0), t(m);
+    sync_dets(c);
+    for (unsigned k = 0; k < c->n_states; k++) {  // rdm.cc:648-657, state by state
+      if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
+      rdm2(c, t.data());
+      if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
+      for (size_t i = 0; i < m; i++) acc[i] += t[i];
+    }
+    std::memcpy(out_half, acc.data(), m * 8);
+  });
+}
+
+shci_status shci_generalized_fock(shci_ctx* c, double* F) {
+  if (!c || !F) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    sync_dets(c);
+    if (!c->H.valid || c->H.n != c->up.size()) build_hamiltonian(c, SHCI_PREC_FP64);
+    generalized_fock(c, F);
+  });
+}
+
+shci_status shci_orbital_parameters(shci_ctx* c, uint32_t* p, uint32_t* q, size_t cap,
+                                    size_t* n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    const auto& sym = c->I.orb_sym;
+    size_t k = 0;
+    for (unsigned i = 0; i < c->I.n; i++)
+      for (unsigned j = i + 1; j < c->I.n; j++)
+        if (sym[i] == sym[j]) {
+          if (k < cap && p && q) {
+            p[k] = i;
+            q[k] = j;
+          }
+          k++;
+        }
+    if (n) *n = k;
+  });
+}
+
+shci_status shci_orbital_gradient(shci_ctx* c, const uint32_t* p, const uint32_t* q,
+                                  size_t n_param, double* grad) {
+  if (!c || (n_param && (!p || !q || !grad))) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    const size_t n = c->I.n;
+    for (size_t k = 0; k < n_param; k++)
+      if (p[k] >= n || q[k] >= n) throw ArgError("orbital index out of range");
+    std::vector<double> F(n * n);
+    sync_dets(c);
+    if (!c->H.valid || c->H.n != c->up.size()) build_hamiltonian(c, SHCI_PREC_FP64);
+    generalized_fock(c, F.data());
+    for (size_t k = 0; k < n_param; k++)  // optimization.cc:571-575
+      grad[k] = 2 * (F[p[k] * n + q[k]] - F[q[k] * n + p[k]]);
   });
 }
 

@@ -138,8 +138,13 @@ struct DevQueues {
   bool built = false;
 };
 
+// Largest n_states of a several-state run (the subspace holds 5 vectors per state).
+constexpr unsigned kMaxStates = 8;
+
 struct Davidson {
   DevBuf<double> v[5], Hv[5], w, Hw;
+  // several states (davidson_states): 5 * n_states stored vectors, a Ritz vector per state
+  DevBuf<double> sv[5 * kMaxStates], sHv[5 * kMaxStates], sw[kMaxStates], sHw[kMaxStates];
   DevBuf<double> scal;     // device scalars
   DevBuf<double> partial;  // dot partial sums
   DevBuf<double> rt;       // residual-store row sums of the FP64 energy correction
@@ -174,6 +179,11 @@ struct shci_ctx {
   shci::DevBuf<uint64_t> d_up, d_dn;
   shci::DevBuf<double> d_coef;
   bool dets_dirty = true;  // device copy out of date
+  // n_states > 1 (config "n_states"): d_coef is state 0, d_xcoef[s - 1] state s; energies of
+  // every state from the last variational run (FP64-corrected in mixed mode)
+  unsigned n_states = 1;
+  shci::DevBuf<double> d_xcoef[shci::kMaxStates - 1];
+  std::vector<double> state_energy;
 
   // sorted membership keys of the current det list (for selection / PT2)
   shci::DevBuf<uint64_t> set_up, set_dn;
@@ -181,6 +191,13 @@ struct shci_ctx {
   uint64_t set_hash_mask = 0;
 
   std::vector<double> eps_tried;
+  // second rejection of the selection (solver.h:426-428: config "second_rejection",
+  // "second_rejection_factor"; off and 0.2 by default)
+  bool second_rejection = false;
+  double second_rejection_factor = 0.2;
+  // time-reversal symmetry (config "time_sym"): the det list holds up <= dn, an open det
+  // stands for (|up,dn> + |dn,up>) / sqrt(2); the Hamiltonian is the packed one
+  bool time_sym = false;
 
   shci::DetIndex idx;
   shci::JoinIndex join;

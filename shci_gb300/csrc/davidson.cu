@@ -1,11 +1,14 @@
-// Davidson eigensolver on the device (K5), one state.
+// Davidson eigensolver on the device (K5).
 //
-// Follows Davidson::diagonalize (src/solver/davidson.cc:8-196) with n_states = 1: at most
-// five stored vectors, a restart that collapses onto the current Ritz vector, the diagonal
-// preconditioner with the 1e-8 cut, Gram-Schmidt, the <= 5x5 subspace eigenproblem (solved
-// on the host in FP64 by cyclic Jacobi) with the Ritz vector's first component made
-// non-negative, and convergence |lambda - lambda_prev| <= tol.  All vector work is FP64 on
-// the device; dot products reduce in a fixed order so results do not depend on timing.
+// Follows Davidson::diagonalize (src/solver/davidson.cc:8-196).  davidson(): n_states = 1, at
+// most five stored vectors, a restart that collapses onto the current Ritz vector, the
+// diagonal preconditioner with the 1e-8 cut, Gram-Schmidt, the <= 5x5 subspace eigenproblem
+// (solved on the host in FP64 by cyclic Jacobi) with the Ritz vector's first component made
+// non-negative, and convergence |lambda - lambda_prev| <= tol.  davidson_states(): the same
+// for n_states > 1 (5 n_states stored vectors, one preconditioned vector per step for the
+// states in turn, a subspace solve after the last state's vector, convergence state by state).
+// All vector work is FP64 on the device; dot products reduce in a fixed order so results do
+// not depend on timing.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -111,6 +114,26 @@ __global__ void k_combine(double* __restrict__ w, double* __restrict__ hw, Comb 
   }
 }
 
+// w = sum_k e_k v_k, Hw = sum_k e_k Hv_k over up to 5 * kMaxStates vectors
+struct CombN {
+  const double* v[5 * kMaxStates];
+  const double* hv[5 * kMaxStates];
+  double e[5 * kMaxStates];
+  int k;
+};
+__global__ void k_combine_n(double* __restrict__ w, double* __restrict__ hw, CombN cb, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < cb.k; k++) {
+      a += cb.v[k][i] * cb.e[k];
+      b += cb.hv[k][i] * cb.e[k];
+    }
+    w[i] = a;
+    hw[i] = b;
+  }
+}
+
 class Dots {
  public:
   Dots(shci_ctx* c) : c_(c) {
@@ -145,10 +168,10 @@ class Dots {
 
 }  // namespace
 
-// Cyclic Jacobi on the lower triangle of a k x k matrix (k <= 16): eigenvalues ascending,
-// eigenvectors in columns (evecs[r*k + c]).
+// Cyclic Jacobi on the lower triangle of a k x k matrix: eigenvalues ascending, eigenvectors
+// in columns (evecs[r*k + c]).
 void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs) {
-  double a[16 * 16], v[16 * 16];
+  std::vector<double> a(static_cast<size_t>(k) * k), v(static_cast<size_t>(k) * k);
   for (int i = 0; i < k; i++)
     for (int j = 0; j < k; j++) {
       a[i * k + j] = i >= j ? lower[i * ld + j] : lower[j * ld + i];
@@ -185,9 +208,9 @@ void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs
         }
       }
   }
-  int idx[16];
-  std::iota(idx, idx + k, 0);
-  std::sort(idx, idx + k, [&](int x, int y) { return a[x * k + x] < a[y * k + y]; });
+  std::vector<int> idx(k);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a[x * k + x] < a[y * k + y]; });
   for (int c = 0; c < k; c++) {
     evals[c] = a[idx[c] * k + idx[c]];
     for (int r = 0; r < k; r++) evecs[r * k + c] = v[r * k + idx[c]];
@@ -306,6 +329,170 @@ DavidsonOut davidson(shci_ctx* c, double tol) {
   return out;
 }
 
+double* state_coef(shci_ctx* c, unsigned s) {
+  return s == 0 ? c->d_coef.p : c->d_xcoef[s - 1].p;
+}
+
+// davidson.cc:8-196 for n_states = c->n_states > 1.  The subspace matrix starts with only its
+// diagonal set (:62-77); the initial vectors are normalised and orthogonalised in order.
+DavidsonStatesOut davidson_states(shci_ctx* c, double tol) {
+  DavidsonStatesOut out;
+  auto& D = c->dav;
+  D.ritz = false;
+  const size_t n = c->H.n;
+  cudaStream_t s = c->stream;
+  const unsigned g = grid_for(n, 256, 152 * 16);
+  const unsigned req = c->n_states;
+  const unsigned ns = static_cast<unsigned>(std::min<size_t>(n, req));
+  out.evals.assign(req, 0.0);
+  Dots dots(c);
+  if (n == 1) {
+    SHCI_CUDA(cudaMemcpyAsync(&out.evals[0], c->H.diag.p, 8, cudaMemcpyDeviceToHost, s));
+    const double one = 1.0, zero = 0.0;
+    SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, &one, 8, cudaMemcpyHostToDevice, s));
+    for (unsigned k = 1; k < req; k++)
+      SHCI_CUDA(cudaMemcpyAsync(state_coef(c, k), &zero, 8, cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    out.converged = true;
+    return out;
+  }
+  const size_t nis = std::min<size_t>(n, 5);
+  const size_t m = ns * nis;
+  for (size_t k = 0; k < m; k++) {
+    D.sv[k].mt = D.sHv[k].mt = &c->mem;
+    D.sv[k].resize(n, 1.1);
+    D.sHv[k].resize(n, 1.1);
+  }
+  for (unsigned k = 0; k < ns; k++) {
+    D.sw[k].mt = D.sHw[k].mt = &c->mem;
+    D.sw[k].resize(n, 1.1);
+    D.sHw[k].resize(n, 1.1);
+  }
+  double* scal = D.scal.p;
+  auto host_dots = [&](const double* x, const std::vector<const double*>& ys, double* outv) {
+    for (size_t b = 0; b < ys.size(); b += 6) {
+      Ptrs6 p{};
+      const int mm = static_cast<int>(std::min<size_t>(6, ys.size() - b));
+      for (int q = 0; q < mm; q++) p.p[q] = ys[b + q];
+      dots.mdot(x, p, mm, n, scal);
+      SHCI_CUDA(cudaMemcpyAsync(outv + b, scal, mm * 8, cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+    }
+  };
+  // initial vectors (:44-60)
+  for (unsigned k = 0; k < ns; k++) {
+    SHCI_CUDA(cudaMemcpyAsync(D.sv[k].p, state_coef(c, k), n * 8, cudaMemcpyDeviceToDevice, s));
+    double nrm = std::sqrt(dots.dot_host(D.sv[k].p, D.sv[k].p, n));
+    k_scale<<<g, 256, 0, s>>>(D.sv[k].p, nrm, n);
+    SHCI_LAUNCH_CHECK();
+    if (k > 0) {
+      for (unsigned q = 0; q < k; q++) {
+        dots.mdot(D.sv[k].p, {D.sv[q].p}, n, scal);
+        k_axpy_dev<<<g, 256, 0, s>>>(D.sv[k].p, D.sv[q].p, scal, n);
+        SHCI_LAUNCH_CHECK();
+      }
+      nrm = std::sqrt(dots.dot_host(D.sv[k].p, D.sv[k].p, n));
+      k_scale<<<g, 256, 0, s>>>(D.sv[k].p, nrm, n);
+      SHCI_LAUNCH_CHECK();
+    }
+  }
+  std::vector<double> hk(m * m, 0.0), lam(ns), lam_prev(ns);
+  for (unsigned k = 0; k < ns; k++) {
+    spmv(c, D.sv[k].p, D.sHv[k].p, false);
+    out.n_matvec++;
+    lam[k] = dots.dot_host(D.sv[k].p, D.sHv[k].p, n);
+    hk[k * m + k] = lam[k];
+    SHCI_CUDA(cudaMemcpyAsync(D.sw[k].p, D.sv[k].p, n * 8, cudaMemcpyDeviceToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(D.sHw[k].p, D.sHv[k].p, n * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  lam_prev = lam;
+  bool converged = false;
+  size_t n_conv = 0, pre = 0;
+  for (size_t it = ns; it < m * 2; it++) {
+    const size_t ic = it % m;
+    if (it >= m) {  // restart onto the Ritz vectors (:86-103)
+      if (ic < ns - 1) continue;
+      if (ic == ns - 1) {
+        for (unsigned k = 0; k < ns; k++) {
+          SHCI_CUDA(cudaMemcpyAsync(D.sv[k].p, D.sw[k].p, n * 8, cudaMemcpyDeviceToDevice, s));
+          SHCI_CUDA(cudaMemcpyAsync(D.sHv[k].p, D.sHw[k].p, n * 8, cudaMemcpyDeviceToDevice, s));
+        }
+        for (unsigned k = 0; k < ns; k++) {
+          lam[k] = dots.dot_host(D.sv[k].p, D.sHv[k].p, n);
+          hk[k * m + k] = lam[k];
+          for (unsigned q = k + 1; q < ns; q++) {
+            const double e = dots.dot_host(D.sv[k].p, D.sHv[q].p, n);
+            hk[k * m + q] = e;
+            hk[q * m + k] = e;
+          }
+        }
+        continue;
+      }
+    }
+    // preconditioned residual of state `pre` (:133-143)
+    k_precond<<<g, 256, 0, s>>>(D.sv[ic].p, D.sHw[pre].p, D.sw[pre].p, c->H.diag.p, lam[pre], n);
+    SHCI_LAUNCH_CHECK();
+    for (size_t i = 0; i < ic; i++) {  // (:145-152)
+      dots.mdot(D.sv[ic].p, {D.sv[i].p}, n, scal);
+      k_axpy_dev<<<g, 256, 0, s>>>(D.sv[ic].p, D.sv[i].p, scal, n);
+      SHCI_LAUNCH_CHECK();
+    }
+    const double nrm = std::sqrt(dots.dot_host(D.sv[ic].p, D.sv[ic].p, n));
+    if (nrm < 1e-12) {
+      converged = true;
+      break;
+    }
+    k_scale<<<g, 256, 0, s>>>(D.sv[ic].p, nrm, n);
+    SHCI_LAUNCH_CHECK();
+    spmv(c, D.sv[ic].p, D.sHv[ic].p, false);
+    out.n_matvec++;
+    {  // row ic of the subspace matrix (:163-167)
+      std::vector<const double*> ys(ic + 1);
+      for (size_t i = 0; i <= ic; i++) ys[i] = D.sv[i].p;
+      std::vector<double> row(ic + 1);
+      host_dots(D.sHv[ic].p, ys, row.data());
+      for (size_t i = 0; i <= ic; i++) hk[ic * m + i] = row[i];
+    }
+    c->launches += 4 + 2 * ic;
+    if (pre + 1 == ns) {  // subspace solve (:169-172) and Ritz vectors (:173-194)
+      const int k = static_cast<int>(ic + 1);
+      std::vector<double> ev(k), evec(static_cast<size_t>(k) * k);
+      jacobi_eig(k, hk.data(), static_cast<int>(m), ev.data(), evec.data());
+      for (unsigned st = 0; st < ns; st++) {
+        lam[st] = ev[st];
+        const double factor = evec[st] < 0 ? -1.0 : 1.0;
+        CombN cb{};
+        cb.k = k;
+        for (int i = 0; i < k; i++) {
+          cb.v[i] = D.sv[i].p;
+          cb.hv[i] = D.sHv[i].p;
+          cb.e[i] = evec[i * k + st] * factor;
+        }
+        k_combine_n<<<g, 256, 0, s>>>(D.sw[st].p, D.sHw[st].p, cb, n);
+        SHCI_LAUNCH_CHECK();
+        c->launches += 1;
+      }
+      for (unsigned st = static_cast<unsigned>(n_conv); st < ns; st++) {  // (:180-186)
+        if (std::fabs(lam[st] - lam_prev[st]) > tol) break;
+        n_conv++;
+      }
+      if (n_conv == ns) converged = true;
+      if (!converged) lam_prev = lam;
+      if (converged) break;
+    }
+    pre++;
+    if (pre >= ns) pre = n_conv;
+  }
+  for (unsigned k = 0; k < ns; k++) {
+    SHCI_CUDA(cudaMemcpyAsync(state_coef(c, k), D.sw[k].p, n * 8, cudaMemcpyDeviceToDevice, s));
+    out.evals[k] = lam[k];
+  }
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  out.converged = converged;
+  c->prof.flush();
+  return out;
+}
+
 // Rayleigh quotient of d_coef with value + residual.  When d_coef is still the Ritz vector w
 // of the last Davidson call on this (mixed) Hamiltonian, w^T H w = w^T Hw + w^T R w with Hw =
 // H32 w kept by Davidson (FP32 values, FP64 diagonal), so only the residual store R is read
@@ -335,12 +522,19 @@ double rayleigh_fp64(shci_ctx* c) {
       return num / den;
     }
   }
+  return rayleigh_fp64_of(c, c->d_coef.p);
+}
+
+double rayleigh_fp64_of(shci_ctx* c, const double* x) {
+  const size_t n = c->H.n;
+  auto& D = c->dav;
+  Dots dots(c);
   D.ritz = false;  // Hw is overwritten below
   D.Hw.mt = &c->mem;
   D.Hw.resize(n, 1.1);
-  spmv(c, c->d_coef.p, D.Hw.p, true);
-  const double num = dots.dot_host(c->d_coef.p, D.Hw.p, n);
-  const double den = dots.dot_host(c->d_coef.p, c->d_coef.p, n);
+  spmv(c, x, D.Hw.p, true);
+  const double num = dots.dot_host(x, D.Hw.p, n);
+  const double den = dots.dot_host(x, x, n);
   return num / den;
 }
 

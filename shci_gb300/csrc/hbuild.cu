@@ -436,6 +436,7 @@ static size_t store_room(shci_ctx* c) {
 //   scan            - group index + scan traversal, count and fill (packed rows).
 // SHCI_HBUILD=scan forces the scan path, SHCI_HBUILD=join2 the two-pass join.
 size_t build_hamiltonian(shci_ctx* c, int precision) {
+  if (c->time_sym) return build_time_sym(c, precision);
   auto& H = c->H;
   auto& ix = c->idx;
   const size_t n = c->up.size();

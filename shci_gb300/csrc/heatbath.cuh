@@ -38,7 +38,14 @@ struct SelParams {
   int n_orbs, n_up, n_elecs, n_pairs;
   int var_sd;
   uint32_t pass, n_src_total;  // sources are i = pass + 5 k, i < n_src_total
+  // second rejection (chem_system.cc:300-308, 318-324, 364-370): off unless rej_on
+  int rej_on;
+  double rej_factor;  // second_rejection_factor
+  double e_hf_1b;     // sum of h_pp over the HF det's electrons (chem_system.cc:812-823)
+  int time_sym;       // time-reversal symmetry: list holds up <= dn, open dets stand for pairs
 };
+
+constexpr double kSqrt2 = 1.4142135623730951;  // Util::SQRT2 (src/util.h:58)
 
 __device__ __forceinline__ int nth_bit(uint64_t x, int k) {
   const unsigned lo = static_cast<unsigned>(x), hi = static_cast<unsigned>(x >> 32);
@@ -158,6 +165,7 @@ __device__ __forceinline__ bool in_set(const SelParams& P, uint64_t u, uint64_t 
 __device__ __forceinline__ double src_eps_min(const SelParams& P, uint32_t i) {
   double e = P.eps_var / fabs(P.coef[i]);
   if (i == 0 && P.var_sd) e = 0.0;
+  if (P.time_sym && P.up[i] != P.dn[i]) e *= kSqrt2;  // solver.h:447
   return e;
 }
 

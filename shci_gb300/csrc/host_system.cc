@@ -102,14 +102,69 @@ std::vector<unsigned> convert_syms(const std::vector<int>& raw) {
 
 }  // namespace
 
-unsigned point_group_order(const std::string& pg) {
+unsigned point_group_order(const std::string& pg, bool* linear) {
   std::string s;
   for (char c : pg) s.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(c))));
+  if (linear) *linear = false;
   if (s == "c1") return 1;
   if (s == "c2" || s == "cs" || s == "ci") return 2;
   if (s == "c2v" || s == "c2h" || s == "d2") return 4;
   if (s == "d2h") return 8;
-  throw std::runtime_error("unsupported point group '" + pg + "' (C1..D2h are supported)");
+  if (s == "dooh" || s == "dih" || s == "coov" || s == "civ") {
+    if (linear) *linear = true;
+    return 128;
+  }
+  throw std::runtime_error("unsupported point group '" + pg +
+                           "' (C1, C2, Cs, Ci, C2v, C2h, D2, D2h, Dooh/Dih, Coov/Civ)");
+}
+
+// Labels 1, 2 are Lz = 0 (g, u); from 3 on, four labels per |Lz|: +g, +u, -g, -u.
+int linear_lz(int label, int* gu) {
+  if (label <= 2) {
+    *gu = label - 1;
+    return 0;
+  }
+  const int mag = 1 + ((label - 3) >> 2);
+  *gu = (label + 1) & 1;
+  return (((label - 1) >> 1) & 1) ? mag : -mag;
+}
+
+namespace {
+
+int linear_label(int lz, int gu) {
+  if (lz == 0) return gu + 1;
+  return (std::abs(lz) << 2) - 1 + gu + (lz < 0 ? 2 : 0);
+}
+
+// The irrep of the conjugate (Lz -> -Lz), DoohUtil::get_inverse (dooh_util.cc:35-45).
+unsigned linear_inverse(unsigned label) {
+  int gu;
+  const int lz = linear_lz(static_cast<int>(label), &gu);
+  return lz > 0 ? label + 2 : lz < 0 ? label - 2 : label;
+}
+
+}  // namespace
+
+unsigned irrep_product(bool linear, unsigned a, unsigned b) {
+  if (!linear) return ((a - 1) ^ (b - 1)) + 1;  // C1..D2h: XOR group on (irrep - 1)
+  int ga, gb;
+  const int la = linear_lz(static_cast<int>(a), &ga), lb = linear_lz(static_cast<int>(b), &gb);
+  return static_cast<unsigned>(linear_label(la + lb, (ga + gb) & 1));
+}
+
+void screen_linear(HostIntegrals& I) {
+  if (!I.linear) return;
+  const unsigned n = I.n;
+  std::vector<int> lz(n);
+  for (unsigned o = 0; o < n; o++) {
+    int gu;
+    lz[o] = linear_lz(static_cast<int>(I.orb_sym[o]), &gu);
+  }
+  for (unsigned p = 0; p < n; p++)
+    for (unsigned q = 0; q < n; q++)
+      for (unsigned r = 0; r < n; r++)
+        for (unsigned s = 0; s < n; s++)
+          if (lz[p] + lz[r] != lz[q] + lz[s]) I.g2[((size_t)(p * n + q) * n + r) * n + s] = 0.0;
 }
 
 void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsigned n_dn,
@@ -117,7 +172,7 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
                   const unsigned* occs_dn) {
   std::ifstream f(path);
   if (!f.good()) throw std::runtime_error("cannot open FCIDUMP '" + path + "'");
-  I.n_syms = point_group_order(point_group);
+  I.n_syms = point_group_order(point_group, &I.linear);
   unsigned n = 0;
   std::vector<int> raw_syms;
   {
@@ -255,6 +310,10 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
         for (unsigned s = 0; s < n; s++)
           I.g2[((size_t)(p * n + q) * n + r) * n + s] = R.g(p, q, r, s);
     }
+  // The orbital energies above read the tables unscreened: the reference sets the integrals'
+  // point group only after Integrals::load (chem_system.cc:33-34), and (ii|oo), (io|oi)
+  // conserve Lz anyway.
+  screen_linear(I);
 }
 
 double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn) {
@@ -292,8 +351,6 @@ double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn) {
 }
 
 namespace {
-
-unsigned sym_product(unsigned a, unsigned b) { return ((a - 1) ^ (b - 1)) + 1; }
 
 // |two-body double| of the queue element (p,q) -> (r,s) (chem_system.cc:261-287, 579-609).
 double queue_elem(const HostIntegrals& I, unsigned p, unsigned q, unsigned r, unsigned s) {
@@ -351,6 +408,9 @@ void build_queues(const HostIntegrals& I, HostQueues& Q) {
   };
   const size_t n_pairs = combine2(n, 2 * n);
   std::vector<std::vector<E>> dq(n_pairs);
+  // irrep that s must have given p, q, r: the product of p, q and r's conjugate (linear groups
+  // conjugate r, chem_system.cc:133-135; the other groups are their own conjugates)
+  auto sym_r = [&](unsigned r) { return I.linear ? linear_inverse(I.orb_sym[r]) : I.orb_sym[r]; };
   auto sort_desc = [](std::vector<E>& v) {
     std::sort(v.begin(), v.end(), [](const E& a, const E& b) { return a.H > b.H; });
   };
@@ -358,9 +418,9 @@ void build_queues(const HostIntegrals& I, HostQueues& Q) {
   parallel_for(n, [&](unsigned p) {
     for (unsigned q = p + 1; q < n; q++) {
       auto& v = dq[combine2(p, q)];
-      const unsigned sq = sym_product(I.orb_sym[p], I.orb_sym[q]);
+      const unsigned sq = irrep_product(I.linear, I.orb_sym[p], I.orb_sym[q]);
       for (unsigned r = 0; r < n; r++) {
-        const unsigned sr = sym_product(sq, I.orb_sym[r]);
+        const unsigned sr = irrep_product(I.linear, sq, sym_r(r));
         if (sr >= sym_orbs.size()) continue;
         for (unsigned s : sym_orbs[sr]) {
           if (s < r) continue;
@@ -375,9 +435,9 @@ void build_queues(const HostIntegrals& I, HostQueues& Q) {
   parallel_for(n, [&](unsigned p) {
     for (unsigned q = n + p; q < 2 * n; q++) {
       auto& v = dq[combine2(p, q)];
-      const unsigned sq = sym_product(I.orb_sym[p], I.orb_sym[q - n]);
+      const unsigned sq = irrep_product(I.linear, I.orb_sym[p], I.orb_sym[q - n]);
       for (unsigned r = 0; r < n; r++) {
-        const unsigned sr = sym_product(sq, I.orb_sym[r]);
+        const unsigned sr = irrep_product(I.linear, sq, sym_r(r));
         if (sr >= sym_orbs.size()) continue;
         for (unsigned s : sym_orbs[sr]) {
           const double H = queue_elem(I, p, q, r, s + n);

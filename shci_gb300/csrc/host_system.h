@@ -18,6 +18,9 @@ struct HostIntegrals {
   std::vector<double> g2;           // [n^4]
   uint64_t hf_up = 0, hf_dn = 0;
   unsigned n_syms = 1;
+  // Linear molecules (D-infinity-h / C-infinity-v): irreps are (Lz, g/u) labels in the
+  // reference's "Adam's notation" and products add Lz (src/chem/dooh_util.cc).
+  bool linear = false;
 
   double h(unsigned p, unsigned q) const { return h1[p * n + q]; }
   double g(unsigned p, unsigned q, unsigned r, unsigned s) const {
@@ -31,7 +34,21 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
                   const std::string& point_group, int reorder, const unsigned* occs_up,
                   const unsigned* occs_dn);
 
-unsigned point_group_order(const std::string& pg);
+// Number of irreps of a point group name as ProductTable::get_n_syms counts them
+// (src/chem/product_table.cc:37-47; 128 for the linear groups); *linear tells whether the name
+// is one of the linear groups ("Dooh", "Dih", "Coov", "Civ": ChemSystem::get_point_group,
+// src/chem/chem_system.cc:198-221, maps all four to D-infinity-h).
+unsigned point_group_order(const std::string& pg, bool* linear = nullptr);
+
+// Lz and g/u of a linear-group irrep label (DoohUtil::get_lz, src/chem/dooh_util.cc:5-15).
+int linear_lz(int label, int* gu);
+// Product of two irreps (ProductTable::get_product, product_table.cc:31-36 and
+// DoohUtil::get_product, dooh_util.cc:27-33).
+unsigned irrep_product(bool linear, unsigned a, unsigned b);
+// Zeroes every (pq|rs) whose orbitals do not conserve Lz, lz_p + lz_r != lz_q + lz_s: the
+// test Integrals::get_2b applies to every two-body lookup once the system's point group is
+// linear (src/chem/integrals.cc:394-406).  No-op unless I.linear.
+void screen_linear(HostIntegrals& I);
 
 // Heat-bath queues in CSR form (src/chem/chem_system.cc:74-196).
 struct HostQueues {

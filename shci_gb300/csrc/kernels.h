@@ -36,6 +36,8 @@ void hamiltonian_elems_noalloc(shci_ctx* c, const uint64_t* ui, const uint64_t* 
 // scan; the SHCI_HBUILD environment variable set to "scan" forces the scan)
 void build_index(shci_ctx* c);
 size_t build_hamiltonian(shci_ctx* c, int precision);
+// timesym.cu: the packed time-reversal-symmetric Hamiltonian (c->time_sym)
+size_t build_time_sym(shci_ctx* c, int precision);
 
 // hjoin.cu: two-hole core join.  join_prepare returns false (nothing held) when the join
 // cannot be used for the current dets; join_rows runs one pass (mode as the row kernels;
@@ -72,7 +74,19 @@ struct DavidsonOut {
 };
 // Runs on c->H with the initial vector c->d_coef (length H.n); Ritz vector left in d_coef.
 DavidsonOut davidson(shci_ctx* c, double tol);
+// Several states (c->n_states > 1): initial vectors d_coef and d_xcoef[0 .. n_states - 2],
+// Ritz vectors left there; eigenvalues per state in evals.
+struct DavidsonStatesOut {
+  std::vector<double> evals;
+  bool converged = false;
+  int n_matvec = 0;
+};
+DavidsonStatesOut davidson_states(shci_ctx* c, double tol);
 double rayleigh_fp64(shci_ctx* c);
+// FP64 Rayleigh quotient x^T H x / x^T x with value + residual (any device vector x).
+double rayleigh_fp64_of(shci_ctx* c, const double* x);
+// Pointer to the device coefficients of state s (0 = d_coef).
+double* state_coef(shci_ctx* c, unsigned s);
 void jacobi_eig(int k, const double* lower, int ld, double* evals, double* evecs);
 
 // select.cu
@@ -113,5 +127,10 @@ void find_connected(shci_ctx* c, const uint64_t* up, const uint64_t* dn, const d
 // rdm.cu
 void rdm1(shci_ctx* c, double* out);       // host [n*n]
 void rdm2(shci_ctx* c, double* out_half);  // host [n^2 (n^2+1) / 2]
+void rdm1_dev(shci_ctx* c, double* res_dev);    // device [n*n] (state 0 coefficients)
+void rdm2_dev(shci_ctx* c, double* half_dev);   // device [n^2 (n^2+1) / 2]
+
+// orbopt.cu: generalized Fock matrix F[n*n] (host) from the RDMs of every state
+void generalized_fock(shci_ctx* c, double* F);
 
 }  // namespace shci

@@ -301,6 +301,16 @@ void sorted_set_with_perm(shci_ctx* c, DevBuf<uint64_t>& su, DevBuf<uint64_t>& s
 }  // namespace
 
 void rdm1(shci_ctx* c, double* out) {
+  const int n = c->I.n;
+  DevBuf<double> res;
+  res.mt = &c->mem;
+  res.resize((size_t)n * n);
+  rdm1_dev(c, res.p);
+  SHCI_CUDA(cudaMemcpyAsync(out, res.p, (size_t)n * n * 8, cudaMemcpyDeviceToHost, c->stream));
+  SHCI_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void rdm1_dev(shci_ctx* c, double* res_dev) {
   sync_dets(c);
   const size_t n_dets = c->up.size();
   const int n = c->I.n;
@@ -309,41 +319,46 @@ void rdm1(shci_ctx* c, double* out) {
   DevBuf<uint64_t> su, sd;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned> sym;
-  DevBuf<double> partial, res;
+  DevBuf<double> partial;
   su.mt = sd.mt = &c->mem;
   perm.mt = sym.mt = &c->mem;
-  partial.mt = res.mt = &c->mem;
+  partial.mt = &c->mem;
   sorted_set_with_perm(c, su, sd, perm);
   sym.resize(n);
   SHCI_CUDA(cudaMemcpyAsync(sym.p, c->I.orb_sym.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice, s));
   partial.resize((size_t)kRdmBlocks * n * n);
-  res.resize((size_t)n * n);
   {
     ProfScope ps(c->prof, s, "rdm1");
     k_rdm1<<<kRdmBlocks, 256, (size_t)n * n * sizeof(double), s>>>(
         c->d_up.p, c->d_dn.p, c->d_coef.p, (uint32_t)n_dets, sym.p, n, su.p, sd.p, perm.p,
         partial.p);
     SHCI_LAUNCH_CHECK();
-    k_rdm1_sum<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(partial.p, kRdmBlocks, n * n, res.p);
+    k_rdm1_sum<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(partial.p, kRdmBlocks, n * n, res_dev);
     SHCI_LAUNCH_CHECK();
   }
-  SHCI_CUDA(cudaMemcpyAsync(out, res.p, (size_t)n * n * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->prof.flush();
   c->launches += 2;
 }
 
 void rdm2(shci_ctx* c, double* out_half) {
+  const size_t nn = (size_t)c->I.n * c->I.n, size = nn * (nn + 1) / 2;
+  DevBuf<double> half;
+  half.mt = &c->mem;
+  half.resize(size);
+  rdm2_dev(c, half.p);
+  SHCI_CUDA(cudaMemcpyAsync(out_half, half.p, size * 8, cudaMemcpyDeviceToHost, c->stream));
+  SHCI_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void rdm2_dev(shci_ctx* c, double* half_dev) {
   auto& H = c->H;
   if (!H.valid || H.n != c->up.size()) throw ArgError("the 2-RDM needs the current Hamiltonian");
   sync_dets(c);
   const int n = c->I.n;
   const size_t nn = (size_t)n * n, size = nn * (nn + 1) / 2;
   cudaStream_t s = c->stream;
-  DevBuf<double> half;
-  half.mt = &c->mem;
-  half.resize(size);
-  SHCI_CUDA(cudaMemsetAsync(half.p, 0, size * 8, s));
+  SHCI_CUDA(cudaMemsetAsync(half_dev, 0, size * 8, s));
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   {
@@ -354,12 +369,11 @@ void rdm2(shci_ctx* c, double* out_half) {
       // diagonal terms once, with the current segment (which covers every row)
       k_rdm2<<<static_cast<unsigned>(sms) * 8u, 256, 0, s>>>(
           c->d_up.p, c->d_dn.p, c->d_coef.p, (uint32_t)g.n, g.row_ptr, g.row_cnt, g.col, n,
-          k + 1 == segs.size(), half.p);
+          k + 1 == segs.size(), half_dev);
       SHCI_LAUNCH_CHECK();
       c->launches += 1;
     }
   }
-  SHCI_CUDA(cudaMemcpyAsync(out_half, half.p, size * 8, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->prof.flush();
   c->launches += 1;

@@ -17,6 +17,10 @@
 //                 variational set and (singles) the |H_ai| >= eps_min rule,
 //   compaction + two-stage radix sort + unique -> this pass's new dets in ascending Det order.
 // New dets of a pass join the variational set before the next pass, as in the reference.
+// With second rejection (off by default) the emission also drops window entries whose
+// |H|^2 / (one-body energy difference to HF) is below factor * eps_min^2 and records, per
+// source, the largest |H| it dropped; eps_tried_prev then becomes 1.000000001 * max(that,
+// eps_min) (solver.h:461-465, chem_system.cc:300-308, 318-324, 364-370, 401).
 #include <algorithm>
 #include <cmath>
 
@@ -59,19 +63,69 @@ __global__ void __launch_bounds__(kSelWarps * 32)
   }
 }
 
+// rej_max (second rejection only): the largest rejected |H| of each source, else null.  As
+// find_connected_dets returns it: max(largest rejected, eps_min), except that a det whose
+// eps_min is above every double's |H| returns eps_min before the doubles (chem_system.cc:
+// 339-340), dropping what its singles rejected.
 __global__ void k_sel_mark(SelParams P, uint32_t k_begin, uint32_t k_end,
-                           const double* eps_min_in) {
+                           const double* eps_min_in, const double* rej_max) {
   for (uint32_t k = k_begin + blockIdx.x * blockDim.x + threadIdx.x; k < k_end;
        k += gridDim.x * blockDim.x) {
     const uint32_t i = P.pass + 5u * k;
     const double eps_min = eps_min_in[k - k_begin];
-    if (eps_min < P.eps_tried[i]) P.eps_tried[i] = 1.000000001 * eps_min;
+    if (eps_min < P.eps_tried[i]) {
+      const bool rej = rej_max && !(eps_min > P.max_hci);
+      P.eps_tried[i] = 1.000000001 * (rej ? fmax(rej_max[k - k_begin], eps_min) : eps_min);
+    }
   }
+}
+
+// One-body energy difference of det (up, dn) from HF, accumulated in the reference's order
+// (chem_system.cc:300-308): -e_hf_1b, then h_pp over the alpha electrons, then the beta ones.
+__device__ __forceinline__ double diff_from_hf(const SelParams& P, uint64_t up, uint64_t dn) {
+  const int n = P.n_orbs;
+  double d = -P.e_hf_1b;
+  for (uint64_t m = up; m; m &= m - 1) d += P.I.h1[ctz64(m) * (n + 1)];
+  for (uint64_t m = dn; m; m &= m - 1) d += P.I.h1[ctz64(m) * (n + 1)];
+  return d;
+}
+
+// Second-rejection test of entry e of slot `slot` (chem_system.cc:318-324, 364-370): true
+// when the entry is dropped; *h is its |H| (the queue's S or H).
+__device__ __forceinline__ bool second_rejected(const SelParams& P, uint64_t up, uint64_t dn,
+                                                int slot, uint32_t e, double diff,
+                                                double eps_min, double* h) {
+  const int n = P.n_orbs;
+  const double* d1 = P.I.h1;
+  double den;
+  if (slot < P.n_elecs) {
+    const int p = slot < P.n_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
+    const int r = static_cast<int>(P.s_r[e]);
+    *h = P.s_S[e];
+    den = diff - d1[p * (n + 1)] + d1[r * (n + 1)];
+  } else {
+    const uint32_t pr = P.pair_tab[slot - P.n_elecs];
+    const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
+    const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
+    const uint32_t rs = P.d_rs[e];
+    int r = static_cast<int>(rs & 0xffff) % n, s = static_cast<int>(rs >> 16) % n;
+    if (p < n && q >= n && p > q - n) {  // the reference swaps r and s here (:357-361)
+      const int t = r;
+      r = s;
+      s = t;
+    }
+    *h = P.d_H[e];
+    den = diff - d1[(p % n) * (n + 1)] - d1[(q % n) * (n + 1)] + d1[r * (n + 1)] +
+          d1[s * (n + 1)];
+  }
+  const double hv = *h;
+  return den > 0. && __ddiv_rn(__dmul_rn(hv, hv), den) <
+                         __dmul_rn(__dmul_rn(P.rej_factor, eps_min), eps_min);
 }
 
 __global__ void __launch_bounds__(kSelWarps * 32)
     k_sel_emit(SelParams P, uint32_t k_begin, uint32_t k_end, const uint64_t* off,
-               const double* eps_min_in, uint64_t* out_up, uint64_t* out_dn) {
+               const double* eps_min_in, uint64_t* out_up, uint64_t* out_dn, double* rej_max) {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t wpg = gridDim.x * kSelWarps;
   const int n = P.n_orbs;
@@ -83,6 +137,8 @@ __global__ void __launch_bounds__(kSelWarps * 32)
     const uint64_t up = P.up[i], dn = P.dn[i];
     uint64_t base = off[k - k_begin];
     const int n_slots = P.n_elecs + P.n_pairs;
+    const double diff = P.rej_on ? diff_from_hf(P, up, dn) : 0.0;
+    double rmax = 0.0;  // largest rejected |H| seen by this lane
     for (int s0 = 0; s0 < n_slots; s0 += 32) {
       const int slot = s0 + lane;
       uint32_t lo = 0, c = 0;
@@ -110,16 +166,31 @@ __global__ void __launch_bounds__(kSelWarps * 32)
         const uint32_t e = o_lo + (t - (o_inc - o_c));
         uint64_t cu, cd;
         bool single;
+        double hr;
+        if (P.rej_on && second_rejected(P, up, dn, o_slot, e, diff, eps_min, &hr)) {
+          rmax = fmax(rmax, hr);
+          out_up[base + t] = kInvalid;
+          out_dn[base + t] = kInvalid;
+          continue;
+        }
         bool ok = make_candidate(P, up, dn, o_slot, e, &cu, &cd, &single);
-        if (ok && in_set(P, cu, cd)) ok = false;
+        // time_sym: the stored form has up <= dn (solver.h:452-454)
+        const bool flip = P.time_sym && cu > cd;
+        const uint64_t ru = flip ? cd : cu, rd = flip ? cu : cd;
+        if (ok && in_set(P, ru, rd)) ok = false;
         if (ok && single) {  // small single excitations are filtered (solver.h:456-459)
           const double h = h_offdiag(P.I, up, dn, cu, cd);
           if (fabs(h) < eps_min) ok = false;
         }
-        out_up[base + t] = ok ? cu : kInvalid;
-        out_dn[base + t] = ok ? cd : kInvalid;
+        out_up[base + t] = ok ? ru : kInvalid;
+        out_dn[base + t] = ok ? rd : kInvalid;
       }
       base += total;
+    }
+    if (P.rej_on) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(kFull, rmax, o));
+      if (lane == 0) rej_max[k - k_begin] = rmax;
     }
   }
 }
@@ -151,6 +222,23 @@ __global__ void k_fill_coef(double* c, size_t from, size_t to, double v) {
   for (size_t i = from + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < to;
        i += (size_t)gridDim.x * blockDim.x)
     c[i] = v;
+}
+
+// Several states: the coefficient of largest magnitude over the states, the first one on
+// ties (solver.h:440-444).
+struct StatePtrs {
+  const double* p[kMaxStates - 1];
+};
+__global__ void k_max_coef(const double* c0, StatePtrs xs, int n_extra, size_t n, double* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double m = c0[i];
+    for (int k = 0; k < n_extra; k++) {
+      const double v = xs.p[k][i];
+      if (fabs(v) > fabs(m)) m = v;
+    }
+    out[i] = m;
+  }
 }
 
 }  // namespace
@@ -351,21 +439,49 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
   P.n_pairs = static_cast<int>(pairs.size());
   P.var_sd = var_sd ? 1 : 0;
   P.n_src_total = static_cast<uint32_t>(n_dets);
+  P.rej_on = c->second_rejection ? 1 : 0;
+  P.rej_factor = c->second_rejection_factor;
+  P.time_sym = c->time_sym ? 1 : 0;
+  P.e_hf_1b = 0.0;
+  if (c->second_rejection) {
+    // ChemSystem::get_e_hf_1b (chem_system.cc:812-823) on dets[0]: alpha, then beta (doubled
+    // alpha under time_sym)
+    for (uint64_t m = c->up[0]; m; m &= m - 1) P.e_hf_1b += c->I.h(__builtin_ctzll(m), __builtin_ctzll(m));
+    if (c->time_sym) {
+      P.e_hf_1b *= 2.;
+    } else {
+      for (uint64_t m = c->dn[0]; m; m &= m - 1)
+        P.e_hf_1b += c->I.h(__builtin_ctzll(m), __builtin_ctzll(m));
+    }
+  }
 
+  // several states: the sources' thresholds use the largest |c| over the states
+  DevBuf<double> d_selc;
+  if (c->n_states > 1) {
+    d_selc.mt = &c->mem;
+    d_selc.resize(n_dets);
+    StatePtrs xs{};
+    for (unsigned k = 1; k < c->n_states; k++) xs.p[k - 1] = c->d_xcoef[k - 1].p;
+    k_max_coef<<<grid_for(n_dets, 256), 256, 0, s>>>(c->d_coef.p, xs,
+                                                     static_cast<int>(c->n_states - 1), n_dets,
+                                                     d_selc.p);
+    SHCI_LAUNCH_CHECK();
+    c->launches += 1;
+  }
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   const unsigned grid = static_cast<unsigned>(sms) * 8u;
   const uint64_t kCap = 1ull << 27;  // candidates per chunk
   size_t n_new_total = 0;
   DevBuf<uint64_t> cnt, pass_up, pass_dn, cu, cd;
-  DevBuf<double> epsm;
+  DevBuf<double> epsm, rejm;
   cnt.mt = pass_up.mt = pass_dn.mt = cu.mt = cd.mt = &c->mem;
-  epsm.mt = &c->mem;
+  epsm.mt = rejm.mt = &c->mem;
   for (uint32_t pass = 0; pass < 5; pass++) {
     P.pass = pass;
     P.up = c->d_up.p;
     P.dn = c->d_dn.p;
-    P.coef = c->d_coef.p;
+    P.coef = c->n_states > 1 ? d_selc.p : c->d_coef.p;
     P.set_up = c->set_up.p;
     P.set_dn = c->set_dn.p;
     P.set_n = static_cast<uint32_t>(c->set_up.n);
@@ -377,6 +493,10 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
     if (n_src) {
       cnt.resize(n_src + 1, 1.25);
       epsm.resize(n_src, 1.25);
+      if (P.rej_on) {
+        rejm.resize(n_src, 1.25);
+        SHCI_CUDA(cudaMemsetAsync(rejm.p, 0, n_src * 8, s));
+      }
       k_sel_count<<<grid, kSelWarps * 32, 0, s>>>(P, 0, n_src, cnt.p, epsm.p);
       SHCI_LAUNCH_CHECK();
       std::vector<uint64_t> hc(n_src);
@@ -403,7 +523,8 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
           cd.resize(tot, 1.25);
           {
             ProfScope ps(c->prof, s, "select_emit");
-            k_sel_emit<<<grid, kSelWarps * 32, 0, s>>>(P, k0, k1, d_off.p, epsm.p + k0, cu.p, cd.p);
+            k_sel_emit<<<grid, kSelWarps * 32, 0, s>>>(P, k0, k1, d_off.p, epsm.p + k0, cu.p, cd.p,
+                                                       P.rej_on ? rejm.p + k0 : nullptr);
             SHCI_LAUNCH_CHECK();
           }
           // compact valid candidates, then sort + unique
@@ -417,7 +538,8 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
         }
         k0 = k1;
       }
-      k_sel_mark<<<grid_for(n_src, 256), 256, 0, s>>>(P, 0, n_src, epsm.p);
+      k_sel_mark<<<grid_for(n_src, 256), 256, 0, s>>>(P, 0, n_src, epsm.p,
+                                                      P.rej_on ? rejm.p : nullptr);
       SHCI_LAUNCH_CHECK();
       c->launches += 2;
     }
@@ -436,6 +558,16 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
       SHCI_CUDA(cudaMemcpyAsync(c->d_dn.p + old, pass_dn.p, pass_n * 8, cudaMemcpyDeviceToDevice, s));
       k_fill_coef<<<grid_for(pass_n, 256), 256, 0, s>>>(c->d_coef.p, old, old + pass_n, 1e-16);
       SHCI_LAUNCH_CHECK();
+      // states 1..: 1e-16, except that while the list is small (<= 50 dets when this step
+      // began) det k starts as state k's unit vector (solver.h:479-486)
+      for (unsigned k = 1; k < c->n_states; k++) {
+        auto& xc = c->d_xcoef[k - 1];
+        xc.grow_keep(old + pass_n, s);
+        k_fill_coef<<<grid_for(pass_n, 256), 256, 0, s>>>(xc.p, old, old + pass_n, 1e-16);
+        SHCI_LAUNCH_CHECK();
+        if (n_dets <= 50 && k >= old && k < old + pass_n)
+          k_fill_coef<<<1, 32, 0, s>>>(xc.p, k, k + 1, 1.0);
+      }
       SHCI_CUDA(cudaStreamSynchronize(s));
       n_new_total += pass_n;
       // the new dets join the membership set before the next pass

@@ -1,6 +1,6 @@
 // Variational stage on the device: Solver<S>::run_all_variations / run_variation
-// (src/solver/solver.h:338-397, 413-539) with n_states = 1, driving selection (select.cu),
-// the Hamiltonian build (hbuild.cu) and Davidson (davidson.cu).
+// (src/solver/solver.h:338-397, 413-539), driving selection (select.cu), the Hamiltonian build
+// (hbuild.cu) and Davidson (davidson.cu; several states when c->n_states > 1).
 #include <cmath>
 
 #include "ctx.h"
@@ -22,12 +22,25 @@ static double run_variation(shci_ctx* c, double eps_var, bool until_converged, d
       build_hamiltonian(c, precision);
     }
     const double tol = until_converged ? target_error / 500000 : target_error / 50;
-    DavidsonOut r = davidson(c, tol);
-    double e = r.eval;
-    if (precision == SHCI_PREC_MIXED) e = rayleigh_fp64(c);  // final FP64 correction
+    DavidsonOut r;
+    if (c->n_states == 1) {
+      r = davidson(c, tol);
+      c->state_energy.assign(1, r.eval);
+      if (precision == SHCI_PREC_MIXED) c->state_energy[0] = rayleigh_fp64(c);  // FP64 correction
+    } else {
+      DavidsonStatesOut rs = davidson_states(c, tol);
+      r.eval = rs.evals[0];
+      r.converged = rs.converged;
+      r.n_matvec = rs.n_matvec;
+      c->state_energy = rs.evals;
+      if (precision == SHCI_PREC_MIXED)
+        for (unsigned k = 0; k < c->n_states && k < c->H.n; k++)
+          c->state_energy[k] = rayleigh_fp64_of(c, state_coef(c, k));
+    }
+    const double e = c->state_energy[0];
     if (trace)
       trace->push_back(VarIter{n_dets_new, 2 * (c->H.nnz + c->H.n) - c->H.n, e, r.eval,
-                               r.converged, r.n_matvec});
+                               r.converged, r.n_matvec, c->state_energy});
     if (n_dets_new < n_dets * 1.001) dets_converged = true;
     if (dets_converged && r.converged) converged = true;
     n_dets = n_dets_new;

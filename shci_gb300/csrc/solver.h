@@ -15,6 +15,7 @@ struct VarIter {
   double eval;        // Davidson eigenvalue
   bool converged;
   int n_matvec;
+  std::vector<double> energies;  // every state's reported energy (n_states > 1)
 };
 
 std::vector<double> run_all_variations(shci_ctx* c, const std::vector<double>& eps_vars,

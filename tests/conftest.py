@@ -34,6 +34,26 @@ def w1_fcidump(data_dir):
 
 
 @pytest.fixture(scope="session")
+def cr_fcidump(data_dir):
+    """The reference's Cr-dimer FCIDUMP (38 orbitals, D-infinity-h), unpacked from the
+    committed gzip copy."""
+    import gzip
+    path = os.path.join(data_dir, "cr_dimer_FCIDUMP")
+    if not os.path.exists(path):
+        with gzip.open(os.path.join(GOLDEN, "cr_dimer", "FCIDUMP.gz"), "rb") as f:
+            data = f.read()
+        with open(path, "wb") as g:
+            g.write(data)
+    return path
+
+
+@pytest.fixture(scope="session")
+def cr_pins():
+    import json
+    return json.load(open(os.path.join(GOLDEN, "cr_dimer_pins.json")))
+
+
+@pytest.fixture(scope="session")
 def c_atom_pins():
     import json
     return json.load(open(os.path.join(GOLDEN, "c_atom_pins.json")))

@@ -66,3 +66,111 @@ def test_cli_stock_stochastic_settings(tmp_path):
     tot = res["energy_total"]["5.00e-05"]["5.00e-08"]
     ref_tot = ref["energy_total"]["5.00e-05"]["5.00e-08"]
     assert abs(tot["value"] - ref_tot["value"]) < 5 * (tot["uncert"] + ref_tot["uncert"])
+
+
+def _read_wf(path):
+    """Reads a wf_eps1_*.dat file of this build (layout documented in cli/wf_file.h)."""
+    import struct
+
+    import numpy as np
+    b = open(path, "rb").read()
+    assert b[:8] == b"SHCIGWF1"
+    n_up, n_dn, n_states, time_sym = struct.unpack_from("<4I", b, 8)
+    n, e_hf, e_var = struct.unpack_from("<Qdd", b, 24)
+    o = 48
+    up = np.frombuffer(b, np.uint64, n, o)
+    dn = np.frombuffer(b, np.uint64, n, o + 8 * n)
+    coefs = np.frombuffer(b, np.float64, n, o + 16 * n)
+    assert len(b) == o + 24 * n and (n_states, time_sym) == (1, 0)
+    return dict(n_up=n_up, n_dn=n_dn, e_hf=e_hf, e_var=e_var, up=up, dn=dn, coefs=coefs)
+
+
+def test_cli_wavefunction_files(tmp_path):
+    """wf_eps1_<eps>.dat checkpoints: written after each eps_var, loaded instead of recomputed
+    on the next run (solver.h:348-397), read by the PT2 stage under skip_var; a file of another
+    format is neither read nor overwritten."""
+    import numpy as np
+    from shci_gb300 import build
+    exe = build.build_cli()
+    base = {"system": "chem", "n_up": 4, "n_dn": 2, "eps_vars": [2e-4, 1e-4],
+            "eps_vars_schedule": [2e-3, 1e-3, 5e-4], "chem": {"point_group": "d2h"},
+            "eps_pt_dtm": 5e-6, "eps_pt_psto": 5e-6, "eps_pt": 5e-6}
+
+    def run(d, **kw):
+        d.mkdir(exist_ok=True)
+        if not (d / "FCIDUMP").exists():
+            shutil.copyfile(C_ATOM, d / "FCIDUMP")
+        (d / "config.json").write_text(json.dumps(dict(base, **kw)))
+        r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr
+        return r.stdout, json.load(open(d / "result.json"))
+
+    a = tmp_path / "a"
+    out1, res1 = run(a)  # variation + PT2, writes the files
+    w = {e: _read_wf(a / ("wf_eps1_%s.dat" % e)) for e in ("2.00e-04", "1.00e-04")}
+    for e, f in w.items():
+        assert (f["n_up"], f["n_dn"]) == (4, 2)
+        assert f["e_var"] == res1["energy_var"][e]
+        assert f["e_hf"] == res1["energy_hf"]
+        assert abs(np.dot(f["coefs"], f["coefs"]) - 1.0) < 1e-10
+        # (thousands separators only where the en_US locale is installed)
+        assert "ndets= {}".format(len(f["up"])) in out1.replace(",", "")
+    # second run in the same directory: both stages loaded, nothing recomputed
+    (a / "result.json").unlink()
+    out2, res2 = run(a)
+    assert ("Loaded {} dets from: wf_eps1_1.00e-04.dat".format(len(w["1.00e-04"]["up"]))
+            in out2.replace(",", ""))
+    assert "Iteration 1 " not in out2
+    assert res2["energy_var"] == res1["energy_var"]
+    assert res2["energy_total"] == res1["energy_total"]
+    # PT2 only, from the files
+    b = tmp_path / "b"
+    b.mkdir()
+    for e in ("2.00e-04", "1.00e-04"):
+        shutil.copyfile(a / ("wf_eps1_%s.dat" % e), b / ("wf_eps1_%s.dat" % e))
+    out3, res3 = run(b, skip_var=True)
+    assert "Iteration" not in out3
+    assert res3["energy_total"] == res1["energy_total"]
+    # a file of another format is left alone and the stage is computed
+    c = tmp_path / "c"
+    c.mkdir()
+    (c / "wf_eps1_2.00e-04.dat").write_bytes(b"\x00hps-like bytes")
+    out4, res4 = run(c, eps_vars=[2e-4], var_only=True)
+    assert "not a wavefunction file of this build" in out4
+    assert (c / "wf_eps1_2.00e-04.dat").read_bytes() == b"\x00hps-like bytes"
+    assert res4["energy_var"]["2.00e-04"] == res1["energy_var"]["2.00e-04"]
+
+
+def test_cli_two_states(tmp_path):
+    """n_states = 2: every state's energy_var and energy_total under the reference's keys
+    (state suffix "_1", solver.h:1406-1412), the "Iteration" lines with both energies, and a
+    wavefunction file holding both states; the energies equal the library's several-state run."""
+    import struct
+
+    import numpy as np
+    import shci_gb300 as S
+    from shci_gb300 import build
+    exe = build.build_cli()
+    shutil.copyfile(C_ATOM, tmp_path / "FCIDUMP")
+    cfg = {"system": "chem", "n_up": 4, "n_dn": 2, "n_states": 2, "eps_vars": [2e-4],
+           "eps_vars_schedule": [2e-3, 1e-3, 5e-4], "chem": {"point_group": "d2h"},
+           "eps_pt_dtm": 1e-5, "eps_pt_psto": 1e-5, "eps_pt": 1e-5, "gpu": {"precision": "fp64"}}
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr
+    res = json.load(open(tmp_path / "result.json"))
+    e0, e1 = res["energy_var"]["2.00e-04"], res["energy_var_1"]["2.00e-04"]
+    assert e0 < e1
+    assert "1.00e-05" in res["energy_total"]["2.00e-04"]
+    assert "1.00e-05" in res["energy_total_1"]["2.00e-04"]
+    assert "(state 1)" in r.stdout
+    it_lines = [l for l in r.stdout.splitlines() if l.startswith("Iteration ")]
+    assert it_lines and all(len(l.split("energy=")[1].split()) == 2 for l in it_lines)
+    b = (tmp_path / "wf_eps1_2.00e-04.dat").read_bytes()
+    assert struct.unpack_from("<4I", b, 8)[2] == 2
+    c = S.Context()
+    c.load_fcidump(tmp_path / "FCIDUMP", 4, 2, "d2h")
+    c.set_n_states(2)
+    c.run_variation([2e-4], [2e-3, 1e-3, 5e-4], 5e-5)
+    assert np.max(np.abs(c.state_energies() - [e0, e1])) < 1e-12
+    c.close()

@@ -1,0 +1,98 @@
+"""Orbital-optimisation inputs from the device RDMs (src/chem/optimization.cc): the generalized
+Fock matrix (:620-650), the parameter pairs (:500-522) and the gradient 2 (F_pq - F_qp)
+(:565-578), against the oracle's restatement on the same wavefunction, plus two checks that
+do not lean on the oracle: the energy identity E = e_core + (sum_pq D_pq h_pq + sum_m F_mm) / 2
+and the gradient as the derivative of the energy under orbital rotations (central differences
+of E(kappa) with the RDMs held fixed)."""
+import numpy as np
+import pytest
+
+from conftest import C_ATOM
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c_atom_var(oracle_mod):
+    import shci_gb300 as S
+    c = S.Context()
+    c.load_fcidump(C_ATOM, 4, 2, "d2h")
+    e = c.run_variation([2e-4], [2e-3, 1e-3, 5e-4], 5e-5)
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    up, dn, coefs = c.dets()
+    o.set_dets(up, dn, coefs)
+    o.update_hamiltonian()
+    return dict(c=c, o=o, e=e[0])
+
+
+def _energy_from_rdms(g1, half, h1, g2, e_core):
+    """E = e_core + sum_pq D_pq h_pq + 1/2 sum Gamma(m,r,s,q) (mq|rs) for fixed RDMs."""
+    n = h1.shape[0]
+    nn = n * n
+    idx = np.arange(nn)
+    a, b = np.meshgrid(idx, idx, indexing="ij")
+    hi, lo = np.maximum(a, b), np.minimum(a, b)
+    G = half[hi * (hi + 1) // 2 + lo].reshape(n, n, n, n)  # G[m, q, r, s] = Gamma(m, r, s, q)
+    return e_core + np.sum(g1 * h1) + 0.5 * np.einsum("mqrs,mqrs->", G, g2)
+
+
+def test_generalized_fock_and_gradient(c_atom_var):
+    c, o = c_atom_var["c"], c_atom_var["o"]
+    F = c.generalized_fock()
+    g1, half = o.rdm1(), o.rdm2_half()
+    oF = o.generalized_fock(g1, half)
+    assert np.max(np.abs(F - oF)) < 1e-10
+    h1, g2, sym, _, e_core = c.integrals()
+    assert np.all(F[sym[:, None] != sym[None, :]] == 0.0)
+    # energy identity (Helgaker 10.8.24 traced): the variational energy
+    e = e_core + 0.5 * (np.sum(g1 * h1) + np.trace(F))
+    assert abs(e - c_atom_var["e"]) < 1e-9
+    p, q = c.orbital_parameters()
+    op, oq = o.orbital_parameters()
+    assert np.array_equal(p, op) and np.array_equal(q, oq) and len(p) > 0
+    g = c.orbital_gradient(p, q)
+    assert np.max(np.abs(g - 2 * (oF[p, q] - oF[q, p]))) < 1e-10
+    assert np.max(np.abs(g)) > 1e-6  # a truncated wavefunction is not stationary in the orbitals
+    # the gradient is dE/dkappa for the rotation exp(K), K_pq = -kappa, K_qp = kappa
+    # (fill_rot_matrix_with_parameters, optimization.cc:524-540), RDMs fixed
+    from scipy.linalg import expm
+    n = h1.shape[0]
+    step = 1e-4
+    worst = 0.0
+    for k in np.argsort(-np.abs(g))[:6]:
+        es = []
+        for sgn in (1, -1):
+            K = np.zeros((n, n))
+            K[p[k], q[k]] = -sgn * step
+            K[q[k], p[k]] = sgn * step
+            U = expm(K)
+            h1r = U.T @ h1 @ U
+            g2r = np.einsum("pi,qj,rk,sl,pqrs->ijkl", U, U, U, U, g2, optimize=True)
+            es.append(_energy_from_rdms(g1, half, h1r, g2r, e_core))
+        fd = (es[0] - es[1]) / (2 * step)
+        worst = max(worst, abs(abs(fd) - abs(g[k])))
+        assert np.sign(fd) == np.sign(g[k]) or abs(g[k]) < 1e-8
+    assert worst < 1e-7
+
+
+def test_generalized_fock_two_states(oracle_mod):
+    """Two states: F is formed from the RDMs summed over the states (rdm.cc:222-231)."""
+    import shci_gb300 as S
+    c = S.Context()
+    c.load_fcidump(C_ATOM, 4, 2, "d2h")
+    c.set_n_states(2)
+    c.run_variation([5e-4], [2e-3, 1e-3], 5e-5)
+    F = c.generalized_fock()
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    up, dn, c0 = c.dets()
+    c1 = c.state_coefs(1)
+    o.set_dets(up, dn, c0)
+    o.update_hamiltonian()
+    g1, half = o.rdm1(), o.rdm2_half()
+    o.set_coefs(c1)
+    g1, half = g1 + o.rdm1(), half + o.rdm2_half()
+    assert np.max(np.abs(F - o.generalized_fock(g1, half))) < 1e-10
+    h1, _, _, _, e_core = c.integrals()
+    es = c.state_energies()
+    assert abs(2 * e_core + 0.5 * (np.sum(g1 * h1) + np.trace(F)) - es.sum()) < 1e-9
+    c.close()

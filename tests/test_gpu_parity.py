@@ -202,6 +202,57 @@ def test_variation_synthetic_matches_oracle(shci, oracle_mod, w1_fcidump):
     assert np.array_equal(up, oup) and np.array_equal(dn, odn)
 
 
+@pytest.mark.parametrize("which", ["c_atom", "w1"])
+def test_variation_second_rejection_matches_oracle(shci, oracle_mod, w1_fcidump, which):
+    """Selection with second rejection (config "second_rejection", factor 0.2): per-iteration
+    det and nonzero counts, det lists (order included) and energies equal the oracle's; the
+    rejection changes the result (fewer dets than without it).  The eps_tried_prev memo is
+    compared bit for bit in test_second_rejection_step_bitexact (here each side's memo follows
+    its own Davidson vector, whose small coefficients differ in relative terms)."""
+    if which == "c_atom":
+        args, eps, sched = (C_ATOM, 4, 2, "d2h"), [1e-4], SCHED_C
+    else:
+        args, eps, sched = (w1_fcidump, 5, 5), [2e-4, 1e-4], []
+    o = oracle_mod.Oracle(*args)
+    eo = o.run_all_variations(eps, sched, 5e-5, second_rejection=True)
+    c = new_ctx(shci, *args)
+    c.set_second_rejection(True, 0.2)
+    e = c.run_variation(eps, sched, 5e-5)
+    assert np.max(np.abs(e - eo)) < 1e-9
+    nd, nz, _ = c.var_trace()
+    ond, onz, _ = o.iterations()
+    assert np.array_equal(nd, ond) and np.array_equal(nz, onz)
+    up, dn, _ = c.dets()
+    oup, odn, _ = o.dets()
+    assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+    plain = new_ctx(shci, *args)
+    plain.run_variation(eps, sched, 5e-5)
+    assert plain.n_dets() > c.n_dets()
+
+
+def test_second_rejection_step_bitexact(shci, oracle_mod):
+    """One selection step with second rejection from the same coefficients: det list and the
+    eps_tried_prev memo bit for bit (memo entries from a rejected |H| included)."""
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o.run_all_variations([1e-3], [2e-3], 5e-5, second_rejection=True)
+    up, dn, coefs = o.dets()
+    c = new_ctx(shci, C_ATOM, 4, 2, "d2h")
+    c.build_queues()
+    c.set_dets(up, dn, coefs)
+    c.set_second_rejection(True, 0.2)
+    o2 = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o2.set_dets(up, dn, coefs)
+    o2.L.orc_set_second_rejection(o2.h, 1)
+    assert c.select(5e-4) == o2.select(5e-4)
+    gu, gd, _ = c.dets()
+    ou, od, _ = o2.dets()
+    assert np.array_equal(gu, ou) and np.array_equal(gd, od)
+    ge, oe = c.eps_tried()[:len(up)], o2.eps_tried()[:len(up)]
+    assert np.array_equal(ge, oe)
+    rejected = np.abs(ge - 1.000000001 * 5e-4 / np.abs(coefs)) > 1e-12 * ge
+    assert rejected.sum() > 0  # some memo entries come from a rejected |H|
+
+
 def test_pt2_dtm_matches_oracle_and_reference(shci, oracle_mod, c_oracle, c_atom_pins):
     up, dn, coefs = c_oracle.dets()
     c = new_ctx(shci, C_ATOM, 4, 2, "d2h")

@@ -181,3 +181,102 @@ def test_oracle_w2_pins(oracle_mod, data_dir):
         assert abs(a["energy"] - b["energy"]) < 1e-10
     assert got["pt_dtm"]["n_pt_dets"] == pins["pt_dtm"]["n_pt_dets"]
     assert abs(got["pt_dtm"]["correction"] - pins["pt_dtm"]["correction"]) < 1e-12
+
+
+def test_oracle_cr_dimer_linear_group(oracle_mod, cr_fcidump, cr_pins):
+    """The reference's Cr-dimer run (examples/Cr: 38 orbitals, 10a4b, point group D-infinity-h):
+    HF energy, heat-bath queue size and maximum, and for every variational iteration up to the
+    first at eps_var = 2e-4 the det count, symmetric nonzero count, energy and each Davidson
+    step's eigenvalue estimate, as the log prints them."""
+    p = cr_pins
+    o = oracle_mod.Oracle(cr_fcidump, p["n_up"], p["n_dn"], p["point_group"])
+    info = o.info()
+    assert abs(info["energy_hf"] - p["energy_hf"]) < 1e-9
+    assert abs(info["max_hci"] - p["max_hci_queue_elem"]) < 1e-9
+    assert info["n_hci"] == p["n_hci_queue_entries"]
+    te = p["target_error"]
+    for it in p["iterations"]:
+        main = it["eps1"] in p["eps_vars"]
+        o.select(it["eps1"])
+        nz = o.update_hamiltonian()
+        _, _, c = o.dets()
+        # solver.h:500-501: target_error / 50 for schedule steps, / 500000 to convergence
+        e, c2, _, tr = o.davidson(c, te / 500000 if main else te / 50)
+        o.set_coefs(c2)
+        assert len(c) == it["n_dets"]
+        assert 2 * nz - len(c) == it["nnz"]  # upper elements + diagonal -> symmetric count
+        assert abs(e - it["energy"]) < 1e-8
+        assert len(tr) == len(it["davidson"])
+        assert np.max(np.abs(np.array(tr) - it["davidson"])) < 2e-10
+
+
+def test_oracle_several_states(oracle_mod):
+    """The several-state restatement (davidson.cc with n_states > 1, selection on the largest
+    coefficient, unit-vector start of the excited states): with one state its Davidson equals
+    the one-state path; on the C atom with three states (eps_var 1e-4) the converged state
+    energies are the three lowest eigenvalues of the final Hamiltonian (an independent sparse
+    eigensolver), and the first Hilbert-matrix state of davidson_test.cc is reproduced."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    n = 400
+    rp, cols, vals = [0], [], []
+    for i in range(n):
+        for j in range(i, n):
+            cols.append(j)
+            vals.append(-1.0 / (2 * i + 1) if i == j else -1.0 / 10.0 / (i + j + 1))
+        rp.append(len(cols))
+    e1, v1, _ = oracle_mod.davidson_csr(rp, cols, vals, np.r_[1.0, np.zeros(n - 1)], 1e-6)
+    ev, vecs, _ = oracle_mod.davidson_csr_states(rp, cols, vals, np.eye(1, n), 1e-6)
+    assert ev[0] == e1 and np.max(np.abs(vecs[0] - v1)) < 1e-15
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o.set_n_states(3)
+    o.run_all_variations([1e-4], [2e-3, 1e-3, 5e-4, 2e-4], 5e-5)
+    e, per_iter = o.state_energies()
+    assert per_iter.shape[1] == 3 and np.array_equal(per_iter[-1], e)
+    nz = o.update_hamiltonian()
+    rp, cl, vl = o.hamiltonian(nz)
+    m = len(rp) - 1
+    U = sp.csr_matrix((vl, cl, rp), shape=(m, m))
+    H = U + U.T - sp.diags(U.diagonal())
+    w = np.sort(sla.eigsh(H, k=3, which="SA", tol=1e-12)[0])
+    assert np.max(np.abs(w - e)) < 1e-7
+
+
+def test_oracle_time_sym_is_the_projected_hamiltonian(oracle_mod, w1_fcidump):
+    """The oracle's time_sym traversal (hamiltonian.h:415-598 with the reverse passes) against
+    an independent construction: P^T H P with H the ordinary Hamiltonian of the unpacked list and
+    P the isometry packed -> unpacked (an open det a -> (|a> + |a~>) / sqrt(2)).  Same element
+    set, values to 1e-13; the time_sym variational energies equal the plain run's, whose det
+    space is the unpacked one."""
+    import scipy.sparse as sp
+    o = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    o.set_time_sym(True)
+    e = o.run_all_variations([2e-4, 1e-4], [], 5e-5)
+    p = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    ep = p.run_all_variations([2e-4, 1e-4], [], 5e-5)
+    assert np.max(np.abs(e - ep)) < 1e-8
+    up, dn, _ = o.dets()
+    n = len(up)
+    assert np.all(up <= dn)
+    nz = o.update_hamiltonian()
+    rp, cl, vl = o.hamiltonian(nz)
+    U = sp.csr_matrix((vl, cl.astype(np.int64), rp.astype(np.int64)), shape=(n, n))
+    Hts = (U + U.T - sp.diags(U.diagonal())).tocsr()
+    op = up != dn
+    uu, ud = np.r_[up, dn[op]], np.r_[dn, up[op]]
+    pup, pdn, _ = p.dets()
+    assert set(zip(uu.tolist(), ud.tolist())) == set(zip(pup.tolist(), pdn.tolist()))
+    m = len(uu)
+    q = oracle_mod.Oracle(w1_fcidump, 5, 5)
+    q.set_dets(uu, ud, np.ones(m))
+    nq = q.update_hamiltonian()
+    rq, cq, vq = q.hamiltonian(nq)
+    Uq = sp.csr_matrix((vq, cq.astype(np.int64), rq.astype(np.int64)), shape=(m, m))
+    Hu = Uq + Uq.T - sp.diags(Uq.diagonal())
+    rows = np.r_[np.arange(n), n + np.arange(op.sum())]
+    cols = np.r_[np.arange(n), np.nonzero(op)[0]]
+    vals = np.r_[np.where(op, 1 / np.sqrt(2), 1.0), np.full(op.sum(), 1 / np.sqrt(2))]
+    P = sp.csr_matrix((vals, (rows, cols)), shape=(m, n))
+    Hp = (P.T @ Hu @ P).tocsr()
+    assert abs(Hts - Hp).max() < 1e-13
+    assert Hts.nnz == (abs(Hp) >= 1e-12).sum()
