@@ -168,6 +168,10 @@ struct shci_ctx {
   shci::DevBuf<long long> dfix;
   int dfix_scale = 0;
   bool dfix_valid = false;
+  // PT2 single-excitation elements in 64-bit fixed point (pt2.cu): h_pq, (pq|oo), (po|oq)
+  shci::DevBuf<long long> sfix;
+  int sfix_scale = 0;
+  double sfix_margin = 0.0;
   shci::DevIntegrals dI{};
   double energy_hf = 0.0;
 

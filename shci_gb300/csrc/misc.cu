@@ -188,7 +188,7 @@ void get_rows(shci_ctx* c, const uint64_t* rows, size_t m, uint64_t* offsets, ui
 void upload_integrals(shci_ctx* c) {
   const auto& I = c->I;
   const size_t n = I.n;
-  c->dfix_valid = false;
+  c->dfix_valid = false;  // also marks the single-excitation tables (built with it)
   std::vector<double> d(n * n * n), x(n * n * n), j(n * n), k(n * n);
   for (size_t a = 0; a < n; a++)
     for (size_t b = 0; b < n; b++) {

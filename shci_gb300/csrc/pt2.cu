@@ -159,6 +159,51 @@ struct OutCols {
   double* v[5];
 };
 
+// Single-excitation elements in 64-bit fixed point.  H_ij of a single excitation p -> q is
+// +-(h_pq + sum_o (pq|oo) [2 (pq|oo) for a doubly occupied o] - sum_o (po|oq)), about 2 n_e
+// table entries (chem_system.cc:544-577); in FP64 that chain of dependent additions kept
+// the FP64 pipe (about two operations per SM cycle on GB300) half busy in the emission.  Here
+// every entry is rounded once to a multiple of 2^-s and the sum is exact on the integer pipe;
+// |fixed - FP64| <= margin (entry rounding plus the FP64 evaluation's own rounding).  A
+// value within margin |c_i| of a threshold is formed again in FP64, so every keep / split
+// decision is the FP64 one; kept values differ from it by at most margin |c_i|.
+struct SingleFix {
+  const long long* h1;  // [n*n]
+  const long long* d;   // [n^3] (pq|oo) at (p n + q) n + o
+  const long long* x;   // [n^3] (po|oq) at (p n + q) n + o
+  int n;
+  double inv_scale;     // 2^-s
+  double margin;
+};
+
+__device__ __forceinline__ double h_one_fix(const SingleFix& F, uint64_t ui, uint64_t di,
+                                            uint64_t uj, uint64_t dj) {
+  const uint64_t xu = ui ^ uj;
+  const bool alpha = xu != 0;
+  const uint64_t si = alpha ? ui : di, sj = alpha ? uj : dj;
+  uint64_t oppo = alpha ? di : ui;
+  const uint64_t x = si ^ sj;
+  const int oi = ctz64(si & x), oj = ctz64(sj & x);
+  const int n = F.n;
+  const size_t row = (size_t)(oi * n + oj) * n;
+  const long long* D = F.d + row;
+  const long long* X = F.x + row;
+  long long e = __ldg(F.h1 + oi * n + oj);
+  for (uint64_t m = si & ~(1ull << oi) & ~(1ull << oj); m; m &= m - 1) {
+    const int o = ctz64(m);
+    e -= __ldg(X + o);
+    const long long dd = __ldg(D + o);
+    if (oppo >> o & 1) {
+      oppo &= ~(1ull << o);
+      e += 2 * dd;
+    } else {
+      e += dd;
+    }
+  }
+  for (uint64_t m = oppo; m; m &= m - 1) e += __ldg(D + ctz64(m));
+  return flip_sign(static_cast<double>(e) * F.inv_scale, move_parity(si, oi, oj));
+}
+
 constexpr uint32_t kPtQ = 64;  // per-warp queue of batch members (< 32 waiting + 32 pushed)
 struct PtQueue {
   uint64_t u[kPtQ];
@@ -181,9 +226,9 @@ struct PtQueue {
 // with an exact count.
 template <int MODE>
 __global__ void __launch_bounds__(kPtWarps * 32, 4)
-    k_pt_emit(SelParams P, PtParams Q, StoSources S, uint32_t k_begin, uint32_t k_end,
-              const uint64_t* off, uint64_t* out_up, uint64_t* out_dn, OutCols out,
-              uint8_t* overflow) {
+    k_pt_emit(SelParams P, PtParams Q, StoSources S, SingleFix F, uint32_t k_begin,
+              uint32_t k_end, const uint64_t* off, uint64_t* out_up, uint64_t* out_dn,
+              OutCols out, uint8_t* overflow) {
   __shared__ PtQueue qs[kPtWarps];
   PtQueue& q = qs[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31;
@@ -215,7 +260,16 @@ __global__ void __launch_bounds__(kPtWarps * 32, 4)
       // the pilot's handler tests |H_ai c_i| for single excitations only (solver.h:958-962)
       const bool test = MODE != kSto || !Q.pilot || popc64(up ^ cu) + popc64(dn ^ cd) == 2;
       if (ok && test) {
-        hc = h_offdiag(P.I, up, dn, cu, cd) * coef;
+        if (popc64(up ^ cu) + popc64(dn ^ cd) == 2) {  // single excitation
+          hc = h_one_fix(F, up, dn, cu, cd) * coef;
+          const double a = fabs(hc), m = F.margin * fabs(coef);
+          bool near = fabs(a - Q.eps) <= m;
+          if (MODE == kPsto) near = near || fabs(a - Q.eps_dtm) <= m;
+          if (MODE == kSto) near = near || fabs(a - Q.eps_psto) <= m;
+          if (near) hc = h_one(P.I, up, dn, cu, cd) * coef;
+        } else {
+          hc = h_two(P.I, up, dn, cu, cd) * coef;
+        }
         if (fabs(hc) < Q.eps) ok = false;
       }
       out_up[pos] = ok ? (cu | iter_tag) : kInvalid;
@@ -507,6 +561,51 @@ DiagFix diag_fix(shci_ctx* c) {
   return DiagFix{c->dfix.p, n, std::ldexp(1.0, -c->dfix_scale), I.e_core};
 }
 
+// Fixed-point single-excitation tables (built with the diagonal tables, once per set of
+// integrals).  Scale: the largest |sum| (h_pq plus at most 2 n_e entries, doubled ones
+// counted twice) stays below 2^62.  margin = the rounding of the entries (2^-(s+1) each,
+// twice for a doubled one) + the FP64 evaluation's rounding (each of its <= 2 n_e + 1
+// additions within 2^-53 of a partial sum <= bound) + the final product by c_i, generously.
+SingleFix single_fix(shci_ctx* c) {
+  const auto& I = c->I;
+  const int n = static_cast<int>(I.n);
+  // new integrals invalidate the diagonal tables; rebuild these with them
+  const bool stale = !c->dfix_valid || c->sfix.n != (size_t)n * n + 2 * (size_t)n * n * n;
+  diag_fix(c);
+  if (stale) {
+    const size_t n2 = (size_t)n * n, n3 = n2 * n;
+    std::vector<double> v(n2 + 2 * n3, 0.0);
+    for (int p = 0; p < n; p++)
+      for (int q = 0; q < n; q++) {
+        v[(size_t)p * n + q] = I.h(p, q);
+        for (int o = 0; o < n; o++) {
+          v[n2 + ((size_t)p * n + q) * n + o] = I.g(p, q, o, o);
+          v[n2 + n3 + ((size_t)p * n + q) * n + o] = I.g(p, o, o, q);
+        }
+      }
+    double mh = 0.0, mt = 0.0;
+    for (size_t k = 0; k < n2; k++) mh = std::max(mh, std::fabs(v[k]));
+    for (size_t k = n2; k < v.size(); k++) mt = std::max(mt, std::fabs(v[k]));
+    const int n_e = static_cast<int>(I.n_up + I.n_dn);
+    const double terms = 3.0 * n_e + 1.0;  // bound on the number of entries, doubles twice
+    const double bound = mh + terms * mt;
+    int s = 60;
+    while (s > 0 && bound * std::ldexp(1.0, s) >= std::ldexp(1.0, 62)) s--;
+    std::vector<long long> t(v.size());
+    for (size_t k = 0; k < v.size(); k++) t[k] = std::llround(std::ldexp(v[k], s));
+    c->sfix.mt = &c->mem;
+    c->sfix.resize(t.size());
+    SHCI_CUDA(cudaMemcpyAsync(c->sfix.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice,
+                              c->stream));
+    SHCI_CUDA(cudaStreamSynchronize(c->stream));
+    c->sfix_scale = s;
+    c->sfix_margin = 4.0 * (terms * std::ldexp(1.0, -(s + 1)) + terms * bound * std::ldexp(1.0, -52));
+  }
+  const size_t n2 = (size_t)n * n, n3 = n2 * n;
+  return SingleFix{c->sfix.p, c->sfix.p + n2, c->sfix.p + n2 + n3, n,
+                   std::ldexp(1.0, -c->sfix_scale), c->sfix_margin};
+}
+
 struct PtSetup {
   SelParams P{};
   DevBuf<uint32_t> pairs;
@@ -608,8 +707,8 @@ void pt_emit_append(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSource
       }
       {
         ProfScope ps(c->prof, s, "pt2_emit");
-        k_pt_emit<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, k0, k1, d_off.p, cu.p,
-                                                          cd.p, oc, d_over.p);
+        k_pt_emit<MODE><<<st.grid, kPtWarps * 32, 0, s>>>(st.P, Q, S, single_fix(c), k0, k1,
+                                                          d_off.p, cu.p, cd.p, oc, d_over.p);
         SHCI_LAUNCH_CHECK();
       }
       c->launches += 1;
