@@ -50,16 +50,20 @@ class HostScope {
  public:
   HostScope(Profiler& p, const char* name)
       : p_(p), name_(name), t0_(std::chrono::steady_clock::now()) {}
-  ~HostScope() {
-    if (p_.on)
+  ~HostScope() { stop(); }
+  // records the time so far (once)
+  void stop() {
+    if (p_.on && !done_)
       p_.host(name_, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
                                                                t0_).count());
+    done_ = true;
   }
 
  private:
   Profiler& p_;
   const char* name_;
   std::chrono::steady_clock::time_point t0_;
+  bool done_ = false;
 };
 
 // Records an event pair around the enclosed launches when profiling is on.

@@ -25,7 +25,9 @@
 #include <numeric>
 #include <queue>
 #include <random>
+#include <future>
 #include <stack>
+#include <thread>
 #include <unordered_map>
 
 #include "ctx.h"
@@ -997,29 +999,6 @@ size_t pilot_pt_dets(shci_ctx* c, PtSetup& st, const std::vector<size_t>& src, d
   return pt_emit_reduce<kSto>(c, st, Q, S, n_src, hc, bu, bd, bv, shift + 5);
 }
 
-// Entry indices ordered by key (< key_end), stable: an LSD radix sort in two passes of up to
-// 16 bits over the key's bit width.
-std::vector<uint32_t> stable_order_by_key(const std::vector<uint32_t>& key, size_t key_end) {
-  const size_t n = key.size();
-  int bits = 1;
-  while (bits < 32 && (size_t{1} << bits) < key_end) bits++;
-  const int lo_bits = (bits + 1) / 2, hi_bits = bits - lo_bits;
-  std::vector<uint32_t> a(n), b(n);
-  std::iota(a.begin(), a.end(), 0u);
-  const int shifts[2] = {0, lo_bits};
-  const int widths[2] = {lo_bits, hi_bits};
-  for (int pass = 0; pass < 2; pass++) {
-    if (widths[pass] == 0) continue;
-    const uint32_t nb = 1u << widths[pass], mask = nb - 1u;
-    std::vector<uint32_t> cnt(nb + 1, 0u);
-    for (size_t k = 0; k < n; k++) cnt[((key[a[k]] >> shifts[pass]) & mask) + 1]++;
-    for (uint32_t d = 0; d < nb; d++) cnt[d + 1] += cnt[d];
-    for (size_t k = 0; k < n; k++) b[cnt[(key[a[k]] >> shifts[pass]) & mask]++] = a[k];
-    a.swap(b);
-  }
-  return a;
-}
-
 // Stochastic stage (solver.h:898-1153).  n_dets_in_sample = 0: the sample size comes from
 // the reference's 1,000-draw pilot and the PT memory pt_mem_avail (solver.h:942-1006);
 // semisto: the variational dets above the quantile of the top quarter of the unique-sample
@@ -1136,17 +1115,51 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     info[1] = n_dtm;
     info[2] = n_target;
   }
-  std::vector<double> aprob;
-  std::vector<size_t> alias;
-  alias_tables(probs, aprob, alias);
   std::uniform_int_distribution<size_t> ui_var(0, n_var - 1);
   std::uniform_int_distribution<size_t> ui_batch(0, n_batches - 1);
   const double factor = 1. / (n_dets_in_sample - n_dtm - 1.);
   // Iterations per device pass: the first pass runs the 6 iterations before which the
   // stopping rules cannot fire, later passes 2 (results past the stop are discarded).
   const uint32_t kFirstChunk = 6, kNextChunk = 2;
+  // A pass's random numbers in the reference's order (per iteration: its draws, then its
+  // batch, solver.h:1048-1072).  They depend on nothing but the generator, so a helper thread
+  // draws each pass ahead of it: the first while the alias tables are built, the next during
+  // the current pass's device work (a pass that turns out not to be needed only advanced the
+  // generator, which nothing uses afterwards).
+  const size_t n_draw = n_dets_in_sample - n_dtm;
+  struct PassDraws {
+    std::vector<std::vector<size_t>> r1;
+    std::vector<std::vector<double>> r2;
+    std::vector<size_t> batch;
+  };
+  auto draw_pass = [&gen, &ur, &ui_var, &ui_batch, n_draw](uint32_t n_it) {
+    PassDraws d;
+    d.r1.assign(n_it, std::vector<size_t>(n_draw));
+    d.r2.assign(n_it, std::vector<double>(n_draw));
+    d.batch.resize(n_it);
+    for (uint32_t it = 0; it < n_it; it++) {
+      for (size_t k = 0; k < n_draw; k++) {
+        d.r1[it][k] = ui_var(gen);
+        d.r2[it][k] = ur(gen);
+      }
+      d.batch[it] = ui_batch(gen);
+    }
+    return d;
+  };
+  std::future<PassDraws> next_draws;
+  if (max_iterations > 0)
+    next_draws = std::async(std::launch::async, draw_pass,
+                            static_cast<uint32_t>(std::min<size_t>(kFirstChunk, max_iterations)));
+  std::vector<double> aprob;
+  std::vector<size_t> alias;
+  alias_tables(probs, aprob, alias);
 
-  std::vector<uint32_t> cnt(n_var, 0u);  // per-iteration sample counts (zero between uses)
+  // per-iteration sample counts, one array per iteration of a pass (zero between uses); which
+  // iterations of a pass drew each det (zero between uses); the deterministic dets
+  std::vector<std::vector<uint32_t>> cnts;
+  std::vector<uint8_t> pass_mask(n_var, 0), is_dtm(n_var, 0);
+  for (uint32_t i : dtm_list) is_dtm[i] = 1;
+  static_assert(kFirstChunk <= 8 && kNextChunk <= 8, "iteration masks are 8 bits");
   if (c->prof.on)
     c->prof.host("pt2_host_setup", std::chrono::duration<double, std::milli>(
                                        std::chrono::steady_clock::now() - t_setup).count());
@@ -1163,78 +1176,98 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     std::vector<uint8_t> h_dtm;
     {
       HostScope hs(c->prof, "pt2_host_sample");
-      const size_t n_draw = n_dets_in_sample - n_dtm;
-      std::vector<size_t> r1s(n_draw);
-      std::vector<double> r2s(n_draw);
-      std::vector<uint32_t> ids(n_draw);
-      for (uint32_t it = 0; it < n_it; it++) {
-        // sample counts per det, and the dets in order of first draw (the reference's
-        // unordered_map counts and insertion-ordered list); cnt is cleared after use.
-        // The draws come first, in the reference's order; the alias lookups, independent of
-        // one another, then run as one loop whose cache misses overlap, with the table entries
-        // of a later draw prefetched (the tables are far larger than the host caches).
+      // the pass's random numbers (drawn ahead), then the next pass's, ahead of it
+      HostScope hs_rng(c->prof, "pt2_host_sample_rng");
+      PassDraws draws = next_draws.get();
+      hs_rng.stop();
+      const size_t it_next = iteration + n_it;
+      if (it_next < max_iterations)
+        next_draws = std::async(
+            std::launch::async, draw_pass,
+            static_cast<uint32_t>(std::min<size_t>(kNextChunk, max_iterations - it_next)));
+      const auto& r1s = draws.r1;
+      const auto& r2s = draws.r2;
+      const auto& batch_ids = draws.batch;
+      // Per iteration and on a host thread of its own: the alias lookups (independent of one
+      // another: one loop whose cache misses overlap, the table entries of a later draw
+      // prefetched; the tables are far larger than the host caches), the sample counts per det
+      // and the dets in order of first draw (the reference's unordered_map counts and
+      // insertion-ordered list).
+      while (cnts.size() < n_it) cnts.emplace_back(n_var, 0u);
+      std::vector<std::vector<uint32_t>> lists(n_it);
+      auto sample_one = [&](uint32_t it) {
         constexpr size_t kAhead = 32;
-        for (size_t k = 0; k < n_draw; k++) {
-          r1s[k] = ui_var(gen);
-          r2s[k] = ur(gen);
-        }
+        const auto& r1 = r1s[it];
+        const auto& r2 = r2s[it];
+        auto& cnt = cnts[it];
+        std::vector<uint32_t> ids(n_draw);
         for (size_t k = 0; k < n_draw; k++) {
           if (k + kAhead < n_draw) {
-            __builtin_prefetch(&aprob[r1s[k + kAhead]]);
-            __builtin_prefetch(&alias[r1s[k + kAhead]]);
+            __builtin_prefetch(&aprob[r1[k + kAhead]]);
+            __builtin_prefetch(&alias[r1[k + kAhead]]);
           }
-          const size_t r1 = r1s[k];
-          ids[k] = static_cast<uint32_t>(r2s[k] < aprob[r1] ? r1 : alias[r1]);
+          ids[k] = static_cast<uint32_t>(r2[k] < aprob[r1[k]] ? r1[k] : alias[r1[k]]);
         }
-        std::vector<size_t> list;
+        auto& list = lists[it];
         for (size_t k = 0; k < n_draw; k++) {
           if (k + kAhead < n_draw) __builtin_prefetch(&cnt[ids[k + kAhead]], 1);
           const uint32_t id = ids[k];
           if (cnt[id]++ == 0) list.push_back(id);
         }
-        const size_t batch_id = ui_batch(gen);
-        // the deterministic dets first (count and weight 1), then the sampled ones
-        for (uint32_t i : dtm_list) {
-          h_det.push_back(i);
-          h_iter.push_back(it);
-          h_batch.push_back(static_cast<uint32_t>(batch_id));
-          h_count.push_back(1.0);
-          h_weight.push_back(1.0);
-          h_dtm.push_back(1);
-        }
-        for (size_t k = 0; k < list.size(); k++) {
-          const size_t i = list[k];
-          h_det.push_back(static_cast<uint32_t>(i));
-          h_iter.push_back(it);
-          h_batch.push_back(static_cast<uint32_t>(batch_id));
-          h_count.push_back(static_cast<double>(cnt[i]));
-          h_weight.push_back((n_dets_in_sample - n_dtm) * probs[i]);
-          h_dtm.push_back(0);
-        }
-        for (size_t i : list) cnt[i] = 0;
-      }
-      // group the pass's entries by det (iteration order kept within a det): a det drawn in
-      // several iterations is walked once (the heaviest dets, with the widest windows, are
-      // drawn in nearly every iteration)
-      std::vector<uint32_t> order = stable_order_by_key(h_det, n_var);
-      auto permute = [&](auto& v) {
-        auto w = v;
-        for (size_t k = 0; k < order.size(); k++) w[k] = v[order[k]];
-        v.swap(w);
       };
-      permute(h_det);
-      permute(h_iter);
-      permute(h_batch);
-      permute(h_count);
-      permute(h_weight);
-      permute(h_dtm);
+      {
+        HostScope hs_look(c->prof, "pt2_host_sample_lookup");
+        std::vector<std::thread> th;
+        for (uint32_t it = 1; it < n_it; it++) th.emplace_back(sample_one, it);
+        sample_one(0);
+        for (auto& t : th) t.join();
+      }
+      HostScope hs_group(c->prof, "pt2_host_sample_group");
+      // The pass's entries grouped by det, dets in increasing order and a det's iterations in
+      // order: a det drawn in several iterations is walked once (the heaviest dets, with the
+      // widest windows, are drawn in nearly every iteration).  A bit mask per det marks the
+      // iterations that drew it (all of them for a deterministic det: count and weight 1); one
+      // scan of the masks in det order lays the entries out.
+      const uint8_t all_it = static_cast<uint8_t>((1u << n_it) - 1u);
+      size_t n_ent_pass = n_dtm * n_it;
+      for (uint32_t it = 0; it < n_it; it++) {
+        n_ent_pass += lists[it].size();
+        for (uint32_t i : lists[it]) pass_mask[i] |= static_cast<uint8_t>(1u << it);
+      }
+      for (uint32_t i : dtm_list) pass_mask[i] = all_it;
+      h_det.resize(n_ent_pass);
+      h_iter.resize(n_ent_pass);
+      h_batch.resize(n_ent_pass);
+      h_count.resize(n_ent_pass);
+      h_weight.resize(n_ent_pass);
+      h_dtm.resize(n_ent_pass);
       h_off.clear();
-      for (size_t k = 0; k < h_det.size(); k++)
-        if (k == 0 || h_det[k] != h_det[k - 1]) h_off.push_back(static_cast<uint32_t>(k));
-      h_off.push_back(static_cast<uint32_t>(h_det.size()));
-      for (size_t g = 0; g + 1 < h_off.size(); g++)
-        if (h_off[g + 1] - h_off[g] > 255)
-          throw std::logic_error("stochastic PT2: more than 255 draws of one det in a pass");
+      size_t k = 0;
+      for (size_t i = 0; i < n_var; i++) {
+        const uint32_t m = pass_mask[i];
+        if (!m) continue;
+        pass_mask[i] = 0;
+        h_off.push_back(static_cast<uint32_t>(k));
+        const bool dt = is_dtm[i] != 0;
+        for (uint32_t it = 0; it < n_it; it++) {
+          if (!(m >> it & 1u)) continue;
+          h_det[k] = static_cast<uint32_t>(i);
+          h_iter[k] = it;
+          h_batch[k] = static_cast<uint32_t>(batch_ids[it]);
+          if (dt) {
+            h_count[k] = 1.0;
+            h_weight[k] = 1.0;
+            h_dtm[k] = 1;
+          } else {
+            h_count[k] = static_cast<double>(cnts[it][i]);
+            cnts[it][i] = 0;
+            h_weight[k] = (n_dets_in_sample - n_dtm) * probs[i];
+            h_dtm[k] = 0;
+          }
+          k++;
+        }
+      }
+      h_off.push_back(static_cast<uint32_t>(k));
     }
     const uint32_t n_ent = static_cast<uint32_t>(h_det.size());
     const uint32_t n_src = static_cast<uint32_t>(h_off.size() - 1);  // dets of the pass
