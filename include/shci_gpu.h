@@ -158,8 +158,10 @@ shci_status shci_update_hamiltonian(shci_ctx* ctx, int precision, size_t* nnz_ou
  * context's budget, else the two-pass join, else the group scan. */
 shci_status shci_hamiltonian_stats(shci_ctx* ctx, uint64_t* stats);
 
-/* Device bytes held by the context now, the most it has held, and its budget (0: none)
- * (out[3]).  With a budget, an allocation past it fails with SHCI_ERR_OOM and leaves the
+/* Device bytes held by the context now, the most it has held, its budget (0: none), of the
+ * bytes held those in its cache of released blocks (returned to the driver before an
+ * allocation would fail; at most a quarter of the device), and the most held by live buffers
+ * (out[5]).  With a budget, an allocation past it fails with SHCI_ERR_OOM and leaves the
  * context usable. */
 shci_status shci_memory_stats(shci_ctx* ctx, size_t* out);
 

@@ -303,10 +303,17 @@ class Context:
                     cand_same_beta=int(s[6]), cand_same_alpha=int(s[7]), cand_mixed=int(s[8]))
 
     def memory_stats(self):
-        """(bytes held now, peak bytes held, budget) of the context's device memory."""
-        m = np.zeros(3, np.uint64)
+        """(bytes held now, peak bytes held, budget) of the context's device memory (the bytes
+        held include the context's cache of released blocks: memory_cached())."""
+        m = np.zeros(5, np.uint64)
         self._ck(self.L.shci_memory_stats(self.h, m))
         return int(m[0]), int(m[1]), int(m[2])
+
+    def memory_cached(self):
+        """(bytes in the cache of released blocks, peak bytes held by live buffers)"""
+        m = np.zeros(5, np.uint64)
+        self._ck(self.L.shci_memory_stats(self.h, m))
+        return int(m[3]), int(m[4])
 
     def hamiltonian_rows(self, rows):
         """Elements of the given rows (strict upper part): offsets, cols, FP64 values, each row

@@ -519,6 +519,8 @@ shci_status shci_memory_stats(shci_ctx* c, size_t* out) {
   out[0] = c->mem.used;
   out[1] = c->mem.peak;
   out[2] = c->mem.budget;
+  out[3] = c->mem.cached;
+  out[4] = c->mem.peak_live;
   return SHCI_OK;
 }
 

@@ -105,6 +105,10 @@ double run_slice(int device, const shci_batch_item* items, const std::vector<siz
         create_fail++;
         return;
       }
+      // the workers share the device: each keeps a cache of released blocks of at most its
+      // share of a quarter of the device (a worker's failing allocation returns only its own)
+      size_t f = 0, t = 0;
+      if (cudaMemGetInfo(&f, &t) == cudaSuccess) c->mem.cache_cap = std::max<size_t>(t / 4 / W, 1);
       for (size_t k; (k = next.fetch_add(1)) < end;) solve_one(c, items[order[k]], out[order[k]]);
       shci_destroy(c);
     });

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -33,11 +34,64 @@ struct OverflowError : std::runtime_error {
 
 #define SHCI_LAUNCH_CHECK() SHCI_CUDA(cudaGetLastError())
 
-// Tracks device bytes held by one context against an optional budget.
+// Device bytes held by one context against an optional budget, and the context's cache of
+// released blocks.  A build or a PT2 pass allocates and frees scratch of the same sizes again
+// and again (gigabytes at n = 40, where cudaMalloc / cudaFree of a large block costs about a
+// millisecond and the free synchronises the device); a released block is kept and handed to
+// the next request it fits (up to twice the size asked for).  All work of a context runs on
+// its one stream, so a block reused after a release is ordered after the work that used it.
+// A request that does not fit the device or the budget first returns the cache to the driver.
+// The cache holds at most a quarter of the device's memory, so the driver always keeps room
+// for what it allocates by itself (local memory of launches, library workspaces).
 struct MemTracker {
   size_t budget = 0;  // 0 = unlimited
-  size_t used = 0;
+  size_t used = 0;    // held: live blocks and cached ones
   size_t peak = 0;
+  size_t peak_live = 0;  // the most held by live blocks
+  size_t cached = 0;     // held in the cache
+  size_t cache_cap = 0;  // 0: not set yet (a quarter of the device's memory)
+  std::multimap<size_t, void*> cache;  // released blocks by size in bytes
+
+  MemTracker() = default;
+  MemTracker(const MemTracker&) = delete;
+  MemTracker& operator=(const MemTracker&) = delete;
+  ~MemTracker() { flush(); }
+
+  // A cached block of at least `bytes` (at most twice that); *got = its size.
+  void* take(size_t bytes, size_t* got) {
+    auto it = cache.lower_bound(bytes);
+    if (it == cache.end() || it->first > 2 * bytes) return nullptr;
+    void* p = it->second;
+    *got = it->first;
+    cached -= it->first;
+    cache.erase(it);
+    return p;
+  }
+  void give(void* p, size_t bytes) {
+    if (cache_cap == 0) {
+      size_t f = 0, t = 0;
+      cache_cap = cudaMemGetInfo(&f, &t) == cudaSuccess ? t / 4 : 1;
+    }
+    if (cached + bytes > cache_cap) {
+      cudaFree(p);
+      used -= bytes;
+      return;
+    }
+    cache.emplace(bytes, p);
+    cached += bytes;
+  }
+  void note_live() {
+    if (live() > peak_live) peak_live = live();
+  }
+  // Returns every cached block to the driver.
+  void flush() {
+    for (auto& kv : cache) cudaFree(kv.second);
+    used -= cached;
+    cached = 0;
+    cache.clear();
+  }
+  // Bytes held by live blocks.
+  size_t live() const { return used - cached; }
 };
 
 template <class T>
@@ -54,8 +108,8 @@ struct DevBuf {
 
   void release() {
     if (p) {
-      cudaFree(p);
-      if (mt) mt->used -= cap * sizeof(T);
+      if (mt) mt->give(p, cap * sizeof(T));  // kept for the context's next request
+      else cudaFree(p);
     }
     p = nullptr;
     n = cap = 0;
@@ -68,10 +122,25 @@ struct DevBuf {
     if (c < k) c = k;
     if (c == 0) c = 1;
     const size_t bytes = c * sizeof(T);
-    if (mt && mt->budget && mt->used + bytes > mt->budget)
-      throw OomError("device budget exceeded (" + std::to_string(mt->used + bytes) + " > " +
-                     std::to_string(mt->budget) + " bytes)");
+    if (mt) {
+      size_t got = 0;
+      if (void* b = mt->take(bytes, &got)) {
+        p = static_cast<T*>(b);
+        cap = got / sizeof(T);
+        mt->note_live();
+        return;
+      }
+      if (mt->budget && mt->used + bytes > mt->budget) mt->flush();
+      if (mt->budget && mt->used + bytes > mt->budget)
+        throw OomError("device budget exceeded (" + std::to_string(mt->used + bytes) + " > " +
+                       std::to_string(mt->budget) + " bytes)");
+    }
     cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess && mt && mt->cached) {  // the cache first, then once more
+      cudaGetLastError();
+      mt->flush();
+      e = cudaMalloc(&p, bytes);
+    }
     if (e != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
@@ -81,6 +150,7 @@ struct DevBuf {
     if (mt) {
       mt->used += bytes;
       if (mt->used > mt->peak) mt->peak = mt->used;
+      mt->note_live();
     }
   }
   void resize(size_t k, double slack = 1.0) {

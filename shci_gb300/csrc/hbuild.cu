@@ -422,10 +422,11 @@ static size_t store_room(shci_ctx* c) {
   // the store's current allocation is reused or freed before the new one is made
   const auto& H = c->H;
   size_t held = H.col.cap * 4 + H.val64.cap * 8 + H.val32.cap * 4 + H.res32.cap * 4;
-  size_t room = free_b + held;
+  size_t room = free_b + c->mem.cached + held;  // cached blocks return to the driver on demand
+  const size_t live = c->mem.live();
   if (c->mem.budget)
-    room = std::min(room, c->mem.budget > c->mem.used - held ? c->mem.budget - (c->mem.used - held)
-                                                             : (size_t)0);
+    room = std::min(room, c->mem.budget > live - held ? c->mem.budget - (live - held)
+                                                      : (size_t)0);
   return room;
 }
 

@@ -328,8 +328,9 @@ bool join_prepare(shci_ctx* c) {
   // memory: keys + sort ping-pong (16 B), entry values + ping-pong (8 B), then span (8 B)
   size_t free_b = 0, total_b = 0;
   SHCI_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  size_t avail = free_b;
-  if (c->mem.budget) avail = std::min(avail, c->mem.budget > c->mem.used ? c->mem.budget - c->mem.used : 0);
+  size_t avail = free_b + c->mem.cached;  // cached blocks return to the driver on demand
+  const size_t live = c->mem.live();
+  if (c->mem.budget) avail = std::min(avail, c->mem.budget > live ? c->mem.budget - live : 0);
   if (static_cast<double>(m) * 26.0 > 0.85 * static_cast<double>(avail)) return false;
   J.K = static_cast<uint32_t>(K);
   J.n_up = n_up;

@@ -866,6 +866,7 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
     for (uint64_t v : hc) tot += v;
     size_t free_b = 0, total_b = 0;
     SHCI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    free_b += c->mem.cached;  // cached blocks return to the driver on demand
     const double per = 48.0 * (MODE == kDtm ? 1.0 : 1.3);
     n_batches = static_cast<size_t>(std::ceil(tot * per / (0.4 * free_b)));
     if (n_batches < 1) n_batches = 1;
