@@ -5,9 +5,9 @@
 // concurrently: W worker threads, each owning one context (its own stream and device
 // buffers), pull instances from a shared queue ordered largest first, so the kernels and
 // copies of different instances overlap.  The worker count is chosen by a small autotuner
-// when the caller passes n_workers <= 0: it processes successive slices of the queue with
-// W = 4, 8, 16, 32, 64 workers, measures instances per second on each, and finishes the
-// queue with the fastest W.  An instance's results do not depend on W.
+// when the caller passes n_workers <= 0: on a long queue it solves interleaved slices with a
+// quarter, a half and one worker per host CPU, measures instances per second on each, and
+// finishes the queue with the fastest; a short queue takes one worker per two host CPUs.  An instance's results do not depend on W.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -91,15 +91,17 @@ int fcidump_norb(const char* path) {
   return n;
 }
 
-// Runs items order[begin, end) with W workers; returns elapsed seconds.
-double run_slice(int device, const shci_batch_item* items, const std::vector<size_t>& order,
-                 size_t begin, size_t end, int W, shci_batch_result* out,
-                 std::atomic<int>& create_fail) {
-  std::atomic<size_t> next{begin};
+// Runs the items idx[...] with W workers; returns elapsed seconds.  Each worker's host-side
+// loops (integral loading, PT2 sampling) use its share of the host CPUs.
+double run_slice(int device, const shci_batch_item* items, const std::vector<size_t>& idx, int W,
+                 shci_batch_result* out, std::atomic<int>& create_fail) {
+  std::atomic<size_t> next{0};
   const double t0 = now_s();
+  const unsigned share = std::max(1u, shci::host_threads() / static_cast<unsigned>(W));
   std::vector<std::thread> th;
   for (int w = 0; w < W; w++)
     th.emplace_back([&]() {
+      shci::set_host_threads(share);
       shci_ctx* c = nullptr;
       if (shci_create(&c, device, 0) != SHCI_OK) {
         create_fail++;
@@ -109,7 +111,7 @@ double run_slice(int device, const shci_batch_item* items, const std::vector<siz
       // share of a quarter of the device (a worker's failing allocation returns only its own)
       size_t f = 0, t = 0;
       if (cudaMemGetInfo(&f, &t) == cudaSuccess) c->mem.cache_cap = std::max<size_t>(t / 4 / W, 1);
-      for (size_t k; (k = next.fetch_add(1)) < end;) solve_one(c, items[order[k]], out[order[k]]);
+      for (size_t k; (k = next.fetch_add(1)) < idx.size();) solve_one(c, items[idx[k]], out[idx[k]]);
       shci_destroy(c);
     });
   for (auto& t : th) t.join();
@@ -134,23 +136,42 @@ extern "C" shci_status shci_batch_solve(int device, const shci_batch_item* items
   int W = n_workers;
   size_t done = 0;
   if (W <= 0) {
-    // autotune on successive slices of the queue
-    const int cand[] = {4, 8, 16, 32, 64};
-    double best_rate = 0.0;
-    W = 4;
-    for (int w : cand) {
-      const size_t len = std::min<size_t>(n - done, static_cast<size_t>(2 * w));
-      if (len < static_cast<size_t>(w)) break;
-      const double t = run_slice(device, items, order, done, done + len, w, out, create_fail);
-      const double rate = len / std::max(t, 1e-9);
-      done += len;
-      if (rate > best_rate) {
-        best_rate = rate;
-        W = w;
+    // Each solve is host-latency bound (launches, synchronisations, host-side sampling), so
+    // the useful worker count is set by the host CPUs; beyond about one worker per two CPUs
+    // the workers' launches and synchronisations contend in the driver and the rate falls.
+    // Candidates: a quarter, a half and one worker per CPU.  The first n_cand * L items of
+    // the queue are dealt round robin to the candidates, so each candidate's slice spans the
+    // same range of sizes; the one with the highest rate solves the rest.  A slice's time is
+    // set by its largest instances as much as by the rate, so the tuner runs only on queues
+    // at least four times as long as the slices; shorter ones take a worker per two CPUs.
+    const int cpus = static_cast<int>(shci::host_threads());
+    std::vector<int> cand;
+    for (int w : {cpus / 4, cpus / 2, cpus}) {
+      w = std::min(std::max(w, 1), 64);
+      if (cand.empty() || cand.back() != w) cand.push_back(w);
+    }
+    const size_t nc = cand.size();
+    const size_t L = 2 * static_cast<size_t>(cand.back());
+    W = std::min(std::max(cpus / 2, 1), 64);
+    if (nc > 1 && 4 * nc * L <= n) {
+      double best_rate = 0.0;
+      for (size_t j = 0; j < nc; j++) {
+        std::vector<size_t> idx;
+        for (size_t k = j; k < nc * L; k += nc) idx.push_back(order[k]);
+        const double t = run_slice(device, items, idx, cand[j], out, create_fail);
+        const double rate = idx.size() / std::max(t, 1e-9);
+        if (rate > best_rate) {
+          best_rate = rate;
+          W = cand[j];
+        }
       }
+      done = nc * L;
     }
   }
-  if (done < n) run_slice(device, items, order, done, n, W, out, create_fail);
+  if (done < n) {
+    std::vector<size_t> idx(order.begin() + done, order.end());
+    run_slice(device, items, idx, W, out, create_fail);
+  }
   if (workers_used) *workers_used = W;
   if (create_fail.load() > 0) return SHCI_ERR_CUDA;
   for (size_t k = 0; k < n; k++)

@@ -18,7 +18,28 @@
 #include <atomic>
 #include <thread>
 
+#include <sched.h>
+
 namespace shci {
+
+namespace {
+thread_local unsigned t_host_threads = 0;
+}  // namespace
+
+unsigned host_threads() {
+  if (t_host_threads) return t_host_threads;
+  static const unsigned usable = []() {
+    // the CPUs this process may run on (a container's CPU set), else the machine's count
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0 && CPU_COUNT(&set) > 0)
+      return static_cast<unsigned>(CPU_COUNT(&set));
+    return std::max(1u, std::thread::hardware_concurrency());
+  }();
+  return usable;
+}
+
+void set_host_threads(unsigned n) { t_host_threads = n; }
 
 namespace {
 
@@ -383,7 +404,11 @@ double singles_elem(const HostIntegrals& I, unsigned i, unsigned j) {
 
 template <class F>
 void parallel_for(unsigned n, F f) {
-  unsigned nt = std::max(1u, std::min(n, std::thread::hardware_concurrency()));
+  unsigned nt = std::max(1u, std::min(n, host_threads()));
+  if (nt == 1) {
+    for (unsigned i = 0; i < n; i++) f(i);
+    return;
+  }
   std::vector<std::thread> th;
   std::atomic<unsigned> next{0};
   for (unsigned t = 0; t < nt; t++)

@@ -67,6 +67,11 @@ void build_queues(const HostIntegrals& I, HostQueues& Q);
 
 double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn);
 
+// Host threads a host-side loop of the calling thread may use: the machine's hardware threads
+// unless the calling thread set a cap (the batch runner's workers each take their share).
+unsigned host_threads();
+void set_host_threads(unsigned n);  // 0 = no cap
+
 inline size_t combine2(size_t a, size_t b) {
   return a > b ? (a * (a + 1)) / 2 + b : (b * (b + 1)) / 2 + a;
 }

@@ -17,6 +17,7 @@
 // iteration index stored above the orbital bits of the key, and the reference's stopping
 // rules are then applied iteration by iteration.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1147,9 +1148,12 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
     }
     return d;
   };
+  // one helper thread draws ahead unless the calling thread may use only one host thread
+  const unsigned n_host = host_threads();
+  const auto draw_policy = n_host > 1 ? std::launch::async : std::launch::deferred;
   std::future<PassDraws> next_draws;
   if (max_iterations > 0)
-    next_draws = std::async(std::launch::async, draw_pass,
+    next_draws = std::async(draw_policy, draw_pass,
                             static_cast<uint32_t>(std::min<size_t>(kFirstChunk, max_iterations)));
   std::vector<double> aprob;
   std::vector<size_t> alias;
@@ -1184,7 +1188,7 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
       const size_t it_next = iteration + n_it;
       if (it_next < max_iterations)
         next_draws = std::async(
-            std::launch::async, draw_pass,
+            draw_policy, draw_pass,
             static_cast<uint32_t>(std::min<size_t>(kNextChunk, max_iterations - it_next)));
       const auto& r1s = draws.r1;
       const auto& r2s = draws.r2;
@@ -1218,9 +1222,13 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
       };
       {
         HostScope hs_look(c->prof, "pt2_host_sample_lookup");
+        std::atomic<uint32_t> next_it{0};
+        auto run = [&]() {
+          for (uint32_t it; (it = next_it.fetch_add(1)) < n_it;) sample_one(it);
+        };
         std::vector<std::thread> th;
-        for (uint32_t it = 1; it < n_it; it++) th.emplace_back(sample_one, it);
-        sample_one(0);
+        for (uint32_t t = 1; t < std::min<uint32_t>(n_it, n_host); t++) th.emplace_back(run);
+        run();
         for (auto& t : th) t.join();
       }
       HostScope hs_group(c->prof, "pt2_host_sample_group");
