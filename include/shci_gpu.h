@@ -72,6 +72,19 @@ shci_status shci_load_fcidump(shci_ctx* ctx, const char* path, unsigned n_up, un
                               const char* point_group, int reorder, const unsigned* occs_up,
                               const unsigned* occs_dn);
 
+/* Integrals cache (Integrals::save_to_cache / load_from_cache, src/chem/integrals.cc:17-35,
+ * 424-440): the prepared integrals (reordered h1, g2, orbital symmetries, orbital order, HF
+ * det, E_core) in this build's own little-endian layout (magic "SHCIGIC1"; the reference's hps
+ * byte format is not available).  Save writes `path` unless a file not in this layout is there
+ * (*written = 0: it is not overwritten).  Load reads `path` when it is in this layout
+ * (*loaded = 1) and leaves the context unchanged otherwise (*loaded = 0: missing or foreign
+ * file); the point group is passed again, as the reference takes it from the config.  A file
+ * in this layout that is truncated or inconsistent gives SHCI_ERR_IO, one written for other
+ * n_up / n_dn gives SHCI_ERR_ARG. */
+shci_status shci_save_integrals_cache(shci_ctx* ctx, const char* path, int* written);
+shci_status shci_load_integrals_cache(shci_ctx* ctx, const char* path, unsigned n_up,
+                                      unsigned n_dn, const char* point_group, int* loaded);
+
 /* Set already-prepared integrals: h1[n*n] (h_pq), g2[n^4] (chemists' (pq|rs) at
  * ((p*n+q)*n+r)*n+s), orb_sym[n] (irreps 1..8, or linear-group labels; NULL = all 1).  The
  * HF det is given.  Linear groups screen g2 by Lz as shci_load_fcidump does. */

@@ -48,6 +48,8 @@ def load():
         "shci_destroy": [vp],
         "shci_load_fcidump": [vp, ctypes.c_char_p, u, u, ctypes.c_char_p, i, vp, vp],
         "shci_set_integrals": [vp, i, u, u, d, _f64p, _f64p, vp, ctypes.c_char_p, u64, u64],
+        "shci_save_integrals_cache": [vp, ctypes.c_char_p, P(i)],
+        "shci_load_integrals_cache": [vp, ctypes.c_char_p, u, u, ctypes.c_char_p, P(i)],
         "shci_get_integrals": [vp, P(i), P(d), vp, vp, vp, vp],
         "shci_get_hf": [vp, P(u64), P(u64), P(d)],
         "shci_build_queues": [vp, _f64p],
@@ -204,6 +206,25 @@ class Context:
         n = ctypes.c_int()
         self._ck(self.L.shci_get_integrals(self.h, ctypes.byref(n), None, None, None, None, None))
         self.n_orbs = n.value
+
+    def save_integrals_cache(self, path):
+        """Writes the integrals cache; False when a file of another format is there."""
+        w = ctypes.c_int()
+        self._ck(self.L.shci_save_integrals_cache(self.h, str(path).encode(), ctypes.byref(w)))
+        return bool(w.value)
+
+    def load_integrals_cache(self, path, n_up, n_dn, point_group="C1"):
+        """Loads the integrals cache; False (context unchanged) when missing or foreign."""
+        ok = ctypes.c_int()
+        self._ck(self.L.shci_load_integrals_cache(self.h, str(path).encode(), n_up, n_dn,
+                                                  point_group.encode(), ctypes.byref(ok)))
+        if ok.value:
+            self.n_up, self.n_dn = n_up, n_dn
+            n = ctypes.c_int()
+            self._ck(self.L.shci_get_integrals(self.h, ctypes.byref(n), None, None, None, None,
+                                               None))
+            self.n_orbs = n.value
+        return bool(ok.value)
 
     def set_integrals(self, h1, g2, n_up, n_dn, hf_up, hf_dn, e_core=0.0, orb_sym=None,
                       point_group="C1"):

@@ -278,9 +278,27 @@ int main(int, char* argv[]) {
   shci_ctx* c = nullptr;
   if (shci_create(&c, device, 0) != SHCI_OK) die("cannot create a context on the GPU");
   std::vector<unsigned> ou(occ_u.begin(), occ_u.end()), od(occ_d.begin(), occ_d.end());
-  ck(c, shci_load_fcidump(c, "FCIDUMP", n_up, n_dn, pg.c_str(), reorder,
-                          ou.empty() ? nullptr : ou.data(), od.empty() ? nullptr : od.data()),
-     "load FCIDUMP");
+  // Integrals::load (integrals.cc:17-35): the cache when asked for and present, else FCIDUMP,
+  // after which the cache is written
+  const char* cache = "integrals_cache.dat";
+  int from_cache = 0;
+  if (cfg_b("load_integrals_cache", false))
+    ck(c, shci_load_integrals_cache(c, cache, n_up, n_dn, pg.c_str(), &from_cache),
+       "integrals cache");
+  if (from_cache) {
+    std::printf("Loaded FCIDUMP cache from: %s\n", cache);
+  } else {
+    ck(c, shci_load_fcidump(c, "FCIDUMP", n_up, n_dn, pg.c_str(), reorder,
+                            ou.empty() ? nullptr : ou.data(), od.empty() ? nullptr : od.data()),
+       "load FCIDUMP");
+    int written = 0;
+    ck(c, shci_save_integrals_cache(c, cache, &written), "integrals cache");
+    if (written)
+      std::printf("FCIDUMP cache saved to: %s\n", cache);
+    else
+      std::printf("Note: %s is not in this build's format; it is neither read nor overwritten.\n",
+                  cache);
+  }
   double e_hf = 0.0;
   uint64_t hf_up = 0, hf_dn = 0;
   ck(c, shci_get_hf(c, &hf_up, &hf_dn, &e_hf), "HF det");

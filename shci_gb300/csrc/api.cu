@@ -203,6 +203,33 @@ shci_status shci_load_fcidump(shci_ctx* c, const char* path, unsigned n_up, unsi
   return st;
 }
 
+shci_status shci_save_integrals_cache(shci_ctx* c, const char* path, int* written) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!path) throw ArgError("null path");
+    need_integrals(c);
+    const CacheStatus st = save_integrals_cache(c->I, path);
+    if (written) *written = st == kCacheOk ? 1 : 0;
+  });
+}
+
+shci_status shci_load_integrals_cache(shci_ctx* c, const char* path, unsigned n_up, unsigned n_dn,
+                                      const char* point_group, int* loaded) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (!path) throw ArgError("null path");
+    if (loaded) *loaded = 0;
+    HostIntegrals I;
+    if (load_integrals_cache(I, path, point_group ? point_group : "C1") != kCacheOk) return;
+    if (I.n_up != n_up || I.n_dn != n_dn)
+      throw ArgError(std::string(path) + " holds integrals for n_up = " +
+                     std::to_string(I.n_up) + ", n_dn = " + std::to_string(I.n_dn));
+    c->I = std::move(I);
+    after_integrals(c);
+    if (loaded) *loaded = 1;
+  });
+}
+
 shci_status shci_set_integrals(shci_ctx* c, int n_orbs, unsigned n_up, unsigned n_dn,
                                double e_core, const double* h1, const double* g2,
                                const unsigned* orb_sym, const char* point_group, uint64_t hf_up,

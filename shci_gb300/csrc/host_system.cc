@@ -337,6 +337,92 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
   screen_linear(I);
 }
 
+namespace {
+static_assert(sizeof(unsigned) == 4, "cache layout stores u32 fields");
+constexpr char kCacheMagic[8] = {'S', 'H', 'C', 'I', 'G', 'I', 'C', '1'};
+
+CacheStatus probe_cache(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return kCacheMissing;
+  char m[8];
+  const bool ours = std::fread(m, 1, 8, f) == 8 && std::memcmp(m, kCacheMagic, 8) == 0;
+  std::fclose(f);
+  return ours ? kCacheOk : kCacheForeign;
+}
+}  // namespace
+
+CacheStatus load_integrals_cache(HostIntegrals& I, const std::string& path,
+                                 const std::string& point_group) {
+  const CacheStatus st = probe_cache(path);
+  if (st != kCacheOk) return st;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return kCacheMissing;
+  bool ok = true;
+  auto rd = [&](void* p, size_t n) { ok = ok && std::fread(p, 1, n, f) == n; };
+  char m[8];
+  uint32_t hdr[3] = {0, 0, 0};
+  rd(m, 8);
+  rd(hdr, sizeof(hdr));
+  HostIntegrals J;
+  const size_t n = hdr[0];
+  ok = ok && n >= 1 && n <= 64 && hdr[1] <= n && hdr[2] <= n;
+  if (ok) {
+    J.n = hdr[0];
+    J.n_up = hdr[1];
+    J.n_dn = hdr[2];
+    rd(&J.e_core, 8);
+    J.orb_sym.resize(n);
+    J.orb_order.resize(n);
+    rd(J.orb_sym.data(), 4 * n);
+    rd(J.orb_order.data(), 4 * n);
+    rd(&J.hf_up, 8);
+    rd(&J.hf_dn, 8);
+    J.h1.resize(n * n);
+    J.g2.resize(n * n * n * n);
+    rd(J.h1.data(), 8 * n * n);
+    rd(J.g2.data(), 8 * n * n * n * n);
+    char extra;
+    ok = ok && std::fread(&extra, 1, 1, f) == 0;  // nothing after g2
+  }
+  std::fclose(f);
+  if (ok) {
+    std::vector<bool> seen(n, false);
+    for (unsigned o : J.orb_order) {
+      ok = ok && o < n && !seen[o];
+      if (o < n) seen[o] = true;
+    }
+    ok = ok && __builtin_popcountll(J.hf_up) == (int)J.n_up &&
+         __builtin_popcountll(J.hf_dn) == (int)J.n_dn &&
+         (n == 64 || ((J.hf_up | J.hf_dn) >> n) == 0);
+  }
+  if (!ok) throw std::runtime_error(path + ": truncated or inconsistent integrals cache");
+  J.n_syms = point_group_order(point_group, &J.linear);
+  I = std::move(J);
+  return kCacheOk;
+}
+
+CacheStatus save_integrals_cache(const HostIntegrals& I, const std::string& path) {
+  if (probe_cache(path) == kCacheForeign) return kCacheForeign;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw std::runtime_error("cannot write " + path);
+  const size_t n = I.n;
+  bool ok = true;
+  auto wr = [&](const void* p, size_t k) { ok = ok && std::fwrite(p, 1, k, f) == k; };
+  const uint32_t hdr[3] = {I.n, I.n_up, I.n_dn};
+  wr(kCacheMagic, 8);
+  wr(hdr, sizeof(hdr));
+  wr(&I.e_core, 8);
+  wr(I.orb_sym.data(), 4 * n);
+  wr(I.orb_order.data(), 4 * n);
+  wr(&I.hf_up, 8);
+  wr(&I.hf_dn, 8);
+  wr(I.h1.data(), 8 * n * n);
+  wr(I.g2.data(), 8 * n * n * n * n);
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) throw std::runtime_error("cannot write " + path);
+  return kCacheOk;
+}
+
 double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn) {
   double ob = 0.0;
   for (uint64_t m = up; m; m &= m - 1) ob += I.h(__builtin_ctzll(m), __builtin_ctzll(m));

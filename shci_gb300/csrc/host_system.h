@@ -34,6 +34,29 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
                   const std::string& point_group, int reorder, const unsigned* occs_up,
                   const unsigned* occs_dn);
 
+// Integrals cache: Integrals::save_to_cache / load_from_cache (src/chem/integrals.cc:17-35,
+// 424-440) keep the prepared integrals (after orbital reordering) in "integrals_cache.dat" so
+// that a later run skips FCIDUMP parsing.  The reference writes its Integrals fields with hps,
+// an un-vendored library whose byte format is not available; this build stores the same fields
+// in its own little-endian layout:
+//
+//   8 bytes   magic "SHCIGIC1"
+//   u32       n_orbs, n_up, n_dn
+//   f64       energy_core
+//   u32       orb_sym[n_orbs]     (irreps after reordering; linear groups: Adam's labels)
+//   u32       orb_order[n_orbs]   (new index -> FCIDUMP index)
+//   u64       det_hf up, dn
+//   f64       h1[n*n], g2[n^4]    (dense, reordered basis; g2 at ((p*n+q)*n+r)*n+s)
+//
+// The point group is not stored (the reference's cache does not hold it either): the caller
+// passes it again.  Load returns kCacheMissing or kCacheForeign (a file not in this layout,
+// for instance one the reference wrote) without touching I; save does not overwrite a foreign
+// file.  A file in this layout that is truncated or inconsistent throws std::runtime_error.
+enum CacheStatus { kCacheMissing = 0, kCacheOk = 1, kCacheForeign = 2 };
+CacheStatus load_integrals_cache(HostIntegrals& I, const std::string& path,
+                                 const std::string& point_group);
+CacheStatus save_integrals_cache(const HostIntegrals& I, const std::string& path);
+
 // Number of irreps of a point group name as ProductTable::get_n_syms counts them
 // (src/chem/product_table.cc:37-47; 128 for the linear groups); *linear tells whether the name
 // is one of the linear groups ("Dooh", "Dih", "Coov", "Civ": ChemSystem::get_point_group,

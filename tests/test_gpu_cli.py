@@ -174,3 +174,73 @@ def test_cli_two_states(tmp_path):
     c.run_variation([2e-4], [2e-3, 1e-3, 5e-4], 5e-5)
     assert np.max(np.abs(c.state_energies() - [e0, e1])) < 1e-12
     c.close()
+
+
+def test_integrals_cache_roundtrip(tmp_path):
+    """Integrals::save_to_cache / load_from_cache (integrals.cc:17-35, 424-440): a context
+    loaded from the cache holds the same prepared integrals (reordered tables, symmetries,
+    orbital order, HF det) and gives the same variational energies as one that parsed the
+    FCIDUMP; foreign files are neither read nor overwritten; a damaged cache is an IO error."""
+    import numpy as np
+    import shci_gb300 as S
+    path = tmp_path / "integrals_cache.dat"
+    a = S.Context()
+    a.load_fcidump(C_ATOM, 4, 2, "d2h")
+    assert a.save_integrals_cache(path)
+    b = S.Context()
+    assert b.load_integrals_cache(path, 4, 2, "d2h")
+    for x, y in zip(a.integrals(), b.integrals()):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
+    assert a.hf() == b.hf()
+    ea = a.run_variation([2e-4], [2e-3, 1e-3], 5e-5, precision=S.PREC_FP64)
+    eb = b.run_variation([2e-4], [2e-3, 1e-3], 5e-5, precision=S.PREC_FP64)
+    # (FP64 H*v adds with atomics: equal up to the order of the additions)
+    assert np.max(np.abs(ea - eb)) < 1e-12
+    ua, da, _ = a.dets()
+    ub, db, _ = b.dets()
+    assert np.array_equal(ua, ub) and np.array_equal(da, db)
+    # written for other electron counts
+    with pytest.raises(S.ShciError):
+        S.Context().load_integrals_cache(path, 3, 3, "d2h")
+    # truncated file in this layout
+    bad = tmp_path / "bad.dat"
+    bad.write_bytes(path.read_bytes()[:1000])
+    with pytest.raises(S.ShciError):
+        S.Context().load_integrals_cache(bad, 4, 2, "d2h")
+    # a file of another format (the reference's hps dump, say)
+    foreign = tmp_path / "foreign.dat"
+    foreign.write_bytes(b"\x01\x02not this layout" * 10)
+    c = S.Context()
+    assert not c.load_integrals_cache(foreign, 4, 2, "d2h")
+    c.load_fcidump(C_ATOM, 4, 2, "d2h")
+    assert not c.save_integrals_cache(foreign)
+    assert foreign.read_bytes() == b"\x01\x02not this layout" * 10
+    assert not c.load_integrals_cache(tmp_path / "missing.dat", 4, 2, "d2h")
+    for x in (a, b, c):
+        x.close()
+
+
+def test_cli_integrals_cache(tmp_path):
+    """The driver writes integrals_cache.dat after reading FCIDUMP and, with
+    "load_integrals_cache": true, reads it instead of FCIDUMP (here an empty file)."""
+    from shci_gb300 import build
+    exe = build.build_cli()
+    shutil.copyfile(C_ATOM, tmp_path / "FCIDUMP")
+    cfg = {"system": "chem", "n_up": 4, "n_dn": 2, "eps_vars": [2e-4],
+           "eps_vars_schedule": [2e-3, 1e-3], "chem": {"point_group": "d2h"}, "var_only": True,
+           "gpu": {"precision": "fp64"}}
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "FCIDUMP cache saved to: integrals_cache.dat" in r.stdout
+    e1 = json.load(open(tmp_path / "result.json"))["energy_var"]["2.00e-04"]
+    (tmp_path / "FCIDUMP").write_text("")
+    for f in tmp_path.glob("wf_eps1_*.dat"):
+        f.unlink()
+    (tmp_path / "result.json").unlink()
+    cfg["load_integrals_cache"] = True
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "Loaded FCIDUMP cache from: integrals_cache.dat" in r.stdout
+    assert abs(json.load(open(tmp_path / "result.json"))["energy_var"]["2.00e-04"] - e1) < 1e-12
