@@ -138,7 +138,7 @@ extern "C" shci_status shci_batch_solve(int device, const shci_batch_item* items
   if (W <= 0) {
     // Each solve is host-latency bound (launches, synchronisations, host-side sampling), so
     // the useful worker count is set by the host CPUs; beyond about one worker per two CPUs
-    // the workers' launches and synchronisations contend in the driver and the rate falls.
+    // the workers contend for the GPU and the driver and the rate falls.
     // Candidates: a quarter, a half and one worker per CPU.  The first n_cand * L items of
     // the queue are dealt round robin to the candidates, so each candidate's slice spans the
     // same range of sizes; the one with the highest rate solves the rest.  A slice's time is
