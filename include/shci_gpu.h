@@ -272,6 +272,42 @@ shci_status shci_select(shci_ctx* ctx, double eps_var, int var_sd, size_t* n_new
  * (factor 0.2).  Applies to shci_select and shci_run_variation of this context. */
 shci_status shci_set_second_rejection(shci_ctx* ctx, int enable, double factor);
 
+/* Double excitations on or off (config "has_double_excitation", default on;
+ * chem_system.cc:29, 345; hamiltonian.h:97-104, 487).  Off: find_connected_dets yields single
+ * excitations only (selection, PT2, shci_find_connected_dets) and returns eps_min (what the
+ * singles' second rejection dropped is not kept), and the Hamiltonian leaves out the
+ * opposite-spin doubles (same-spin doubles stay; with time_sym every double stays). */
+shci_status shci_set_has_double_excitation(shci_ctx* ctx, int on);
+
+/* Active space (config "chem/active_space" with "chem/irrep_active_space",
+ * integrals.cc:295-326, chem_system.cc:327-329, 383-387): irrep_active_space[k] orbitals of
+ * irrep k + 1, the lowest in the current orbital order, are active; find_connected_dets skips
+ * excitations whose target orbital lies above the highest active orbital of its irrep (after
+ * the second-rejection test, before the occupancy tests).  n = 0 turns it off; n must cover
+ * every irrep of the orbitals (SHCI_ERR_ARG otherwise).  The reference requires
+ * "reorder_orbs": false with it (the orbital order is the FCIDUMP's).  Reset by loading
+ * integrals. */
+shci_status shci_set_active_space(shci_ctx* ctx, const unsigned* irrep_active_space, size_t n);
+/* Bit r set: orbital r may not be an excitation target. */
+shci_status shci_get_inactive_orbitals(shci_ctx* ctx, uint64_t* mask);
+
+/* Selection of shci_run_variation starts the HF det with eps_min = 0 (config "var_sd",
+ * default "get_pair_contrib", solver.h:423-424, 446).  Off by default. */
+shci_status shci_set_var_sd(shci_ctx* ctx, int on);
+
+/* HF det options of the next shci_load_fcidump (Integrals::generate_det_hf,
+ * integrals.cc:155-226): without occs_up / occs_dn, n_irreps > 0 fills irreps[k] (orbital
+ * symmetry labels as in ORBSYM, linear groups in the reference's labels) with
+ * irrep_occs_up[k] / irrep_occs_dn[k] electrons in orbital order (config "chem/irreps",
+ * "chem/irrep_occs_up", "chem/irrep_occs_dn"; such an HF det counts as explicit, so the
+ * orbitals are not reordered by default); otherwise the lowest orbitals, with the beta
+ * electrons placed above the alpha ones when allow_doubly_occupy = 0 (config
+ * "allow_doubly_occupy_hf", default 1).  An impossible filling gives SHCI_ERR_IO from the
+ * load. */
+shci_status shci_set_hf_options(shci_ctx* ctx, int allow_doubly_occupy, const unsigned* irreps,
+                                const unsigned* irrep_occs_up, const unsigned* irrep_occs_dn,
+                                size_t n_irreps);
+
 /* eps_tried_prev memo (length = n dets at the last selection). */
 shci_status shci_get_eps_tried(shci_ctx* ctx, double* out, size_t cap);
 
@@ -384,6 +420,11 @@ shci_status shci_batch_solve(int device, const shci_batch_item* items, size_t n,
                              shci_batch_result* results, int* workers_used);
 
 /* ---- RDMs: the adjoint of E_var (RDM::get_1rdm / get_2rdm, src/chem/rdm.cc) ---------- */
+
+/* <S^2> of the first state of the context's wavefunction (ChemSystem::get_s2,
+ * chem_system.cc:745-798; config "s2", post_variation :627-634).  A time_sym wavefunction must
+ * be unpacked first (SHCI_ERR_ARG). */
+shci_status shci_get_s2(shci_ctx* ctx, double* s2);
 
 /* 1-RDM of the context's wavefunction: rdm1[p*n + r] = sum_ij c_i c_j <D_i| a+_r a_p |D_j>
  * summed over spin (rdm.cc:12-131), in the reordered orbital basis. */

@@ -73,6 +73,12 @@ def lib():
             "orc_set_n_states": (None, [vp, u]),
             "orc_set_time_sym": (None, [vp, i]),
             "orc_set_second_rejection": (None, [vp, i]),
+            "orc_create_hf": (vp, [ctypes.c_char_p, u, u, ctypes.c_char_p, i, i, vp, vp, vp, u,
+                                   ctypes.c_char_p, sz]),
+            "orc_set_has_double_excitation": (None, [vp, i]),
+            "orc_set_active_space": (None, [vp, vp, u]),
+            "orc_get_s2": (d, [vp]),
+            "orc_set_var_sd": (None, [vp, i]),
             "orc_unpack_time_sym": (None, [vp]),
             "orc_generalized_fock": (None, [vp, _f64p, _f64p, _f64p]),
             "orc_orbital_parameters": (sz, [vp, vp, vp, sz]),
@@ -133,7 +139,8 @@ class Oracle:
     """One SHCI system (integrals, queues, dets, Hamiltonian) in the CPU restatement."""
 
     def __init__(self, fcidump, n_up, n_dn, point_group="C1", reorder=-1, occs_up=None,
-                 occs_dn=None):
+                 occs_dn=None, allow_doubly_occupy=True, irreps=None, irrep_occs_up=None,
+                 irrep_occs_dn=None):
         L = lib()
         err = ctypes.create_string_buffer(512)
         self._keep = []
@@ -143,8 +150,17 @@ class Oracle:
             b = np.ascontiguousarray(occs_dn, dtype=np.uint32)
             self._keep += [a, b]
             ou, od = a.ctypes.data, b.ctypes.data
-        self.h = L.orc_create(str(fcidump).encode(), n_up, n_dn, point_group.encode(), reorder,
-                              ou, od, err, 512)
+        if occs_up is None and (irreps is not None or not allow_doubly_occupy):
+            ir = np.ascontiguousarray(irreps if irreps is not None else [], dtype=np.uint32)
+            iu = np.ascontiguousarray(irrep_occs_up if irreps is not None else [], np.uint32)
+            idn = np.ascontiguousarray(irrep_occs_dn if irreps is not None else [], np.uint32)
+            self._keep += [ir, iu, idn]
+            self.h = L.orc_create_hf(str(fcidump).encode(), n_up, n_dn, point_group.encode(),
+                                     reorder, int(allow_doubly_occupy), ir.ctypes.data,
+                                     iu.ctypes.data, idn.ctypes.data, len(ir), err, 512)
+        else:
+            self.h = L.orc_create(str(fcidump).encode(), n_up, n_dn, point_group.encode(),
+                                  reorder, ou, od, err, 512)
         if not self.h:
             raise RuntimeError("oracle: " + err.value.decode())
         self.L = L
@@ -282,6 +298,20 @@ class Oracle:
         nt = ctypes.c_size_t()
         conv = self.L.orc_davidson(self.h, c, tol, ctypes.byref(e), tr, 64, ctypes.byref(nt))
         return e.value, c, bool(conv), tr[: nt.value]
+
+    def set_has_double_excitation(self, on=True):
+        self.L.orc_set_has_double_excitation(self.h, int(on))
+
+    def set_active_space(self, irrep_active_space):
+        a = np.ascontiguousarray(irrep_active_space, dtype=np.uint32)
+        self._keep.append(a)
+        self.L.orc_set_active_space(self.h, a.ctypes.data if len(a) else None, len(a))
+
+    def s2(self):
+        return self.L.orc_get_s2(self.h)
+
+    def set_var_sd(self, on=True):
+        self.L.orc_set_var_sd(self.h, int(on))
 
     def select(self, eps_var, var_sd=False):
         return self.L.orc_select(self.h, eps_var, int(var_sd))

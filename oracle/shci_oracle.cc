@@ -278,6 +278,10 @@ static void fill_tables(Integrals& I, const std::vector<unsigned>& inv) {
 struct LoadOptions {
   int reorder = -1;  // -1: default (!explicit_orbs), 0/1 forced
   std::vector<unsigned> occs_up, occs_dn;
+  // integrals.cc:163-164, 179-185: "chem/irreps" with "chem/irrep_occs_up/dn", and
+  // "allow_doubly_occupy_hf"
+  std::vector<unsigned> irreps, irrep_occs_up, irrep_occs_dn;
+  bool allow_doubly_occupy = true;
 };
 
 // src/chem/integrals.cc:17-35, 155-226 (fill-lowest / explicit occs), 228-384 (reorder)
@@ -301,9 +305,38 @@ static void load_integrals(Integrals& I, const std::string& path, unsigned n_up,
     for (unsigned o : opt.occs_up) I.det_hf.up |= 1ull << o;
     for (unsigned o : opt.occs_dn) I.det_hf.dn |= 1ull << o;
     I.explicit_orbs = true;
-  } else {
+  } else if (opt.irreps.empty()) {
+    // fill lowest (:176-185)
     for (unsigned i = 0; i < n_up; i++) I.det_hf.up |= 1ull << i;
-    for (unsigned i = 0; i < n_dn; i++) I.det_hf.dn |= 1ull << i;
+    if (opt.allow_doubly_occupy) {
+      for (unsigned i = 0; i < n_dn; i++) I.det_hf.dn |= 1ull << i;
+    } else {
+      for (unsigned i = 0; i < n_dn; i++) I.det_hf.dn |= 1ull << (i + n_up);
+    }
+  } else {
+    // fill according to irreps (:186-215)
+    for (size_t i = 0; i < opt.irreps.size(); i++) {
+      const unsigned irrep = opt.irreps[i];
+      unsigned occ_up = opt.irrep_occs_up.at(i), occ_dn = opt.irrep_occs_dn.at(i);
+      for (unsigned j = 0; j < I.n_orbs; j++) {
+        if (I.orb_sym[j] != irrep) continue;
+        if (occ_up > 0) {
+          I.det_hf.up |= 1ull << j;
+          occ_up--;
+        } else {
+          I.det_hf.up &= ~(1ull << j);
+        }
+        if (occ_dn > 0) {
+          I.det_hf.dn |= 1ull << j;
+          occ_dn--;
+        } else {
+          I.det_hf.dn &= ~(1ull << j);
+        }
+        if (occ_up == 0 && occ_dn == 0 && j >= n_up && j >= n_dn) break;
+      }
+      if (occ_up > 0 || occ_dn > 0) throw std::runtime_error("unable to construct hf with given irrep");
+    }
+    I.explicit_orbs = true;
   }
   // get_orb_energies (:228-255), with the un-reordered tables
   const unsigned n = I.n_orbs;
@@ -427,6 +460,10 @@ struct System {
   double energy_hf_1b = 0.0;
   double second_rejection_factor = 0.2;
   bool has_double_excitation = true;
+  // "chem/active_space" (chem_system.cc:30, integrals.cc:295-326): the highest active orbital
+  // of each irrep; empty = no active space
+  bool enforce_active_space = false;
+  std::vector<int> highest_occ_orb_in_irrep;
 
   std::vector<Det> dets;
   std::vector<double> coefs;  // state 0
@@ -542,6 +579,43 @@ struct System {
 
   // src/base_system.h:108-123: every det with up < dn gets its reverse appended, both
   // coefficients divided by sqrt(2) (SQRT2_INV = src/util.h:60)
+  // <S^2> of a state: src/chem/chem_system.cc:745-798 (serial here, same terms)
+  double get_s2(const std::vector<double>& state_coefs) const {
+    std::unordered_map<Det, double, DetHasher> det2coef;
+    for (size_t i = 0; i < dets.size(); i++) det2coef[dets[i]] = state_coefs[i];
+    double s2 = 0.;
+    const double nu = n_up, nd = n_dn;
+    for (size_t i_det = 0; i_det < dets.size(); i_det++) {
+      const Det this_det = dets[i_det];
+      unsigned num_db_occ = 0;
+      for (unsigned o : occ(this_det.up))
+        if (this_det.dn >> o & 1) num_db_occ++;
+      double diag = 0.5 * nu - num_db_occ + 0.5 * nd;
+      diag += 0.25 * (std::pow(nu, 2) + std::pow(nd, 2)) - 0.5 * nu * nd;
+      diag *= std::pow(state_coefs[i_det], 2);
+      s2 += diag;
+      for (unsigned i_orb = 0; i_orb < n_orbs; i_orb++) {
+        if (!(this_det.dn >> i_orb & 1)) continue;
+        if (this_det.up >> i_orb & 1) continue;
+        for (unsigned j_orb = i_orb + 1; j_orb < n_orbs; j_orb++) {
+          if (!(this_det.up >> j_orb & 1)) continue;
+          if (this_det.dn >> j_orb & 1) continue;
+          Det new_det = this_det;
+          new_det.up &= ~(1ull << j_orb);
+          new_det.up |= 1ull << i_orb;
+          new_det.dn &= ~(1ull << i_orb);
+          new_det.dn |= 1ull << j_orb;
+          const auto it = det2coef.find(new_det);
+          if (it == det2coef.end()) continue;
+          const double perm_up = diff(this_det.up, new_det.up).perm;
+          const double perm_dn = diff(this_det.dn, new_det.dn).perm;
+          s2 += -2 * it->second * state_coefs[i_det] * perm_up * perm_dn;
+        }
+      }
+    }
+    return s2;
+  }
+
   void unpack_time_sym() {
     const size_t n_old = dets.size();
     for (size_t i = 0; i < n_old; i++) {
@@ -761,6 +835,9 @@ struct System {
               continue;
             }
           }
+          if (enforce_active_space) {
+            if (static_cast<int>(r) > highest_occ_orb_in_irrep[I.orb_sym[r] - 1]) continue;
+          }
           Det c = det;
           if (p_id < n_up) {
             if (det.up >> r & 1) continue;
@@ -811,6 +888,11 @@ struct System {
               max_rejection = std::max(max_rejection, H);
               continue;
             }
+          }
+          if (enforce_active_space) {
+            const unsigned rr = r % n, ss = s % n;
+            if (static_cast<int>(rr) > highest_occ_orb_in_irrep[I.orb_sym[rr] - 1]) continue;
+            if (static_cast<int>(ss) > highest_occ_orb_in_irrep[I.orb_sym[ss] - 1]) continue;
           }
           const bool occ_r = r < n ? (det.up >> r & 1) : (det.dn >> (r - n) & 1);
           if (occ_r) continue;
@@ -2158,6 +2240,29 @@ void* orc_create(const char* fcidump, unsigned n_up, unsigned n_dn, const char* 
   }
 }
 
+// orc_create with the HF det options of integrals.cc:163-215 (n_irreps = 0: none).
+void* orc_create_hf(const char* fcidump, unsigned n_up, unsigned n_dn, const char* point_group,
+                    int reorder, int allow_doubly_occupy, const unsigned* irreps,
+                    const unsigned* irrep_occs_up, const unsigned* irrep_occs_dn,
+                    unsigned n_irreps, char* err, size_t err_len) {
+  try {
+    auto* h = new OrcHandle();
+    LoadOptions opt;
+    opt.reorder = reorder;
+    opt.allow_doubly_occupy = allow_doubly_occupy != 0;
+    if (n_irreps) {
+      opt.irreps.assign(irreps, irreps + n_irreps);
+      opt.irrep_occs_up.assign(irrep_occs_up, irrep_occs_up + n_irreps);
+      opt.irrep_occs_dn.assign(irrep_occs_dn, irrep_occs_dn + n_irreps);
+    }
+    h->solver.sys.setup(fcidump, n_up, n_dn, point_group, opt);
+    return h;
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    return nullptr;
+  }
+}
+
 void orc_destroy(void* h) { delete static_cast<OrcHandle*>(h); }
 
 void orc_set_threads(int n) { omp_set_num_threads(n); }
@@ -2444,6 +2549,31 @@ void orc_run_all_variations(void* h, const double* eps_vars, size_t n_eps, const
 
 // Second rejection for single selection steps (orc_select): the flag and energy_hf_1b as
 // run_variation sets them (solver.h:426-428, chem_system.cc:812-823).
+void orc_set_has_double_excitation(void* h, int on) { S(h).sys.has_double_excitation = on != 0; }
+
+// "chem/active_space" with "chem/irrep_active_space" (integrals.cc:295-326): the lowest
+// irrep_active_space[k] orbitals of irrep k + 1 (in orbital order) are active.  n = 0: off.
+void orc_set_active_space(void* h, const unsigned* irrep_active_space, unsigned n) {
+  auto& sys = S(h).sys;
+  sys.enforce_active_space = n > 0;
+  sys.highest_occ_orb_in_irrep.clear();
+  if (!n) return;
+  const unsigned n_irreps = *std::max_element(sys.I.orb_sym.begin(), sys.I.orb_sym.end());
+  std::vector<std::vector<unsigned>> active(n_irreps);
+  for (unsigned i = 0; i < sys.n_orbs; i++) {
+    const unsigned k = sys.I.orb_sym[i] - 1;
+    if (k < n && active[k].size() < irrep_active_space[k]) active[k].push_back(i);
+  }
+  sys.highest_occ_orb_in_irrep.assign(n_irreps, -1);
+  for (unsigned k = 0; k < n_irreps; k++)
+    if (!active[k].empty()) sys.highest_occ_orb_in_irrep[k] = static_cast<int>(active[k].back());
+}
+
+double orc_get_s2(void* h) { return S(h).sys.get_s2(S(h).sys.coefs); }
+
+// "var_sd" for whole variational runs (solver.h:424, 446)
+void orc_set_var_sd(void* h, int on) { S(h).var_sd = on != 0; }
+
 void orc_set_second_rejection(void* h, int on) {
   auto& s = S(h);
   s.second_rejection = on != 0;

@@ -71,6 +71,12 @@ def load():
         "shci_select": [vp, d, i, P(sz)],
         "shci_get_eps_tried": [vp, _f64p, sz],
         "shci_set_second_rejection": [vp, i, d],
+        "shci_set_has_double_excitation": [vp, i],
+        "shci_set_active_space": [vp, vp, sz],
+        "shci_get_inactive_orbitals": [vp, P(u64)],
+        "shci_set_var_sd": [vp, i],
+        "shci_set_hf_options": [vp, i, vp, vp, vp, sz],
+        "shci_get_s2": [vp, P(d)],
         "shci_set_n_states": [vp, u],
         "shci_set_time_sym": [vp, i],
         "shci_unpack_time_sym": [vp],
@@ -471,6 +477,38 @@ class Context:
 
     def set_second_rejection(self, enable=True, factor=0.2):
         self._ck(self.L.shci_set_second_rejection(self.h, int(enable), factor))
+
+    def set_has_double_excitation(self, on=True):
+        self._ck(self.L.shci_set_has_double_excitation(self.h, int(on)))
+
+    def set_active_space(self, irrep_active_space):
+        a = np.ascontiguousarray(irrep_active_space, np.uint32)
+        self._ck(self.L.shci_set_active_space(self.h, a.ctypes.data if len(a) else None, len(a)))
+
+    def inactive_orbitals(self):
+        m = ctypes.c_uint64()
+        self._ck(self.L.shci_get_inactive_orbitals(self.h, ctypes.byref(m)))
+        return m.value
+
+    def set_var_sd(self, on=True):
+        self._ck(self.L.shci_set_var_sd(self.h, int(on)))
+
+    def set_hf_options(self, allow_doubly_occupy=True, irreps=(), irrep_occs_up=(),
+                       irrep_occs_dn=()):
+        """HF det options of the next load_fcidump (chem/irreps, allow_doubly_occupy_hf)."""
+        a = np.ascontiguousarray(irreps, np.uint32)
+        b = np.ascontiguousarray(irrep_occs_up, np.uint32)
+        c = np.ascontiguousarray(irrep_occs_dn, np.uint32)
+        n = len(a)
+        self._ck(self.L.shci_set_hf_options(self.h, int(allow_doubly_occupy),
+                                            a.ctypes.data if n else None,
+                                            b.ctypes.data if n else None,
+                                            c.ctypes.data if n else None, n))
+
+    def s2(self):
+        v = ctypes.c_double()
+        self._ck(self.L.shci_get_s2(self.h, ctypes.byref(v)))
+        return v.value
 
     def eps_tried(self):
         n = self.n_dets()

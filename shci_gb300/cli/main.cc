@@ -278,6 +278,26 @@ int main(int, char* argv[]) {
   shci_ctx* c = nullptr;
   if (shci_create(&c, device, 0) != SHCI_OK) die("cannot create a context on the GPU");
   std::vector<unsigned> ou(occ_u.begin(), occ_u.end()), od(occ_d.begin(), occ_d.end());
+  // HF det options (integrals.cc:155-215): "chem/irreps" with "chem/irrep_occs_up/dn", and
+  // "allow_doubly_occupy_hf"
+  const std::vector<double> irr = cfg_v("chem/irreps", false);
+  std::vector<unsigned> irreps(irr.begin(), irr.end()), irr_up, irr_dn;
+  if (!irreps.empty() && ou.empty() && od.empty()) {
+    const std::vector<double> a = cfg_v("chem/irrep_occs_up", true);
+    const std::vector<double> b = cfg_v("chem/irrep_occs_dn", true);
+    irr_up.assign(a.begin(), a.end());
+    irr_dn.assign(b.begin(), b.end());
+    if (irr_up.size() != irreps.size() || irr_dn.size() != irreps.size())
+      die("chem/irrep_occs_up and chem/irrep_occs_dn need one entry per entry of chem/irreps");
+  } else {
+    irreps.clear();
+  }
+  ck(c, shci_set_hf_options(c, cfg_b("allow_doubly_occupy_hf", true) ? 1 : 0,
+                            irreps.empty() ? nullptr : irreps.data(),
+                            irr_up.empty() ? nullptr : irr_up.data(),
+                            irr_dn.empty() ? nullptr : irr_dn.data(), irreps.size()),
+     "HF options");
+  const bool explicit_orbs = !ou.empty() || !od.empty() || !irreps.empty();
   // Integrals::load (integrals.cc:17-35): the cache when asked for and present, else FCIDUMP,
   // after which the cache is written
   const char* cache = "integrals_cache.dat";
@@ -309,6 +329,22 @@ int main(int, char* argv[]) {
   ck(c, shci_set_second_rejection(c, cfg_b("second_rejection", false) ? 1 : 0,
                                   cfg_d("second_rejection_factor", 0.2)),
      "second rejection");
+  ck(c, shci_set_has_double_excitation(c, cfg_b("has_double_excitation", true) ? 1 : 0),
+     "has_double_excitation");
+  if (cfg_b("chem/active_space", false)) {  // integrals.cc:295-326
+    if (reorder < 0 ? !explicit_orbs : reorder != 0)
+      die("Set reorder_orbs to false for active space calculations");
+    const std::vector<double> as = cfg_v("chem/irrep_active_space", false);
+    if (as.empty()) die("Active space specification is missing or incorrect.");
+    std::vector<unsigned> asu(as.begin(), as.end());
+    ck(c, shci_set_active_space(c, asu.data(), asu.size()), "active space");
+  }
+  // "var_sd" defaults to "get_pair_contrib" (solver.h:423-424)
+  const bool pair_contrib = cfg_b("get_pair_contrib", false);
+  ck(c, shci_set_var_sd(c, cfg_b("var_sd", pair_contrib) ? 1 : 0), "var_sd");
+  if (pair_contrib)
+    std::printf("Note: get_pair_contrib selects with var_sd; its pair-contribution files are "
+                "not written by this build.\n");
   double qinfo[4];
   ck(c, shci_build_queues(c, qinfo), "heat-bath queues");
   std::printf("Max hci queue elem: %.10f Ha\nNumber of entries in hci queue: %'zu\n", qinfo[0],
@@ -458,6 +494,15 @@ int main(int, char* argv[]) {
         std::fclose(f);
       }
     }
+  }
+  // <S^2> of the first state (post_variation, chem_system.cc:627-634)
+  if (cfg_b("s2", false) && !wfs.empty()) {
+    const Wavefunction wf = time_sym ? unpacked(wfs.back()) : wfs.back();
+    put_wf(c, wf);
+    double s2 = 0.0;
+    ck(c, shci_get_s2(c, &s2), "S^2");
+    std::printf("s_squared: %15.10f\n", s2);
+    result_put("s2", s2);
   }
   if (cfg_b("var_only", false)) {
     shci_destroy(c);

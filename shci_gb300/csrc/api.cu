@@ -63,8 +63,16 @@ void reset_states(shci_ctx* c, size_t n) {
   c->state_energy.assign(c->n_states, 0.0);
 }
 
+// The Hamiltonian drops opposite-spin doubles when the system has no double excitations and
+// no time-reversal symmetry (hamiltonian.h:97-104, 487).
+void apply_excitation_flags(shci_ctx* c) {
+  c->dI.no_mixed_doubles = (!c->has_doubles && !c->time_sym) ? 1 : 0;
+}
+
 void after_integrals(shci_ctx* c) {
   upload_integrals(c);
+  apply_excitation_flags(c);
+  c->inactive_orbs = 0;  // an active space refers to the previous integrals' orbitals
   c->have_integrals = true;
   c->Q.built = false;
   c->up.assign(1, c->I.hf_up);
@@ -193,7 +201,7 @@ shci_status shci_load_fcidump(shci_ctx* c, const char* path, unsigned n_up, unsi
     HostIntegrals I;
     try {
       load_fcidump(I, path, n_up, n_dn, point_group ? point_group : "C1", reorder, occs_up,
-                   occs_dn);
+                   occs_dn, c->hf_opts);
     } catch (const std::runtime_error& e) {
       throw;  // mapped to SHCI_ERR_IO below
     }
@@ -367,6 +375,7 @@ shci_status shci_set_time_sym(shci_ctx* c, int on) {
                          std::to_string(i) + ")");
     }
     c->time_sym = on != 0;
+    apply_excitation_flags(c);
     c->H.valid = false;
     c->H.prefix_ok = false;
     c->H.build_id++;
@@ -792,6 +801,76 @@ shci_status shci_set_second_rejection(shci_ctx* c, int enable, double factor) {
   });
 }
 
+shci_status shci_set_has_double_excitation(shci_ctx* c, int on) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    c->has_doubles = on != 0;
+    apply_excitation_flags(c);
+    c->H.valid = false;
+    c->H.prefix_ok = false;
+    c->H.build_id++;
+    c->eps_tried.clear();
+  });
+}
+
+shci_status shci_set_active_space(shci_ctx* c, const unsigned* irrep_active_space, size_t n) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    if (n == 0) {
+      c->inactive_orbs = 0;
+    } else {
+      if (!irrep_active_space) throw ArgError("null irrep_active_space");
+      try {
+        c->inactive_orbs = inactive_orbitals(
+            c->I, std::vector<unsigned>(irrep_active_space, irrep_active_space + n));
+      } catch (const std::invalid_argument& e) {
+        throw ArgError(e.what());
+      }
+    }
+    c->eps_tried.clear();
+  });
+}
+
+shci_status shci_get_inactive_orbitals(shci_ctx* c, uint64_t* mask) {
+  if (!c || !mask) return SHCI_ERR_ARG;
+  return guard(c, [&]() { *mask = c->inactive_orbs; });
+}
+
+shci_status shci_set_var_sd(shci_ctx* c, int on) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() { c->var_sd = on != 0; });
+}
+
+shci_status shci_set_hf_options(shci_ctx* c, int allow_doubly_occupy, const unsigned* irreps,
+                                const unsigned* irrep_occs_up, const unsigned* irrep_occs_dn,
+                                size_t n_irreps) {
+  if (!c) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    if (n_irreps && (!irreps || !irrep_occs_up || !irrep_occs_dn))
+      throw ArgError("null irrep array");
+    HfOptions o;
+    o.allow_doubly_occupy = allow_doubly_occupy != 0;
+    if (n_irreps) {
+      o.irreps.assign(irreps, irreps + n_irreps);
+      o.irrep_occs_up.assign(irrep_occs_up, irrep_occs_up + n_irreps);
+      o.irrep_occs_dn.assign(irrep_occs_dn, irrep_occs_dn + n_irreps);
+    }
+    c->hf_opts = o;
+  });
+}
+
+shci_status shci_get_s2(shci_ctx* c, double* s2) {
+  if (!c || !s2) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (c->time_sym)
+      throw ArgError("S^2 needs the unpacked wavefunction (shci_unpack_time_sym first)");
+    *s2 = get_s2(c);
+  });
+}
+
 shci_status shci_get_eps_tried(shci_ctx* c, double* out, size_t cap) {
   if (!c || !out) return SHCI_ERR_ARG;
   return guard(c, [&]() {
@@ -812,7 +891,7 @@ shci_status shci_run_variation(shci_ctx* c, const double* eps_vars, size_t n_eps
     std::vector<double> sc;
     if (schedule) sc.assign(schedule, schedule + n_sched);
     c->var_trace.clear();
-    auto e = run_all_variations(c, ev, sc, target_error, precision, false, &c->var_trace);
+    auto e = run_all_variations(c, ev, sc, target_error, precision, c->var_sd, &c->var_trace);
     if (energies)
       for (size_t i = 0; i < e.size(); i++) energies[i] = e[i];
   });

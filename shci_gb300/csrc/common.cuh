@@ -27,6 +27,9 @@ struct DevIntegrals {
   const double* xtab;    // [n^3]      (io|oj) at (i*n+j)*n+o       (exchange)
   const double* jtab;    // [n^2]      (aa|bb) at a*n+b
   const double* ktab;    // [n^2]      (ab|ba) at a*n+b
+  // the Hamiltonian leaves out opposite-spin double excitations (has_double_excitation
+  // false without time_sym, hamiltonian.h:487); 0 keeps them
+  int no_mixed_doubles;
 };
 
 __device__ __forceinline__ int popc64(uint64_t x) { return __popcll(x); }

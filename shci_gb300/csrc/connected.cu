@@ -97,6 +97,8 @@ SelParams conn_params(shci_ctx* c, DevBuf<uint32_t>& pairs) {
   P.n_up = static_cast<int>(c->I.n_up);
   P.n_elecs = n_elecs;
   P.n_pairs = static_cast<int>(pr.size());
+  P.no_doubles = c->has_doubles ? 0 : 1;
+  P.inactive = c->inactive_orbs;
   return P;
 }
 

@@ -202,6 +202,16 @@ struct shci_ctx {
   // time-reversal symmetry (config "time_sym"): the det list holds up <= dn, an open det
   // stands for (|up,dn> + |dn,up>) / sqrt(2); the Hamiltonian is the packed one
   bool time_sym = false;
+  // find_connected_dets options (chem_system.cc:29-30, 327-329, 345, 383-387): doubles off
+  // ("has_double_excitation": false; the Hamiltonian then also drops opposite-spin doubles
+  // unless time_sym, hamiltonian.h:97-104, 487) and the active space ("chem/active_space":
+  // targets above the highest active orbital of their irrep are skipped)
+  bool has_doubles = true;
+  uint64_t inactive_orbs = 0;  // orbitals that may not be excitation targets
+  // selection from the HF det with eps_min = 0 ("var_sd", solver.h:424, 446)
+  bool var_sd = false;
+  // HF det construction options (integrals.cc:155-226), used by the next FCIDUMP load
+  shci::HfOptions hf_opts;
 
   shci::DetIndex idx;
   shci::JoinIndex join;

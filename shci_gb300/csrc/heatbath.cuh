@@ -43,6 +43,11 @@ struct SelParams {
   double rej_factor;  // second_rejection_factor
   double e_hf_1b;     // sum of h_pp over the HF det's electrons (chem_system.cc:812-823)
   int time_sym;       // time-reversal symmetry: list holds up <= dn, open dets stand for pairs
+  // find_connected_dets options: no double excitations (has_double_excitation false,
+  // chem_system.cc:345) and orbitals that may not be targets (the active space,
+  // chem_system.cc:327-329, 383-387); 0 and 0 are the reference's defaults
+  int no_doubles;
+  uint64_t inactive;
 };
 
 constexpr double kSqrt2 = 1.4142135623730951;  // Util::SQRT2 (src/util.h:58)
@@ -100,7 +105,7 @@ __device__ __forceinline__ void slot_range(const SelParams& P, uint64_t up, uint
     *cnt = first_below(P.s_S, a, b, eps_min) - a;
     return;
   }
-  if (eps_min > P.max_hci) return;
+  if (P.no_doubles || eps_min > P.max_hci) return;
   const uint32_t pr = P.pair_tab[slot - P.n_elecs];
   const int p = elec_orb(up, dn, pr & 0xffff, P.n_up, n);
   const int q = elec_orb(up, dn, pr >> 16, P.n_up, n);
@@ -184,6 +189,7 @@ __device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, 
     const bool is_up = slot < P.n_up;
     const int p = is_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
     const int r = static_cast<int>(P.s_r[e]);
+    if (P.inactive >> r & 1) return false;
     if (is_up) {
       if (up >> r & 1) return false;
       *cu = (up & ~(1ull << p)) | (1ull << r);
@@ -207,6 +213,8 @@ __device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, 
     s = r + n;
     r = tmp;
   }
+  if ((P.inactive >> (r < n ? r : r - n) & 1) || (P.inactive >> (s < n ? s : s - n) & 1))
+    return false;
   const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
   if (occ_r) return false;
   const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);
@@ -231,6 +239,7 @@ __device__ __forceinline__ bool make_candidate_at(const SelParams& P, uint64_t u
   if (slot < P.n_elecs) {
     const int p = static_cast<int>(orbs);
     const int r = static_cast<int>(P.s_r[e]);
+    if (P.inactive >> r & 1) return false;
     if (slot < P.n_up) {
       if (up >> r & 1) return false;
       *cu = (up & ~(1ull << p)) | (1ull << r);
@@ -251,6 +260,8 @@ __device__ __forceinline__ bool make_candidate_at(const SelParams& P, uint64_t u
     s = r + n;
     r = tmp;
   }
+  if ((P.inactive >> (r < n ? r : r - n) & 1) || (P.inactive >> (s < n ? s : s - n) & 1))
+    return false;
   const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
   if (occ_r) return false;
   const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);

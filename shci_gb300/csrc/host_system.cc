@@ -190,7 +190,7 @@ void screen_linear(HostIntegrals& I) {
 
 void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsigned n_dn,
                   const std::string& point_group, int reorder, const unsigned* occs_up,
-                  const unsigned* occs_dn) {
+                  const unsigned* occs_dn, const HfOptions& hf) {
   std::ifstream f(path);
   if (!f.good()) throw std::runtime_error("cannot open FCIDUMP '" + path + "'");
   I.n_syms = point_group_order(point_group, &I.linear);
@@ -271,16 +271,51 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
   double ecore = 0.0;
   P.fill(raw, ident, ecore);
 
-  // HF det (integrals.cc:155-226): explicit occupations or the lowest orbitals.
+  // HF det (integrals.cc:155-226): explicit occupations, the listed irreps' occupations, or
+  // the lowest orbitals.
+  const auto syms = convert_syms(raw_syms);
   uint64_t hf_up = 0, hf_dn = 0;
   bool explicit_orbs = false;
   if (occs_up && occs_dn) {
     for (unsigned i = 0; i < n_up; i++) hf_up |= 1ull << occs_up[i];
     for (unsigned i = 0; i < n_dn; i++) hf_dn |= 1ull << occs_dn[i];
     explicit_orbs = true;
+  } else if (!hf.irreps.empty()) {
+    if (hf.irrep_occs_up.size() != hf.irreps.size() || hf.irrep_occs_dn.size() != hf.irreps.size())
+      throw std::runtime_error("chem/irrep_occs_up and chem/irrep_occs_dn need one entry per irrep");
+    for (size_t k = 0; k < hf.irreps.size(); k++) {
+      unsigned occ_up = hf.irrep_occs_up[k], occ_dn = hf.irrep_occs_dn[k];
+      for (unsigned j = 0; j < n; j++) {
+        if (syms[j] != hf.irreps[k]) continue;
+        if (occ_up > 0) {
+          hf_up |= 1ull << j;
+          occ_up--;
+        } else {
+          hf_up &= ~(1ull << j);
+        }
+        if (occ_dn > 0) {
+          hf_dn |= 1ull << j;
+          occ_dn--;
+        } else {
+          hf_dn &= ~(1ull << j);
+        }
+        if (occ_up == 0 && occ_dn == 0 && j >= n_up && j >= n_dn) break;
+      }
+      if (occ_up > 0 || occ_dn > 0)
+        throw std::runtime_error("unable to construct hf with given irrep");
+    }
+    if (__builtin_popcountll(hf_up) != (int)n_up || __builtin_popcountll(hf_dn) != (int)n_dn)
+      throw std::runtime_error("chem/irrep_occs_up / irrep_occs_dn do not add up to n_up / n_dn");
+    explicit_orbs = true;
   } else {
     for (unsigned i = 0; i < n_up; i++) hf_up |= 1ull << i;
-    for (unsigned i = 0; i < n_dn; i++) hf_dn |= 1ull << i;
+    if (hf.allow_doubly_occupy) {
+      for (unsigned i = 0; i < n_dn; i++) hf_dn |= 1ull << i;
+    } else {
+      if (n_up + n_dn > n)
+        throw std::runtime_error("allow_doubly_occupy_hf false needs n_up + n_dn <= n_orbs");
+      for (unsigned i = 0; i < n_dn; i++) hf_dn |= 1ull << (i + n_up);
+    }
   }
   // Orbital energies (integrals.cc:228-255) from the un-reordered tables.
   std::vector<double> e(n);
@@ -308,7 +343,6 @@ void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsi
     std::stable_sort(order.begin(), order.end(),
                      [&](unsigned a, unsigned b) { return e[a] < e[b] - kReorderEps; });
   for (unsigned i = 0; i < n; i++) inv[order[i]] = i;
-  const auto syms = convert_syms(raw_syms);
   I.orb_sym.resize(n);
   I.orb_order = order;
   for (unsigned i = 0; i < n; i++) I.orb_sym[i] = syms[order[i]];
@@ -421,6 +455,27 @@ CacheStatus save_integrals_cache(const HostIntegrals& I, const std::string& path
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) throw std::runtime_error("cannot write " + path);
   return kCacheOk;
+}
+
+uint64_t inactive_orbitals(const HostIntegrals& I, const std::vector<unsigned>& irrep_active_space) {
+  unsigned n_irreps = 0;
+  for (unsigned s : I.orb_sym) n_irreps = std::max(n_irreps, s);
+  if (irrep_active_space.size() < n_irreps)
+    throw std::invalid_argument("chem/irrep_active_space needs an entry for each of the " +
+                                std::to_string(n_irreps) + " irreps");
+  std::vector<int> highest(n_irreps, -1);
+  std::vector<unsigned> taken(n_irreps, 0);
+  for (unsigned i = 0; i < I.n; i++) {
+    const unsigned k = I.orb_sym[i] - 1;
+    if (taken[k] < irrep_active_space[k]) {
+      taken[k]++;
+      highest[k] = static_cast<int>(i);
+    }
+  }
+  uint64_t mask = 0;
+  for (unsigned r = 0; r < I.n; r++)
+    if (static_cast<int>(r) > highest[I.orb_sym[r] - 1]) mask |= 1ull << r;
+  return mask;
 }
 
 double host_diag(const HostIntegrals& I, uint64_t up, uint64_t dn) {

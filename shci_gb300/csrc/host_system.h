@@ -28,11 +28,29 @@ struct HostIntegrals {
   }
 };
 
+// HF det options of Integrals::generate_det_hf (src/chem/integrals.cc:155-226): without
+// explicit occupations, the HF det fills each listed irrep ("chem/irreps") with its
+// "chem/irrep_occs_up" / "chem/irrep_occs_dn" electrons in orbital order (and then counts as
+// explicit: no reordering by default), or else the lowest orbitals, the beta electrons on
+// top of the alpha ones when "allow_doubly_occupy_hf" is false.
+struct HfOptions {
+  bool allow_doubly_occupy = true;
+  std::vector<unsigned> irreps, irrep_occs_up, irrep_occs_dn;
+};
+
 // Reads FCIDUMP and prepares the integrals like Integrals::load (src/chem/integrals.cc:17-384).
 // Throws std::runtime_error with a message on failure.
 void load_fcidump(HostIntegrals& I, const std::string& path, unsigned n_up, unsigned n_dn,
                   const std::string& point_group, int reorder, const unsigned* occs_up,
-                  const unsigned* occs_dn);
+                  const unsigned* occs_dn, const HfOptions& hf = HfOptions());
+
+// Orbitals outside the active space (Integrals::reorder_orbs, src/chem/integrals.cc:295-326):
+// per irrep k the first irrep_active_space[k] orbitals of irrep k + 1, in orbital order, are
+// active, and an orbital above the highest active orbital of its irrep may not be an
+// excitation target (chem_system.cc:327-329, 383-387).  An irrep with no active orbital
+// allows none of its orbitals as targets (the reference reads past an empty list there).
+// Throws std::invalid_argument when fewer entries than irreps are given.
+uint64_t inactive_orbitals(const HostIntegrals& I, const std::vector<unsigned>& irrep_active_space);
 
 // Integrals cache: Integrals::save_to_cache / load_from_cache (src/chem/integrals.cc:17-35,
 // 424-440) keep the prepared integrals (after orbital reordering) in "integrals_cache.dat" so

@@ -91,6 +91,7 @@ struct RowSink {
   // Queue the lanes' candidates (cand) as singles or doubles; drain full queues.
   __device__ __forceinline__ void push(bool cand, bool single, uint32_t j, uint64_t uj,
                                        uint64_t dj) {
+    if (I.no_mixed_doubles && !single && uj != ui && dj != di) cand = false;
 #pragma unroll
     for (int t = 0; t < 2; t++) {
       const bool mine = cand && (single == (t == 0));

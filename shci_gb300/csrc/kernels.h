@@ -133,4 +133,7 @@ void rdm2_dev(shci_ctx* c, double* half_dev);   // device [n^2 (n^2+1) / 2]
 // orbopt.cu: generalized Fock matrix F[n*n] (host) from the RDMs of every state
 void generalized_fock(shci_ctx* c, double* F);
 
+// spin.cu: <S^2> of the first state over the current det list (ChemSystem::get_s2).
+double get_s2(shci_ctx* c);
+
 }  // namespace shci

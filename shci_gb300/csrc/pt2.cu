@@ -651,6 +651,8 @@ void pt_setup(shci_ctx* c, PtSetup& st) {
   P.n_up = static_cast<int>(c->I.n_up);
   P.n_elecs = n_elecs;
   P.n_pairs = static_cast<int>(pairs.size());
+  P.no_doubles = c->has_doubles ? 0 : 1;
+  P.inactive = c->inactive_orbs;
   int sms = 0;
   SHCI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   st.grid = static_cast<unsigned>(sms) * 8u;

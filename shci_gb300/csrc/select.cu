@@ -65,8 +65,9 @@ __global__ void __launch_bounds__(kSelWarps * 32)
 
 // rej_max (second rejection only): the largest rejected |H| of each source, else null.  As
 // find_connected_dets returns it: max(largest rejected, eps_min), except that a det whose
-// eps_min is above every double's |H| returns eps_min before the doubles (chem_system.cc:
-// 339-340), dropping what its singles rejected.
+// eps_min is above every double's |H|, or a system without double excitations, returns
+// eps_min before the doubles (chem_system.cc:339-340, 345), dropping what its singles
+// rejected.
 __global__ void k_sel_mark(SelParams P, uint32_t k_begin, uint32_t k_end,
                            const double* eps_min_in, const double* rej_max) {
   for (uint32_t k = k_begin + blockIdx.x * blockDim.x + threadIdx.x; k < k_end;
@@ -74,7 +75,7 @@ __global__ void k_sel_mark(SelParams P, uint32_t k_begin, uint32_t k_end,
     const uint32_t i = P.pass + 5u * k;
     const double eps_min = eps_min_in[k - k_begin];
     if (eps_min < P.eps_tried[i]) {
-      const bool rej = rej_max && !(eps_min > P.max_hci);
+      const bool rej = rej_max && !P.no_doubles && !(eps_min > P.max_hci);
       P.eps_tried[i] = 1.000000001 * (rej ? fmax(rej_max[k - k_begin], eps_min) : eps_min);
     }
   }
@@ -442,6 +443,8 @@ size_t select_dets(shci_ctx* c, double eps_var, bool var_sd) {
   P.rej_on = c->second_rejection ? 1 : 0;
   P.rej_factor = c->second_rejection_factor;
   P.time_sym = c->time_sym ? 1 : 0;
+  P.no_doubles = c->has_doubles ? 0 : 1;
+  P.inactive = c->inactive_orbs;
   P.e_hf_1b = 0.0;
   if (c->second_rejection) {
     // ChemSystem::get_e_hf_1b (chem_system.cc:812-823) on dets[0]: alpha, then beta (doubled
