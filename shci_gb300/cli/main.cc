@@ -121,6 +121,11 @@ void result_put(const std::string& k, double v) {
   result_dump();
 }
 
+void result_put_str(const std::string& k, const std::string& v) {
+  g_result.put(k) = Json::string(v);
+  result_dump();
+}
+
 std::string key_eps(double e) { return fmt("%#.2e", e); }
 
 std::string wf_filename(double eps_var) { return fmt("wf_eps1_%#.2e.dat", eps_var); }
@@ -342,9 +347,7 @@ int main(int, char* argv[]) {
   // "var_sd" defaults to "get_pair_contrib" (solver.h:423-424)
   const bool pair_contrib = cfg_b("get_pair_contrib", false);
   ck(c, shci_set_var_sd(c, cfg_b("var_sd", pair_contrib) ? 1 : 0), "var_sd");
-  if (pair_contrib)
-    std::printf("Note: get_pair_contrib selects with var_sd; its pair-contribution files are "
-                "not written by this build.\n");
+
   double qinfo[4];
   ck(c, shci_build_queues(c, qinfo), "heat-bath queues");
   std::printf("Max hci queue elem: %.10f Ha\nNumber of entries in hci queue: %'zu\n", qinfo[0],
@@ -362,6 +365,60 @@ int main(int, char* argv[]) {
   const std::vector<double> eps_vars = cfg_v("eps_vars", true);
   const std::vector<double> schedule = cfg_v("eps_vars_schedule", true);
   std::vector<Wavefunction> wfs;
+  // Solver<S>::save_pair_contrib (solver.h:1227-1296): the first state's H_0j c_j / c_0 of
+  // every det j within a double excitation of det 0, summed per pair (i, j) of the det-0
+  // orbitals it vacates (i = j for singles; pairs i != j halved), in det order
+  auto save_pair_contrib = [&](const Wavefunction& w, double eps_var) {
+    const uint64_t hu = w.up[0], hd = w.dn[0];
+    if (hu != hd) die("non sym det_hf not implemented");
+    const size_t nd = w.up.size();
+    std::vector<uint64_t> iu(nd, hu), id(nd, hd);
+    std::vector<double> h(nd, 0.0);
+    ck(c, shci_hamiltonian_elems(c, iu.data(), id.data(), w.up.data(), w.dn.data(), nd, h.data()),
+       "pair contributions");
+    std::vector<double> contrib((size_t)n_up * n_up, 0.0);
+    const double c0 = w.coefs[0];
+    auto left = [](uint64_t a, uint64_t b, unsigned* o) {  // orbitals in a only, ascending
+      unsigned k = 0;
+      for (uint64_t m = a & ~b; m && k < 3; m &= m - 1) o[k++] = __builtin_ctzll(m);
+      return k;
+    };
+    for (size_t d = 1; d < nd; d++) {
+      unsigned lu[3], ld[3];
+      const unsigned nu = left(hu, w.up[d], lu), ndn = left(hd, w.dn[d], ld);
+      if (nu + ndn > 2) continue;
+      size_t i = 0, j = 0;
+      if (nu == 2) {
+        i = lu[0];
+        j = lu[1];
+      } else if (nu == 1) {
+        i = lu[0];
+        j = ndn == 1 ? ld[0] : i;
+        if (j < i) std::swap(i, j);
+      } else {
+        i = ld[0];
+        j = ndn == 2 ? ld[1] : i;
+        if (j < i) std::swap(i, j);
+      }
+      if (i >= n_up || j >= n_up) die("pair contribution outside the first n_up orbitals");
+      double v = h[d] * w.coefs[d] / c0;
+      if (w.up[d] != w.dn[d] && time_sym) v = h[d] * w.coefs[d] / c0 * 1.4142135623730951;
+      contrib[i * n_up + j] += v;
+    }
+    char name[64];
+    std::snprintf(name, sizeof(name), "pair_contrib_%#.2e.csv", eps_var);
+    FILE* f = std::fopen(name, "w");
+    if (!f) die(std::string("cannot write ") + name);
+    std::fprintf(f, "i,j,pair_contrib\n");
+    for (size_t i = 0; i < n_up; i++)
+      for (size_t j = i; j < n_up; j++) {
+        double v = contrib[i * n_up + j];
+        if (i != j) v /= 2;
+        std::fprintf(f, "%zu,%zu,%.15g\n", i, j, v);
+      }
+    std::fclose(f);
+    result_put_str("pair_contrib/" + key_eps(eps_var), name);
+  };
   if (!cfg_b("skip_var", false)) {
     std::printf("Final iteration 0 HF ndets= 1 energy= %.8f\n", e_hf);
     double eps_prev = 1e100;
@@ -378,6 +435,7 @@ int main(int, char* argv[]) {
         for (size_t k = 0; k < lw.n_states(); k++)
           result_put("energy_var" + state_suffix(k) + "/" + key_eps(eps_var), lw.energy_of(k));
         wfs.push_back(std::move(lw));
+        if (pair_contrib) save_pair_contrib(wfs.back(), eps_var);
         eps_prev = eps_var;
         continue;
       }
@@ -426,6 +484,7 @@ int main(int, char* argv[]) {
         result_put("energy_var" + state_suffix(st) + "/" + key_eps(eps_var), wf.energy_of(st));
       save_wf(fn, n_up, n_dn, time_sym, e_hf, wf);
       wfs.push_back(std::move(wf));
+      if (pair_contrib) save_pair_contrib(wfs.back(), eps_var);
       eps_prev = eps_var;
     }
   }

@@ -199,3 +199,46 @@ def test_cli_options(tmp_path):
     (tmp_path / "config.json").write_text(json.dumps(cfg2))
     r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
+
+
+def test_cli_pair_contrib(tmp_path, oracle_mod, w1_fcidump):
+    """"get_pair_contrib": true selects with var_sd and writes pair_contrib_<eps>.csv
+    (solver.h:1227-1296), recomputed here from the written wavefunction with the oracle's
+    matrix elements, in the reference's det order."""
+    from shci_gb300 import build
+    from test_gpu_cli import _read_wf
+    exe = build.build_cli()
+    shutil.copyfile(w1_fcidump, tmp_path / "FCIDUMP")
+    cfg = {"system": "chem", "n_up": 5, "n_dn": 5, "eps_vars": [2e-4], "eps_vars_schedule": [],
+           "chem": {"point_group": "c1"}, "var_only": True, "get_pair_contrib": True,
+           "gpu": {"precision": "fp64"}}
+    (tmp_path / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    res = json.load(open(tmp_path / "result.json"))
+    assert res["pair_contrib"]["2.00e-04"] == "pair_contrib_2.00e-04.csv"
+    lines = open(tmp_path / "pair_contrib_2.00e-04.csv").read().splitlines()
+    assert lines[0] == "i,j,pair_contrib" and len(lines) == 1 + 5 * 6 // 2
+    got = {(int(a), int(b)): float(v) for a, b, v in (l.split(",") for l in lines[1:])}
+    w = _read_wf(tmp_path / "wf_eps1_2.00e-04.dat")
+    o = oracle_mod.Oracle(tmp_path / "FCIDUMP", 5, 5)
+    up, dn, coefs = w["up"], w["dn"], w["coefs"]
+    hf = (int(up[0]), int(dn[0]))
+    want = {}
+    for d in range(1, len(up)):
+        lu = [k for k in range(64) if (hf[0] & ~int(up[d])) >> k & 1]
+        ld = [k for k in range(64) if (hf[1] & ~int(dn[d])) >> k & 1]
+        if len(lu) + len(ld) > 2:
+            continue
+        if len(lu) == 2:
+            i, j = lu
+        elif len(lu) == 1:
+            i, j = sorted([lu[0], ld[0] if ld else lu[0]])
+        else:
+            i, j = sorted([ld[0], ld[1] if len(ld) == 2 else ld[0]])
+        h = o.h_elem(hf, (int(up[d]), int(dn[d])))
+        want[(i, j)] = want.get((i, j), 0.0) + h * coefs[d] / coefs[0]
+    for (i, j), v in got.items():
+        x = want.get((i, j), 0.0) / (2 if i != j else 1)
+        assert abs(v - x) <= 1e-13 * max(1.0, abs(x))
+    assert any(abs(v) > 1e-4 for v in got.values())
