@@ -358,6 +358,15 @@ shci_status shci_pt2_psto(shci_ctx* ctx, double energy_var, double eps_pt_dtm,
                           double eps_pt, double* correction, double* uncert, size_t* n_pt_dets,
                           size_t* n_batches_done);
 
+/* Automatic batch count of the pseudo-stochastic stage ("n_batches_pt_psto" 0 or unset,
+ * solver.h:772-814): the unique PT dets of hash batch 0 of 128 from every 100th variational
+ * det starting at 50 (single excitations below eps_pt_psto dropped), then
+ * n = ceil(2.5 * 128 * 100 * n_pilot * 48 / (pt_mem_avail * mem_usage)), at least 16
+ * (mem_usage = config "pt_psto_mem_usage", default 1; pt_mem_avail from shci_pt_mem_avail).
+ * Needs n_orbs <= 57. */
+shci_status shci_pt2_psto_auto_batches(shci_ctx* ctx, double eps_pt_psto, double pt_mem_avail,
+                                       double mem_usage, size_t* n_batches, size_t* n_pilot_dets);
+
 /* Stochastic stage (Solver<S>::get_energy_pt_sto, solver.h:898-1153): |c_i|-weighted
  * samples drawn on the host with the reference's generator
  * (std::default_random_engine(random_seed)) and alias tables, a random hash batch per

@@ -96,6 +96,7 @@ def load():
         "shci_hamiltonian_stats": [vp, _u64p],
         "shci_memory_stats": [vp, _u64p],
         "shci_pt2_psto": [vp, d, d, d, sz, d, d, P(d), P(d), P(sz), P(sz)],
+        "shci_pt2_psto_auto_batches": [vp, d, d, d, P(sz), P(sz)],
         "shci_pt2_sto": [vp, d, d, d, sz, sz, i, u, sz, d, d, d, d, P(d), P(d), P(sz), _u64p, _f64p, sz],
         "shci_pt_mem_avail": [vp, d, P(d)],
         "shci_mapreduce_sum": [vp, _f64p, sz, _f64p],
@@ -552,6 +553,13 @@ class Context:
                                       target_error, eps_pt, ctypes.byref(v), ctypes.byref(u),
                                       ctypes.byref(n), ctypes.byref(b)))
         return v.value, u.value, n.value, b.value
+
+    def psto_auto_batches(self, eps_pt_psto, pt_mem_avail, mem_usage=1.0):
+        """(batch count, pilot PT dets) of the automatic psto batch count."""
+        nb, npd = ctypes.c_size_t(), ctypes.c_size_t()
+        self._ck(self.L.shci_pt2_psto_auto_batches(self.h, eps_pt_psto, pt_mem_avail, mem_usage,
+                                                   ctypes.byref(nb), ctypes.byref(npd)))
+        return nb.value, npd.value
 
     def pt2_sto(self, energy_var, eps_pt_psto, eps_pt, n_batches, n_samples, seed=347634253,
                 max_iter=100, target_error=5e-5, psto_uncert=0.0, semisto=False,

@@ -622,9 +622,20 @@ int main(int, char* argv[]) {
                   eps_pt_dtm, dtm, u_dtm);
       double value = energy + dtm, uncert = 0.0;
       double psto = 0.0, u_psto = 0.0;
+      double pt_mem = 0.0;
+      if (eps_pt_psto < eps_pt_dtm || eps_pt < eps_pt_psto)
+        ck(c, shci_pt_mem_avail(c, cfg_d("mem_total", machine_memory()), &pt_mem), "PT memory");
       if (eps_pt_psto < eps_pt_dtm) {
         size_t n_psto = 0, nb = 0;
-        const size_t nb_psto = std::max<size_t>(16, (size_t)cfg_d("n_batches_pt_psto", 16));
+        // n_batches_pt_psto, or the reference's estimate from a pilot and the PT memory
+        // (solver.h:772-814)
+        size_t nb_psto = (size_t)cfg_d("n_batches_pt_psto", 0);
+        if (nb_psto == 0) {
+          ck(c, shci_pt2_psto_auto_batches(c, eps_pt_psto, pt_mem,
+                                           cfg_d("pt_psto_mem_usage", 1.0), &nb_psto, nullptr),
+             "psto batches");
+          std::printf("Number of psto batches: %zu\n", nb_psto);
+        }
         ck(c, shci_pt2_psto(c, energy, eps_pt_dtm, eps_pt_psto, nb_psto, target_error, eps_pt,
                             &psto, &u_psto, &n_psto, &nb),
            "PT2 psto");
@@ -638,8 +649,6 @@ int main(int, char* argv[]) {
         // n_dets_in_sample_pt_sto is set; semisto_sto (default true) needs the pilot
         const size_t n_samples = (size_t)cfg_d("n_dets_in_sample_pt_sto", 0);
         const bool semisto = cfg_b("semisto_sto", true);
-        double pt_mem = 0.0;
-        ck(c, shci_pt_mem_avail(c, cfg_d("mem_total", machine_memory()), &pt_mem), "PT memory");
         double sto = 0.0, u_sto = 0.0;
         size_t iters = 0, info[3] = {0, 0, 0};
         ck(c, shci_pt2_sto(c, energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),

@@ -1118,6 +1118,20 @@ shci_status shci_pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, dou
   });
 }
 
+shci_status shci_pt2_psto_auto_batches(shci_ctx* c, double eps_pt_psto, double pt_mem_avail,
+                                       double mem_usage, size_t* n_batches, size_t* n_pilot) {
+  if (!c || !n_batches) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    if (!(pt_mem_avail >= 1.0) || !(mem_usage > 0.0))
+      throw ArgError("pt_mem_avail and mem_usage must be positive");
+    size_t np = 0;
+    *n_batches = psto_auto_batches(c, eps_pt_psto, pt_mem_avail, mem_usage, &np);
+    if (n_pilot) *n_pilot = np;
+  });
+}
+
 shci_status shci_pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
                          size_t n_batches, size_t n_dets_in_sample, int semisto,
                          unsigned random_seed, size_t max_iterations, double target_error,

@@ -107,6 +107,9 @@ struct Pt2Out {
 Pt2Out pt2_dtm(shci_ctx* c, double energy_var, double eps_pt_dtm, size_t n_batches);
 Pt2Out pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
                 size_t n_batches, double target_error, double eps_pt);
+// pt2.cu: the pseudo-stochastic stage's automatic batch count (solver.h:772-814)
+size_t psto_auto_batches(shci_ctx* c, double eps_pt_psto, double pt_mem_avail, double mem_usage,
+                         size_t* n_pilot);
 Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt,
                size_t n_batches, size_t n_dets_in_sample, bool semisto, unsigned random_seed,
                size_t max_iterations, double target_error, double psto_uncert,

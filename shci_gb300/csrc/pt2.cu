@@ -1003,6 +1003,24 @@ size_t pilot_pt_dets(shci_ctx* c, PtSetup& st, const std::vector<size_t>& src, d
   return pt_emit_reduce<kSto>(c, st, Q, S, n_src, hc, bu, bd, bv, shift + 5);
 }
 
+size_t psto_auto_batches(shci_ctx* c, double eps_pt_psto, double pt_mem_avail, double mem_usage,
+                         size_t* n_pilot) {
+  const int shift = c->I.n;
+  if (shift > 57) throw ArgError("the automatic psto batch count supports n_orbs <= 57");
+  PtSetup st;
+  pt_setup(c, st);
+  std::vector<size_t> src;
+  for (size_t i = 50; i < c->up.size(); i += 100) src.push_back(i);
+  const size_t n_pt = pilot_pt_dets(c, st, src, eps_pt_psto, shift);
+  if (n_pilot) *n_pilot = n_pt;
+  const size_t bytes_per_entry = 2 * 16 + 16;  // solver.h:402, 774
+  const double mem = static_cast<double>(static_cast<size_t>(pt_mem_avail)) * mem_usage;
+  size_t nb = static_cast<size_t>(std::ceil(2.5 * 128 * 100 * static_cast<double>(n_pt) *
+                                            static_cast<double>(bytes_per_entry) / mem));
+  if (nb < 16) nb = 16;
+  return nb;
+}
+
 // Stochastic stage (solver.h:898-1153).  n_dets_in_sample = 0: the sample size comes from
 // the reference's 1,000-draw pilot and the PT memory pt_mem_avail (solver.h:942-1006);
 // semisto: the variational dets above the quantile of the top quarter of the unique-sample

@@ -242,3 +242,35 @@ def test_cli_pair_contrib(tmp_path, oracle_mod, w1_fcidump):
         x = want.get((i, j), 0.0) / (2 if i != j else 1)
         assert abs(v - x) <= 1e-13 * max(1.0, abs(x))
     assert any(abs(v) > 1e-4 for v in got.values())
+
+
+def test_psto_auto_batches_matches_pilot(oracle_mod):
+    """The automatic psto batch count (solver.h:772-814): the pilot's unique PT dets equal a
+    recount with the oracle's connection lists, hashes and elements, and the count follows
+    the reference's formula (at least 16)."""
+    import math
+    import shci_gb300 as S
+    c = S.Context()
+    c.load_fcidump(C_ATOM, 4, 2, "d2h")
+    c.run_variation([1e-4], [2e-3, 1e-3, 5e-4, 2e-4], 5e-5, precision=S.PREC_FP64)
+    up, dn, coefs = c.dets()
+    assert len(up) > 250
+    o = oracle_mod.Oracle(C_ATOM, 4, 2, "d2h")
+    o.set_dets(up, dn, coefs)
+    eps = 1e-7
+    var = set(zip(up.tolist(), dn.tolist()))
+    pt = set()
+    for i in range(50, len(up), 100):
+        src = (int(up[i]), int(dn[i]))
+        cu, cd, nx = o.find_connected(src, 1e100 / abs(coefs[i]), eps / abs(coefs[i]))
+        for a, b, x in zip(cu.tolist(), cd.tolist(), nx.tolist()):
+            if (a, b) in var or (o.L.orc_rehash(o.L.orc_det_hash(a, b)) & 127):
+                continue
+            if x == 1 and abs(o.h_elem(src, (a, b), 1) * coefs[i]) < eps:
+                continue
+            pt.add((a, b))
+    for mem in (1e6, 1e15):
+        nb, n_pilot = c.psto_auto_batches(eps, mem)
+        assert n_pilot == len(pt) > 0
+        assert nb == max(16, math.ceil(2.5 * 128 * 100 * len(pt) * 48 / mem))
+    c.close()
