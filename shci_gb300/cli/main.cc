@@ -651,7 +651,9 @@ int main(int, char* argv[]) {
         const bool semisto = cfg_b("semisto_sto", true);
         double sto = 0.0, u_sto = 0.0;
         size_t iters = 0, info[3] = {0, 0, 0};
-        ck(c, shci_pt2_sto(c, energy, eps_pt_psto, eps_pt, (size_t)cfg_d("n_batches_pt_sto", 64),
+        size_t nb_sto = (size_t)cfg_d("n_batches_pt_sto", 0);
+        if (nb_sto == 0) nb_sto = 64;  // solver.h:907-908
+        ck(c, shci_pt2_sto(c, energy, eps_pt_psto, eps_pt, nb_sto,
                            n_samples, semisto ? 1 : 0, (unsigned)cfg_d("random_seed", 347634253),
                            (size_t)cfg_d("max_pt_iterations", 100), target_error, u_psto, pt_mem,
                            cfg_d("pt_sto_mem_usage", 0.4), &sto, &u_sto, &iters, info, nullptr, 0),
