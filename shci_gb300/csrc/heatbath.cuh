@@ -189,12 +189,12 @@ __device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, 
     const bool is_up = slot < P.n_up;
     const int p = is_up ? nth_bit(up, slot) : nth_bit(dn, slot - P.n_up);
     const int r = static_cast<int>(P.s_r[e]);
-    if (P.inactive >> r & 1) return false;
+    // an inactive target (active space) fails like an occupied one
     if (is_up) {
-      if (up >> r & 1) return false;
+      if ((up | P.inactive) >> r & 1) return false;
       *cu = (up & ~(1ull << p)) | (1ull << r);
     } else {
-      if (dn >> r & 1) return false;
+      if ((dn | P.inactive) >> r & 1) return false;
       *cd = (dn & ~(1ull << p)) | (1ull << r);
     }
     return true;
@@ -213,11 +213,11 @@ __device__ __forceinline__ bool make_candidate(const SelParams& P, uint64_t up, 
     s = r + n;
     r = tmp;
   }
-  if ((P.inactive >> (r < n ? r : r - n) & 1) || (P.inactive >> (s < n ? s : s - n) & 1))
-    return false;
-  const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
+  // an inactive target (active space) fails like an occupied one
+  const uint64_t bu = up | P.inactive, bd = dn | P.inactive;
+  const bool occ_r = r < n ? (bu >> r & 1) : (bd >> (r - n) & 1);
   if (occ_r) return false;
-  const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);
+  const bool occ_s = s < n ? (bu >> s & 1) : (bd >> (s - n) & 1);
   if (occ_s) return false;
   uint64_t u = up, d = dn;
   if (p < n) u &= ~(1ull << p); else d &= ~(1ull << (p - n));
@@ -239,12 +239,12 @@ __device__ __forceinline__ bool make_candidate_at(const SelParams& P, uint64_t u
   if (slot < P.n_elecs) {
     const int p = static_cast<int>(orbs);
     const int r = static_cast<int>(P.s_r[e]);
-    if (P.inactive >> r & 1) return false;
+    // an inactive target (active space) fails like an occupied one
     if (slot < P.n_up) {
-      if (up >> r & 1) return false;
+      if ((up | P.inactive) >> r & 1) return false;
       *cu = (up & ~(1ull << p)) | (1ull << r);
     } else {
-      if (dn >> r & 1) return false;
+      if ((dn | P.inactive) >> r & 1) return false;
       *cd = (dn & ~(1ull << p)) | (1ull << r);
     }
     return true;
@@ -260,11 +260,11 @@ __device__ __forceinline__ bool make_candidate_at(const SelParams& P, uint64_t u
     s = r + n;
     r = tmp;
   }
-  if ((P.inactive >> (r < n ? r : r - n) & 1) || (P.inactive >> (s < n ? s : s - n) & 1))
-    return false;
-  const bool occ_r = r < n ? (up >> r & 1) : (dn >> (r - n) & 1);
+  // an inactive target (active space) fails like an occupied one
+  const uint64_t bu = up | P.inactive, bd = dn | P.inactive;
+  const bool occ_r = r < n ? (bu >> r & 1) : (bd >> (r - n) & 1);
   if (occ_r) return false;
-  const bool occ_s = s < n ? (up >> s & 1) : (dn >> (s - n) & 1);
+  const bool occ_s = s < n ? (bu >> s & 1) : (bd >> (s - n) & 1);
   if (occ_s) return false;
   uint64_t u = up, d = dn;
   if (p < n) u &= ~(1ull << p); else d &= ~(1ull << (p - n));
