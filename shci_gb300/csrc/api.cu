@@ -1,8 +1,12 @@
 // C ABI of libshci_gpu.so (declared in include/shci_gpu.h).  Every entry point catches
 // exceptions and CUDA errors and turns them into a status plus shci_last_error().
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "ctx.h"
 #include "kernels.h"
@@ -317,25 +321,47 @@ shci_status shci_set_dets(shci_ctx* c, const uint64_t* up, const uint64_t* dn,
     need_integrals(c);
     if (n == 0 || !up || !dn) throw ArgError("empty det list");
     const uint64_t full = c->I.n == 64 ? ~0ull : ((1ull << c->I.n) - 1ull);
-    for (size_t i = 0; i < n; i++) {
-      if ((up[i] & ~full) || (dn[i] & ~full) ||
-          __builtin_popcountll(up[i]) != (int)c->I.n_up ||
-          __builtin_popcountll(dn[i]) != (int)c->I.n_dn)
-        throw ArgError("det " + std::to_string(i) + " has the wrong electron count or orbitals");
-    }
-    // device copies straight from the caller's buffers (pinned buffers give async DMA)
+    // checks and host copies in chunks over the host threads
+    const size_t n_chunks = std::min<size_t>(host_threads(), (n + 65535) / 65536);
+    auto chunked = [&](auto f) {
+      std::vector<std::thread> th;
+      for (size_t t = 1; t < n_chunks; t++) th.emplace_back(f, n * t / n_chunks, n * (t + 1) / n_chunks);
+      f(size_t{0}, n / n_chunks);
+      for (auto& x : th) x.join();
+    };
+    std::atomic<size_t> bad{n};
+    chunked([&](size_t b, size_t e) {
+      for (size_t i = b; i < e; i++)
+        if ((up[i] & ~full) || (dn[i] & ~full) ||
+            __builtin_popcountll(up[i]) != (int)c->I.n_up ||
+            __builtin_popcountll(dn[i]) != (int)c->I.n_dn) {
+          size_t cur = bad.load();
+          while (i < cur && !bad.compare_exchange_weak(cur, i)) {
+          }
+          break;
+        }
+    });
+    if (bad.load() < n)
+      throw ArgError("det " + std::to_string(bad.load()) +
+                     " has the wrong electron count or orbitals");
+    // device copies straight from the caller's buffers (pinned buffers give async DMA), the
+    // host copies meanwhile
     cudaStream_t s = c->stream;
     c->d_up.resize(n, 1.1);
     c->d_dn.resize(n, 1.1);
     c->d_coef.resize(n, 1.1);
     SHCI_CUDA(cudaMemcpyAsync(c->d_up.p, up, n * 8, cudaMemcpyHostToDevice, s));
     SHCI_CUDA(cudaMemcpyAsync(c->d_dn.p, dn, n * 8, cudaMemcpyHostToDevice, s));
-    c->up.assign(up, up + n);
-    c->dn.assign(dn, dn + n);
-    if (coefs) {
-      SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, coefs, n * 8, cudaMemcpyHostToDevice, s));
-      c->coefs.assign(coefs, coefs + n);
-    } else {
+    if (coefs) SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, coefs, n * 8, cudaMemcpyHostToDevice, s));
+    c->up.resize(n);
+    c->dn.resize(n);
+    if (coefs) c->coefs.resize(n);
+    chunked([&](size_t b, size_t e) {
+      std::memcpy(c->up.data() + b, up + b, (e - b) * 8);
+      std::memcpy(c->dn.data() + b, dn + b, (e - b) * 8);
+      if (coefs) std::memcpy(c->coefs.data() + b, coefs + b, (e - b) * 8);
+    });
+    if (!coefs) {
       c->coefs.assign(n, 1e-16);
       c->coefs[0] = 1.0;
       SHCI_CUDA(cudaMemcpyAsync(c->d_coef.p, c->coefs.data(), n * 8, cudaMemcpyHostToDevice, s));
