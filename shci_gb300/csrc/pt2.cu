@@ -916,20 +916,38 @@ Pt2Out pt_batched(shci_ctx* c, double e_var, PtParams Q, size_t n_batches, doubl
   return out;
 }
 
-// Vose alias tables, as src/util.cc:128-175.
+// f(begin, end) over [0, n) in contiguous chunks, one per host thread (chunk k on thread k).
+template <class F>
+void host_chunks(size_t n, F f) {
+  const size_t k = std::max<size_t>(1, std::min<size_t>(host_threads(), (n + 65535) / 65536));
+  std::vector<std::thread> th;
+  for (size_t t = 1; t < k; t++) th.emplace_back(f, t, n * t / k, n * (t + 1) / k);
+  f(size_t{0}, size_t{0}, n / k);
+  for (auto& x : th) x.join();
+}
+
+// Vose alias tables, as src/util.cc:128-175.  The scaled probabilities and the initial
+// small / large stacks are formed in chunks on the host threads (each chunk's indices in
+// order, the chunks concatenated in order: the stacks the sequential pass would build); the
+// pairing loop is sequential.
 void alias_tables(const std::vector<double>& p, std::vector<double>& np, std::vector<size_t>& al) {
   const size_t L = p.size();
   np.assign(L, 0.0);
   al.assign(L, 0);
   std::vector<double> t(L);
   std::vector<size_t> small, large;  // used as stacks (back = top)
+  std::vector<std::vector<size_t>> cs(host_threads()), cl(host_threads());
+  host_chunks(L, [&](size_t k, size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) {
+      t[i] = p[i] * L;
+      if (t[i] < 1.) cs[k].push_back(i);
+      else cl[k].push_back(i);
+    }
+  });
   small.reserve(L);
   large.reserve(L);
-  for (size_t i = 0; i < L; i++) {
-    t[i] = p[i] * L;
-    if (t[i] < 1.) small.push_back(i);
-    else large.push_back(i);
-  }
+  for (auto& v : cs) small.insert(small.end(), v.begin(), v.end());
+  for (auto& v : cl) large.insert(large.end(), v.begin(), v.end());
   while (!small.empty() && !large.empty()) {
     const size_t l = large.back(), s = small.back();
     np[s] = t[s];
@@ -1052,7 +1070,9 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   double sum_w = 0.0;
   for (size_t i = 0; i < n_var; i++) sum_w += std::abs(coefs[i]);
   std::vector<double> probs(n_var), cum;
-  for (size_t i = 0; i < n_var; i++) probs[i] = std::abs(coefs[i]) / sum_w;
+  host_chunks(n_var, [&](size_t, size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) probs[i] = std::abs(coefs[i]) / sum_w;
+  });
   if (n_dets_in_sample == 0) {  // the pilot draws by inverse CDF
     cum.resize(n_var);
     for (size_t i = 0; i < n_var; i++) cum[i] = i > 0 ? probs[i] + cum[i - 1] : probs[i];
@@ -1175,14 +1195,21 @@ Pt2Out pt2_sto(shci_ctx* c, double energy_var, double eps_pt_psto, double eps_pt
   if (max_iterations > 0)
     next_draws = std::async(draw_policy, draw_pass,
                             static_cast<uint32_t>(std::min<size_t>(kFirstChunk, max_iterations)));
+  // per-iteration sample counts, one array per iteration of a pass (zero between uses; set up
+  // on a helper thread while the alias tables are built); which iterations of a pass drew
+  // each det (zero between uses); the deterministic dets
+  std::vector<std::vector<uint32_t>> cnts;
+  std::vector<uint8_t> pass_mask, is_dtm;
+  auto zeroed = std::async(n_host > 1 ? std::launch::async : std::launch::deferred, [&]() {
+    const size_t k = std::min<size_t>(std::max<size_t>(kFirstChunk, kNextChunk), max_iterations);
+    for (size_t it = 0; it < k; it++) cnts.emplace_back(n_var, 0u);
+    pass_mask.assign(n_var, 0);
+    is_dtm.assign(n_var, 0);
+  });
   std::vector<double> aprob;
   std::vector<size_t> alias;
   alias_tables(probs, aprob, alias);
-
-  // per-iteration sample counts, one array per iteration of a pass (zero between uses); which
-  // iterations of a pass drew each det (zero between uses); the deterministic dets
-  std::vector<std::vector<uint32_t>> cnts;
-  std::vector<uint8_t> pass_mask(n_var, 0), is_dtm(n_var, 0);
+  zeroed.get();
   for (uint32_t i : dtm_list) is_dtm[i] = 1;
   static_assert(kFirstChunk <= 8 && kNextChunk <= 8, "iteration masks are 8 bits");
   if (c->prof.on)
