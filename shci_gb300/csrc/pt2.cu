@@ -617,6 +617,7 @@ struct PtSetup {
 
 void pt_setup(shci_ctx* c, PtSetup& st) {
   if (!c->Q.built) throw ArgError("heat-bath queues not built (call shci_build_queues)");
+  HostScope hs(c->prof, "pt2_host_pt_setup");
   sync_dets(c);
   cudaStream_t s = c->stream;
   const int n_elecs = static_cast<int>(c->I.n_up + c->I.n_dn);
@@ -688,6 +689,7 @@ void pt_emit_append(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSource
     uint32_t k1 = k0;
     while (k1 < n_src && (k1 == k0 || tot + slots[k1] <= kCap)) tot += slots[k1++];
     if (tot > 0) {
+      HostScope hs_off(c->prof, "pt2_host_offsets");
       std::vector<uint64_t> off(k1 - k0 + 1);
       uint64_t acc = 0;
       for (uint32_t k = k0; k < k1; k++) {
@@ -699,6 +701,7 @@ void pt_emit_append(shci_ctx* c, PtSetup& st, const PtParams& Q, const StoSource
       d_off.mt = &c->mem;
       d_off.resize(off.size());
       SHCI_CUDA(cudaMemcpyAsync(d_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
+      hs_off.stop();
       d_over.resize(k1 - k0);
       SHCI_CUDA(cudaMemsetAsync(d_over.p, 0, k1 - k0, s));
       cu.resize(tot, 1.25);
