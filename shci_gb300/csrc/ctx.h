@@ -112,6 +112,7 @@ struct DevHamiltonian {
   DevBuf<float> xs;           // [2n] x split into float pairs
   DevBuf<unsigned long long> yfix;  // [n] y in 64-bit fixed point
   DevBuf<float> rowabs;       // [n] scratch for the bound
+  bool rowabs_hb = false;     // rowabs holds the heat-bath bounds of the dets (not store sums)
 };
 
 // All segments of H: older ones, then the current build's.
@@ -133,6 +134,9 @@ struct DevQueues {
   DevBuf<uint32_t> s_off;
   DevBuf<double> s_S;
   DevBuf<uint32_t> s_r;
+  // sums of the queue values: per orbital over its singles queue, per pair over its doubles
+  // queue (bounds of sum_j |H_ij| over all excitations of a det)
+  DevBuf<double> s_tot, d_tot;
   double max_hci = 0.0, max_singles = 0.0;
   size_t n_hci = 0, n_singles = 0;
   bool built = false;

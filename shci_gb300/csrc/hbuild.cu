@@ -25,6 +25,7 @@
 #include <cstring>
 
 #include "ctx.h"
+#include "heatbath.cuh"
 #include "hrow.cuh"
 #include "kernels.h"
 
@@ -436,6 +437,48 @@ static size_t store_room(shci_ctx* c) {
 //   join, two pass  - count, scan, fill (packed rows), when the bound does not fit in memory;
 //   scan            - group index + scan traversal, count and fill (packed rows).
 // SHCI_HBUILD=scan forces the scan path, SHCI_HBUILD=join2 the two-pass join.
+namespace {
+
+// Bound of sum_j |H_ij| over every excitation of det i (both triangles of its row): the singles
+// queue values of its electrons' orbitals (each S_pr bounds |H| of p -> r for any det) plus
+// the doubles queue values of its electron pairs (the exact |H| of each pq -> rs), summed per
+// orbital / pair ahead (s_tot, d_tot); a warp per det, lanes over its electrons.  The mixed
+// H*v only needs a valid bound for its fixed-point scale, and one per det, independent of the
+// det list, saves the fill an FP32 atomic per stored element.
+__global__ void k_hb_row_bound(const uint64_t* __restrict__ up, const uint64_t* __restrict__ dn,
+                               uint32_t begin, uint32_t end, int n, int n_up, int n_elecs,
+                               const double* __restrict__ stot, const double* __restrict__ dtot,
+                               float* __restrict__ rowabs) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = begin + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < end;
+       i += warps) {
+    const uint64_t u = up[i], d = dn[i];
+    double acc = 0.0;
+    for (int a = static_cast<int>(lane); a < n_elecs; a += 32) {
+      const int p = elec_orb(u, d, a, n_up, n);
+      acc += stot[p < n ? p : p - n];
+      for (int b = a + 1; b < n_elecs; b++) {
+        const int q = elec_orb(u, d, b, n_up, n);
+        int p2 = p, q2 = q;
+        if (p >= n && q >= n) {
+          p2 -= n;
+          q2 -= n;
+        } else if (p < n && q >= n && p > q - n) {
+          p2 = q - n;
+          q2 = p + n;
+        }
+        acc += dtot[c2(p2, q2)];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if (lane == 0) rowabs[i] = __double2float_ru(acc);
+  }
+}
+
+}  // namespace
+
 size_t build_hamiltonian(shci_ctx* c, int precision) {
   if (c->time_sym) return build_time_sym(c, precision);
   auto& H = c->H;
@@ -499,20 +542,37 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   const unsigned grid = static_cast<unsigned>(dev_sms) * 8u;
   unsigned* work = c->err_word.p;
   SHCI_CUDA(cudaMemsetAsync(work, 0, 8 * sizeof(unsigned), s));
-  // a mixed build also sums |H_ij| per det (the H*v fixed-point bound); an incremental one
-  // adds to the sums of the older segments
+  // A mixed build needs a bound of sum_j |H_ij| per det (the H*v fixed-point scale): the
+  // heat-bath bound of each det when the queues exist (new dets only on an incremental update
+  // over such bounds), else the stored elements' |H| summed by the fill (an incremental one
+  // adding to the sums of the older segments).
   float* absacc = nullptr;
+  bool hb_bound = false;
   if (precision == SHCI_PREC_MIXED) {
-    if (n_prev) {
-      H.rowabs.grow_keep(n, s, 1.1);
-      SHCI_CUDA(cudaMemsetAsync(H.rowabs.p + n_prev, 0, (n - n_prev) * sizeof(float), s));
+    if (n_prev) H.rowabs.grow_keep(n, s, 1.1);
+    else H.rowabs.resize(n, 1.1);
+    if (c->Q.built) {
+      const uint32_t begin = (n_prev && H.rowabs_hb) ? static_cast<uint32_t>(n_prev) : 0u;
+      const int n_elecs = static_cast<int>(c->I.n_up + c->I.n_dn);
+      k_hb_row_bound<<<grid_for((size_t)(n - begin) * 32, 256), 256, 0, s>>>(
+          c->d_up.p, c->d_dn.p, begin, static_cast<uint32_t>(n), static_cast<int>(c->I.n),
+          static_cast<int>(c->I.n_up), n_elecs, c->Q.s_tot.p, c->Q.d_tot.p, H.rowabs.p);
+      SHCI_LAUNCH_CHECK();
+      c->launches += 1;
+      H.rowabs_hb = true;
+      hb_bound = true;
     } else {
-      H.rowabs.resize(n, 1.1);
-      SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
+      // (older rows keep their sums, or their heat-bath bounds, which bound any new columns too)
+      if (n_prev)
+        SHCI_CUDA(cudaMemsetAsync(H.rowabs.p + n_prev, 0, (n - n_prev) * sizeof(float), s));
+      else
+        SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, n * sizeof(float), s));
+      absacc = H.rowabs.p;
+      H.rowabs_hb = false;
     }
-    absacc = H.rowabs.p;
   } else {
     H.rowabs.release();
+    H.rowabs_hb = false;
   }
   k_hdiag<<<grid_for(n, 256), 256, 0, s>>>(c->dI, c->d_up.p, c->d_dn.p, (uint32_t)n, H.diag.p);
   SHCI_LAUNCH_CHECK();
@@ -556,7 +616,7 @@ size_t build_hamiltonian(shci_ctx* c, int precision) {
   unsigned long long cand[3] = {0, 0, 0};
   SHCI_CUDA(cudaMemcpyAsync(cand, work + 2, 24, cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));
-  if (absacc) finish_mixed_bound(c);
+  if (absacc || hb_bound) finish_mixed_bound(c);
   H.nnz_current = nnz;
   H.nnz = nnz;
   for (const auto& sg : H.older) H.nnz += sg->nnz;

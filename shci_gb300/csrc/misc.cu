@@ -223,6 +223,13 @@ void upload_queues(shci_ctx* c) {
   upload(D.s_off, Q.s_off, s, &c->mem);
   upload(D.s_S, Q.s_S, s, &c->mem);
   upload(D.s_r, Q.s_r, s, &c->mem);
+  std::vector<double> stot(Q.s_off.size() - 1, 0.0), dtot(Q.d_off.size() - 1, 0.0);
+  for (size_t p = 0; p + 1 < Q.s_off.size(); p++)
+    for (size_t e = Q.s_off[p]; e < Q.s_off[p + 1]; e++) stot[p] += Q.s_S[e];
+  for (size_t pq = 0; pq + 1 < Q.d_off.size(); pq++)
+    for (size_t e = Q.d_off[pq]; e < Q.d_off[pq + 1]; e++) dtot[pq] += Q.d_H[e];
+  upload(D.s_tot, stot, s, &c->mem);
+  upload(D.d_tot, dtot, s, &c->mem);
   SHCI_CUDA(cudaStreamSynchronize(s));
   D.n_pairs = Q.d_off.size() - 1;
   D.max_hci = Q.max_hci;

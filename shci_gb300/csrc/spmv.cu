@@ -239,6 +239,7 @@ void mixed_bound(shci_ctx* c, unsigned grid) {
   cudaStream_t s = c->stream;
   const uint32_t n = static_cast<uint32_t>(H.n);
   H.rowabs.resize(n, 1.1);
+  H.rowabs_hb = false;
   SHCI_CUDA(cudaMemsetAsync(H.rowabs.p, 0, (size_t)n * 4, s));
   for (const SegView& g : segments(H)) {
     k_rowabs<true><<<grid, 256, 0, s>>>(g.row_ptr, g.row_cnt, g.col, g.val32, g.res32, H.diag.p,

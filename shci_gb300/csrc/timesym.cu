@@ -193,6 +193,7 @@ size_t build_time_sym(shci_ctx* c, int precision) {
   H.packed = true;
   H.bound_valid = false;
   H.rowabs.release();
+  H.rowabs_hb = false;
   H.row_ptr.resize(n + 1, 1.25);
   H.row_cnt.resize(n + 1, 1.25);
   H.diag.resize(n, 1.25);
