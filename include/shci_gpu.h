@@ -295,7 +295,7 @@ shci_status shci_get_inactive_orbitals(shci_ctx* ctx, uint64_t* mask);
  * default "get_pair_contrib", solver.h:423-424, 446).  Off by default. */
 shci_status shci_set_var_sd(shci_ctx* ctx, int on);
 
-/* HF det options of the next shci_load_fcidump (Integrals::generate_det_hf,
+/* HF det options of the following shci_load_fcidump calls (Integrals::generate_det_hf,
  * integrals.cc:155-226): without occs_up / occs_dn, n_irreps > 0 fills irreps[k] (orbital
  * symmetry labels as in ORBSYM, linear groups in the reference's labels) with
  * irrep_occs_up[k] / irrep_occs_dn[k] electrons in orbital order (config "chem/irreps",

@@ -214,7 +214,7 @@ struct shci_ctx {
   uint64_t inactive_orbs = 0;  // orbitals that may not be excitation targets
   // selection from the HF det with eps_min = 0 ("var_sd", solver.h:424, 446)
   bool var_sd = false;
-  // HF det construction options (integrals.cc:155-226), used by the next FCIDUMP load
+  // HF det construction options (integrals.cc:155-226), used by the FCIDUMP loads that follow
   shci::HfOptions hf_opts;
 
   shci::DetIndex idx;

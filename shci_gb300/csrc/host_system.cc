@@ -459,7 +459,10 @@ CacheStatus save_integrals_cache(const HostIntegrals& I, const std::string& path
 
 uint64_t inactive_orbitals(const HostIntegrals& I, const std::vector<unsigned>& irrep_active_space) {
   unsigned n_irreps = 0;
-  for (unsigned s : I.orb_sym) n_irreps = std::max(n_irreps, s);
+  for (unsigned s : I.orb_sym) {
+    if (s == 0) throw std::invalid_argument("orbital symmetry labels start at 1");
+    n_irreps = std::max(n_irreps, s);
+  }
   if (irrep_active_space.size() < n_irreps)
     throw std::invalid_argument("chem/irrep_active_space needs an entry for each of the " +
                                 std::to_string(n_irreps) + " irreps");
