@@ -430,6 +430,20 @@ shci_status shci_batch_solve(int device, const shci_batch_item* items, size_t n,
 
 /* ---- RDMs: the adjoint of E_var (RDM::get_1rdm / get_2rdm, src/chem/rdm.cc) ---------- */
 
+/* Natural orbitals (Optimization::get_natorb_rotation_matrix, optimization.cc:6-79): the
+ * context's 1-RDM (summed over the states) diagonalised within each irrep; rot[i * n + p] is
+ * the rotation (column p of an irrep's block = the eigenvector of its p-th largest
+ * occupation, in that irrep's orbital order), occ[p] the occupation numbers. */
+shci_status shci_natural_orbitals(shci_ctx* ctx, double* rot, double* occ);
+
+/* Rotates the context's integrals by the orthogonal rot (rot[i * n + p] = U_ip, mixing only
+ * orbitals of the same irrep): (pq|rs) -> sum_ijkl U_ip U_jq U_kr U_ls (ij|kl) on the device,
+ * one index at a time, and h -> U^T h U (Optimization::rotate_integrals / rewrite_integrals,
+ * optimization.cc:81-240; each class of symmetry-equal integrals keeps its first value of
+ * largest magnitude, as the reference's tables do).  The det list returns to the HF det and
+ * the heat-bath queues are rebuilt on the next use, as after a new FCIDUMP. */
+shci_status shci_rotate_integrals(shci_ctx* ctx, const double* rot);
+
 /* <S^2> of the first state of the context's wavefunction (ChemSystem::get_s2,
  * chem_system.cc:745-798; config "s2", post_variation :627-634).  A time_sym wavefunction must
  * be unpacked first (SHCI_ERR_ARG). */

@@ -77,6 +77,8 @@ def load():
         "shci_set_var_sd": [vp, i],
         "shci_set_hf_options": [vp, i, vp, vp, vp, sz],
         "shci_get_s2": [vp, P(d)],
+        "shci_natural_orbitals": [vp, _f64p, _f64p],
+        "shci_rotate_integrals": [vp, _f64p],
         "shci_set_n_states": [vp, u],
         "shci_set_time_sym": [vp, i],
         "shci_unpack_time_sym": [vp],
@@ -505,6 +507,16 @@ class Context:
                                             a.ctypes.data if n else None,
                                             b.ctypes.data if n else None,
                                             c.ctypes.data if n else None, n))
+
+    def natural_orbitals(self):
+        """(rotation U with U[i, p], occupation numbers) of the 1-RDM, per irrep."""
+        n = self.n_orbs
+        rot, occ = np.zeros(n * n), np.zeros(n)
+        self._ck(self.L.shci_natural_orbitals(self.h, rot, occ))
+        return rot.reshape(n, n), occ
+
+    def rotate_integrals(self, rot):
+        self._ck(self.L.shci_rotate_integrals(self.h, np.ascontiguousarray(rot, np.float64).ravel()))
 
     def s2(self):
         v = ctypes.c_double()

@@ -886,6 +886,38 @@ shci_status shci_set_hf_options(shci_ctx* c, int allow_doubly_occupy, const unsi
   });
 }
 
+shci_status shci_natural_orbitals(shci_ctx* c, double* rot, double* occ) {
+  if (!c || !rot || !occ) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    std::vector<double> g1((size_t)c->I.n * c->I.n);
+    const shci_status st = shci_rdm1(c, g1.data());
+    if (st != SHCI_OK) throw std::runtime_error(c->err);
+    natural_orbitals(c, g1.data(), rot, occ);
+  });
+}
+
+shci_status shci_rotate_integrals(shci_ctx* c, const double* rot) {
+  if (!c || !rot) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    const size_t n = c->I.n;
+    for (size_t p = 0; p < n; p++)
+      for (size_t q = 0; q < n; q++) {
+        double d = 0.0;
+        for (size_t i = 0; i < n; i++) d += rot[i * n + p] * rot[i * n + q];
+        if (std::fabs(d - (p == q ? 1.0 : 0.0)) > 1e-8)
+          throw ArgError("rotation matrix is not orthogonal");
+        // the orbital symmetry labels stay valid only for rotations within each irrep
+        if (c->I.orb_sym[p] != c->I.orb_sym[q] && std::fabs(rot[p * n + q]) > 1e-12)
+          throw ArgError("rotation matrix mixes orbitals of different irreps");
+      }
+    rotate_integrals(c, rot);
+    after_integrals(c);
+  });
+}
+
 shci_status shci_get_s2(shci_ctx* c, double* s2) {
   if (!c || !s2) return SHCI_ERR_ARG;
   return guard(c, [&]() {

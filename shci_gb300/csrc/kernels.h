@@ -135,6 +135,10 @@ void rdm2_dev(shci_ctx* c, double* half_dev);   // device [n^2 (n^2+1) / 2]
 
 // orbopt.cu: generalized Fock matrix F[n*n] (host) from the RDMs of every state
 void generalized_fock(shci_ctx* c, double* F);
+// orbopt.cu: natural orbitals of a 1-RDM g1 (n x n) per irrep, and the rotation of the
+// context's integrals by an orthogonal rot (n x n, rot[i * n + p] = U_ip)
+void natural_orbitals(shci_ctx* c, const double* g1, double* rot, double* occ);
+void rotate_integrals(shci_ctx* c, const double* rot);
 
 // spin.cu: <S^2> of the first state over the current det list (ChemSystem::get_s2).
 double get_s2(shci_ctx* c);

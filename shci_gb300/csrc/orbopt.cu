@@ -14,6 +14,8 @@
 // consecutive threads, so the (nq|rs) row of the dense integral table is read coalesced and
 // the RDM row (m n + q) from L2; the partial sums reduce in a fixed order (bit-reproducible).
 // Work n^5 FP64 multiply-adds: 0.1 G at n = 38, 1.1 G at n = 64.
+#include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "ctx.h"
@@ -113,6 +115,123 @@ void generalized_fock(shci_ctx* c, double* F_host) {
   SHCI_CUDA(cudaStreamSynchronize(s));
   c->prof.flush();
   c->launches += 1;
+}
+
+
+// ---------------------------------------------------------------- natural orbitals, rotation
+// Optimization::get_natorb_rotation_matrix (optimization.cc:6-79): the 1-RDM diagonalised
+// within each irrep; column j of an irrep's block of rot is the eigenvector of its j-th
+// largest occupation, occ[inds[i]] = the i-th largest eigenvalue.  Optimization::
+// rotate_integrals / rewrite_integrals (:81-240): (pq|rs) -> sum U_ip U_jq U_kr U_ls (ij|kl)
+// one index at a time, h -> U^T h U, and the rewritten tables keep, for each 8-fold (2-fold)
+// class of equal integrals, the first value of largest magnitude in (p, q, r, s) order, as the
+// reference's hash storage does.
+namespace {
+
+// out[..., c_axis, ...] = sum_i U[i, c_axis] in[..., i, ...]; stride = n^(3 - axis)
+__global__ void k_rot_axis(const double* __restrict__ in, double* __restrict__ out,
+                           const double* __restrict__ U, int n, size_t stride) {
+  const size_t total = (size_t)n * n * n * n;
+  for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < total;
+       id += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>((id / stride) % n);
+    const size_t base = id - (size_t)c * stride;
+    double acc = 0.0;
+    for (int i = 0; i < n; i++) acc = fma(U[i * n + c], in[base + (size_t)i * stride], acc);
+    out[id] = acc;
+  }
+}
+
+}  // namespace
+
+void natural_orbitals(shci_ctx* c, const double* g1, double* rot, double* occ) {
+  const auto& I = c->I;
+  const int n = static_cast<int>(I.n);
+  unsigned n_irreps = 0;
+  for (unsigned s : I.orb_sym) n_irreps = std::max(n_irreps, s);
+  std::fill(rot, rot + (size_t)n * n, 0.0);
+  for (unsigned irrep = 1; irrep <= n_irreps; irrep++) {
+    std::vector<int> inds;
+    for (int i = 0; i < n; i++)
+      if (I.orb_sym[i] == irrep) inds.push_back(i);
+    const int k = static_cast<int>(inds.size());
+    if (!k) continue;
+    std::vector<double> sub((size_t)k * k), ev(k), evec((size_t)k * k);
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < k; j++) sub[i * k + j] = g1[inds[i] * n + inds[j]];
+    jacobi_eig(k, sub.data(), k, ev.data(), evec.data());  // ascending
+    for (int i = 0; i < k; i++) {
+      occ[inds[i]] = ev[k - 1 - i];
+      for (int j = 0; j < k; j++) rot[inds[i] * n + inds[j]] = evec[i * k + (k - 1 - j)];
+    }
+  }
+}
+
+void rotate_integrals(shci_ctx* c, const double* rot) {
+  auto& I = c->I;
+  const int n = static_cast<int>(I.n);
+  const size_t n4 = (size_t)n * n * n * n;
+  cudaStream_t s = c->stream;
+  DevBuf<double> a, b, u;
+  a.mt = b.mt = u.mt = &c->mem;
+  a.resize(n4);
+  b.resize(n4);
+  u.resize((size_t)n * n);
+  SHCI_CUDA(cudaMemcpyAsync(a.p, I.g2.data(), n4 * 8, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(u.p, rot, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
+  // p, q, r, s in the reference's order
+  const size_t strides[4] = {(size_t)n * n * n, (size_t)n * n, (size_t)n, 1};
+  for (int axis = 0; axis < 4; axis++) {
+    k_rot_axis<<<grid_for(n4, 256), 256, 0, s>>>(a.p, b.p, u.p, n, strides[axis]);
+    SHCI_LAUNCH_CHECK();
+    a.swap(b);
+  }
+  std::vector<double> g(n4);
+  SHCI_CUDA(cudaMemcpyAsync(g.data(), a.p, n4 * 8, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 4;
+  // h -> U^T h U, first index then second (:175-199), on the host (n^3)
+  std::vector<double> t((size_t)n * n, 0.0), h((size_t)n * n, 0.0);
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) {
+      double v = 0.0;
+      for (int i = 0; i < n; i++) v += rot[i * n + p] * I.h1[i * n + q];
+      t[p * n + q] = v;
+    }
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) {
+      double v = 0.0;
+      for (int i = 0; i < n; i++) v += rot[i * n + q] * t[p * n + i];
+      h[p * n + q] = v;
+    }
+  // the rewritten tables: one value per class, the first of largest magnitude (:204-240)
+  auto c2 = [](size_t x, size_t y) { return x > y ? x * (x + 1) / 2 + y : y * (y + 1) / 2 + x; };
+  const size_t nn = (size_t)n * n;
+  std::vector<double> cls(c2(nn, nn) + 1, 0.0);
+  std::vector<uint8_t> seen(cls.size(), 0);
+  auto put = [](double& a, uint8_t& f, double v) {
+    if (!f || std::fabs(a) < std::fabs(v)) a = v;
+    f = 1;
+  };
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++)
+      for (int r = 0; r < n; r++)
+        for (int s2 = 0; s2 < n; s2++) {
+          const size_t key = c2(c2(p, q), c2(r, s2));
+          put(cls[key], seen[key], g[((size_t)(p * n + q) * n + r) * n + s2]);
+        }
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++)
+      for (int r = 0; r < n; r++)
+        for (int s2 = 0; s2 < n; s2++)
+          I.g2[((size_t)(p * n + q) * n + r) * n + s2] = cls[c2(c2(p, q), c2(r, s2))];
+  std::vector<double> cls1(c2(n, n) + 1, 0.0);
+  std::vector<uint8_t> seen1(cls1.size(), 0);
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) put(cls1[c2(p, q)], seen1[c2(p, q)], h[p * n + q]);
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) I.h1[p * n + q] = cls1[c2(p, q)];
+  screen_linear(I);
 }
 
 }  // namespace shci

@@ -96,3 +96,67 @@ def test_generalized_fock_two_states(oracle_mod):
     es = c.state_energies()
     assert abs(2 * e_core + 0.5 * (np.sum(g1 * h1) + np.trace(F)) - es.sum()) < 1e-9
     c.close()
+
+
+def test_natural_orbitals(c_atom_var):
+    """Natural orbitals (optimization.cc:6-79): per irrep, the eigenvectors of the 1-RDM by
+    decreasing occupation; the rotation is orthogonal, never mixes irreps, and turns the
+    1-RDM diagonal with the occupations on the diagonal."""
+    c = c_atom_var["c"]
+    g1 = c.rdm1()
+    rot, occ = c.natural_orbitals()
+    n = rot.shape[0]
+    _, _, sym, _, _ = c.integrals()
+    assert np.max(np.abs(rot.T @ rot - np.eye(n))) < 1e-12
+    assert np.all(rot[sym[:, None] != sym[None, :]] == 0.0)
+    assert np.max(np.abs(rot.T @ g1 @ rot - np.diag(occ))) < 1e-10
+    assert abs(occ.sum() - 6.0) < 1e-10
+    for k in set(sym.tolist()):
+        idx = np.where(sym == k)[0]
+        want = np.sort(np.linalg.eigvalsh(g1[np.ix_(idx, idx)]))[::-1]
+        assert np.max(np.abs(occ[idx] - want)) < 1e-10
+
+
+def test_rotated_integrals_keep_the_spectrum(data_dir):
+    """An orbital rotation is a unitary change of basis of the full CI space: the lowest
+    eigenvalues of the complete-space Hamiltonian built from the rotated integrals are the
+    same; rotating back restores the integrals; the rotated tables keep the 8-fold symmetry
+    exactly (one value per class, as the reference's rewritten tables)."""
+    import itertools
+    import os
+    import shci_gb300 as S
+    from shci_gb300 import synthetic
+    path = os.path.join(data_dir, "FCIDUMP_rot8")
+    synthetic.make(path, 8, 4, synthetic.BASE_SEED + 8000)
+    strs = [sum(1 << o for o in cmb) for cmb in itertools.combinations(range(8), 2)]
+    up = np.array([u for u in strs for d in strs], np.uint64)
+    dn = np.array([d for u in strs for d in strs], np.uint64)
+
+    def spectrum(c):
+        c.set_dets(up, dn, None)
+        nnz, _ = c.update_hamiltonian(S.PREC_FP64)
+        rp, cl, vl, diag = c.hamiltonian(nnz)
+        m = len(diag)
+        H = np.diag(diag)
+        for i in range(m):
+            H[i, cl[rp[i]:rp[i + 1]]] = vl[rp[i]:rp[i + 1]]
+        H = np.triu(H) + np.triu(H, 1).T
+        return np.linalg.eigvalsh(H)[:6]
+
+    c = S.Context()
+    c.load_fcidump(path, 2, 2)
+    h0, g0, _, _, _ = c.integrals()
+    e0 = spectrum(c)
+    U, _ = np.linalg.qr(np.random.default_rng(3).standard_normal((8, 8)))
+    c.rotate_integrals(U)
+    h1, g1, _, _, _ = c.integrals()
+    assert np.max(np.abs(h1 - U.T @ h0 @ U)) < 1e-12
+    for perm in ((1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1)):
+        assert np.array_equal(g1, g1.transpose(perm))
+    assert np.max(np.abs(spectrum(c) - e0)) < 1e-10
+    c.rotate_integrals(U.T)
+    h2, g2, _, _, _ = c.integrals()
+    assert np.max(np.abs(h2 - h0)) < 1e-12 and np.max(np.abs(g2 - g0)) < 1e-12
+    with pytest.raises(S.ShciError):
+        c.rotate_integrals(2 * np.eye(8))
+    c.close()
