@@ -444,6 +444,20 @@ shci_status shci_natural_orbitals(shci_ctx* ctx, double* rot, double* occ);
  * the heat-bath queues are rebuilt on the next use, as after a new FCIDUMP. */
 shci_status shci_rotate_integrals(shci_ctx* ctx, const double* rot);
 
+/* Diagonal of the orbital Hessian for the pairs (p[k], q[k]) (Optimization::hessian_diagonal,
+ * optimization.cc:605-618, with hessian_part and Y_matrix, :652-676, Helgaker 10.8.50-53), from
+ * the device RDMs summed over the states (the direct 1-RDM; the reference's Newton step uses
+ * the one contracted from the 2-RDM, equal to rounding).  With shci_orbital_gradient it gives
+ * the approximate Newton step kappa_k = -grad_k / max(hdiag_k, 1e-5) (:315-328). */
+shci_status shci_orbital_hessian_diagonal(shci_ctx* ctx, const uint32_t* p, const uint32_t* q,
+                                          size_t n_param, double* hdiag);
+
+/* rot = exp(X) with X[p_k][q_k] = -kappa_k, X[q_k][p_k] = kappa_k
+ * (Optimization::fill_rot_matrix_with_parameters, optimization.cc:524-563); rot[i * n + j],
+ * ready for shci_rotate_integrals. */
+shci_status shci_orbital_rotation(shci_ctx* ctx, const uint32_t* p, const uint32_t* q,
+                                  const double* kappa, size_t n_param, double* rot);
+
 /* <S^2> of the first state of the context's wavefunction (ChemSystem::get_s2,
  * chem_system.cc:745-798; config "s2", post_variation :627-634).  A time_sym wavefunction must
  * be unpacked first (SHCI_ERR_ARG). */

@@ -79,6 +79,8 @@ def load():
         "shci_get_s2": [vp, P(d)],
         "shci_natural_orbitals": [vp, _f64p, _f64p],
         "shci_rotate_integrals": [vp, _f64p],
+        "shci_orbital_hessian_diagonal": [vp, _u32p, _u32p, sz, _f64p],
+        "shci_orbital_rotation": [vp, _u32p, _u32p, _f64p, sz, _f64p],
         "shci_set_n_states": [vp, u],
         "shci_set_time_sym": [vp, i],
         "shci_unpack_time_sym": [vp],
@@ -514,6 +516,22 @@ class Context:
         rot, occ = np.zeros(n * n), np.zeros(n)
         self._ck(self.L.shci_natural_orbitals(self.h, rot, occ))
         return rot.reshape(n, n), occ
+
+    def orbital_hessian_diagonal(self, p, q):
+        p = np.ascontiguousarray(p, np.uint32)
+        q = np.ascontiguousarray(q, np.uint32)
+        out = np.zeros(len(p))
+        self._ck(self.L.shci_orbital_hessian_diagonal(self.h, p, q, len(p), out))
+        return out
+
+    def orbital_rotation(self, p, q, kappa):
+        n = self.n_orbs
+        rot = np.zeros(n * n)
+        self._ck(self.L.shci_orbital_rotation(self.h, np.ascontiguousarray(p, np.uint32),
+                                              np.ascontiguousarray(q, np.uint32),
+                                              np.ascontiguousarray(kappa, np.float64), len(p),
+                                              rot))
+        return rot.reshape(n, n)
 
     def rotate_integrals(self, rot):
         self._ck(self.L.shci_rotate_integrals(self.h, np.ascontiguousarray(rot, np.float64).ravel()))

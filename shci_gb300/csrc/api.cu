@@ -1160,6 +1160,33 @@ shci_status shci_orbital_gradient(shci_ctx* c, const uint32_t* p, const uint32_t
   });
 }
 
+shci_status shci_orbital_hessian_diagonal(shci_ctx* c, const uint32_t* p, const uint32_t* q,
+                                          size_t n_param, double* hdiag) {
+  if (!c || (n_param && (!p || !q || !hdiag))) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    need_dets(c);
+    const size_t n = c->I.n;
+    for (size_t k = 0; k < n_param; k++)
+      if (p[k] >= n || q[k] >= n || p[k] == q[k]) throw ArgError("bad orbital pair");
+    sync_dets(c);
+    if (!c->H.valid || c->H.n != c->up.size()) build_hamiltonian(c, SHCI_PREC_FP64);
+    orbital_hessian_diagonal(c, p, q, n_param, hdiag);
+  });
+}
+
+shci_status shci_orbital_rotation(shci_ctx* c, const uint32_t* p, const uint32_t* q,
+                                  const double* kappa, size_t n_param, double* rot) {
+  if (!c || !rot || (n_param && (!p || !q || !kappa))) return SHCI_ERR_ARG;
+  return guard(c, [&]() {
+    need_integrals(c);
+    const size_t n = c->I.n;
+    for (size_t k = 0; k < n_param; k++)
+      if (p[k] >= n || q[k] >= n || p[k] == q[k]) throw ArgError("bad orbital pair");
+    rotation_from_parameters(static_cast<int>(n), p, q, kappa, n_param, rot);
+  });
+}
+
 shci_status shci_pt2_psto(shci_ctx* c, double energy_var, double eps_pt_dtm, double eps_pt_psto,
                           size_t n_batches, double target_error, double eps_pt,
                           double* correction, double* uncert, size_t* n_pt_dets,

@@ -139,6 +139,11 @@ void generalized_fock(shci_ctx* c, double* F);
 // context's integrals by an orthogonal rot (n x n, rot[i * n + p] = U_ip)
 void natural_orbitals(shci_ctx* c, const double* g1, double* rot, double* occ);
 void rotate_integrals(shci_ctx* c, const double* rot);
+// orbopt.cu: the diagonal of the orbital Hessian for the pairs (p, q), and rot = exp(X(kappa))
+void orbital_hessian_diagonal(shci_ctx* c, const unsigned* p, const unsigned* q, size_t n_param,
+                              double* hdiag);
+void rotation_from_parameters(int n, const unsigned* p, const unsigned* q, const double* kappa,
+                              size_t n_param, double* rot);
 
 // spin.cu: <S^2> of the first state over the current det list (ChemSystem::get_s2).
 double get_s2(shci_ctx* c);

@@ -67,22 +67,16 @@ __global__ void k_add(double* __restrict__ a, const double* __restrict__ b, size
 
 }  // namespace
 
-void generalized_fock(shci_ctx* c, double* F_host) {
+// 1-RDM and half-stored 2-RDM of the context's wavefunction, summed over the states
+// (rdm.cc:222-231).
+void state_rdms(shci_ctx* c, DevBuf<double>& g1, DevBuf<double>& half) {
   const int n = c->I.n;
   const size_t nn = (size_t)n * n, hs = nn * (nn + 1) / 2;
   cudaStream_t s = c->stream;
-  DevBuf<double> g1, half, t1, th, F;
-  DevBuf<unsigned> sym;
-  g1.mt = half.mt = t1.mt = th.mt = F.mt = &c->mem;
-  sym.mt = &c->mem;
-  g1.resize(nn);
-  half.resize(hs);
-  F.resize(nn);
-  sym.resize(n);
-  SHCI_CUDA(cudaMemcpyAsync(sym.p, c->I.orb_sym.data(), n * sizeof(unsigned),
-                            cudaMemcpyHostToDevice, s));
+  DevBuf<double> t1, th;
+  t1.mt = th.mt = &c->mem;
   sync_dets(c);
-  for (unsigned k = 0; k < c->n_states; k++) {  // sum over the states
+  for (unsigned k = 0; k < c->n_states; k++) {
     if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
     try {
       if (k == 0) {
@@ -105,6 +99,19 @@ void generalized_fock(shci_ctx* c, double* F_host) {
     }
     if (k) c->d_coef.swap(c->d_xcoef[k - 1]);
   }
+}
+
+// F (device, n x n) from the RDMs; also copied to F_host.
+void generalized_fock_from(shci_ctx* c, DevBuf<double>& g1, DevBuf<double>& half,
+                           DevBuf<double>& F, double* F_host) {
+  const int n = c->I.n;
+  const size_t nn = (size_t)n * n;
+  cudaStream_t s = c->stream;
+  DevBuf<unsigned> sym;
+  sym.mt = &c->mem;
+  sym.resize(n);
+  SHCI_CUDA(cudaMemcpyAsync(sym.p, c->I.orb_sym.data(), n * sizeof(unsigned),
+                            cudaMemcpyHostToDevice, s));
   {
     ProfScope ps(c->prof, s, "gen_fock");
     k_gen_fock<<<static_cast<unsigned>(nn), kFockThreads, 0, s>>>(g1.p, half.p, c->h1.p, c->g2.p,
@@ -117,6 +124,17 @@ void generalized_fock(shci_ctx* c, double* F_host) {
   c->launches += 1;
 }
 
+void generalized_fock(shci_ctx* c, double* F_host) {
+  const int n = c->I.n;
+  const size_t nn = (size_t)n * n, hs = nn * (nn + 1) / 2;
+  DevBuf<double> g1, half, F;
+  g1.mt = half.mt = F.mt = &c->mem;
+  g1.resize(nn);
+  half.resize(hs);
+  F.resize(nn);
+  state_rdms(c, g1, half);
+  generalized_fock_from(c, g1, half, F, F_host);
+}
 
 // ---------------------------------------------------------------- natural orbitals, rotation
 // Optimization::get_natorb_rotation_matrix (optimization.cc:6-79): the 1-RDM diagonalised
@@ -232,6 +250,137 @@ void rotate_integrals(shci_ctx* c, const double* rot) {
   for (int p = 0; p < n; p++)
     for (int q = 0; q < n; q++) I.h1[p * n + q] = cls1[c2(p, q)];
   screen_linear(I);
+}
+
+
+// ---------------------------------------------------------------- Newton-type step inputs
+// Optimization::hessian_diagonal / hessian_part / Y_matrix (optimization.cc:605-618, 652-676,
+// Helgaker 10.8.50-53) for the parameter pairs (p, q), and fill_rot_matrix_with_parameters
+// (:524-563): rot = exp(X), X_pq = -kappa, X_qp = kappa, formed from the eigenvectors W and
+// eigenvalues -tau^2 of X^2 as W cos(tau) W^T + W sinc(tau) W^T X.
+namespace {
+
+__device__ __forceinline__ double gam(const double* half, int n, int P, int Q, int R, int S) {
+  const size_t a = (size_t)P * n + S, b = (size_t)Q * n + R;
+  const size_t hi = a > b ? a : b, lo = a > b ? b : a;
+  return half[hi * (hi + 1) / 2 + lo];
+}
+
+// Y(a, b, c, d) = sum_mn (G(a,c,n,m) + G(a,n,c,m)) (bm|nd) + G(a,m,n,c) (bd|mn)
+__device__ __forceinline__ double y_term(const double* half, const double* g2, int n, int a,
+                                         int b, int c, int d, int m, int k) {
+  const size_t n2 = (size_t)n * n;
+  return (gam(half, n, a, c, k, m) + gam(half, n, a, k, c, m)) *
+             g2[((size_t)b * n + m) * n2 + (size_t)k * n + d] +
+         gam(half, n, a, m, k, c) * g2[((size_t)b * n + d) * n2 + (size_t)m * n + k];
+}
+
+__global__ void __launch_bounds__(kFockThreads)
+    k_hess_diag(const double* __restrict__ g1, const double* __restrict__ half,
+                const double* __restrict__ F, const double* __restrict__ h1,
+                const double* __restrict__ g2, int n, const unsigned* __restrict__ pp,
+                const unsigned* __restrict__ qq, double* __restrict__ out) {
+  const int p = static_cast<int>(pp[blockIdx.x]), q = static_cast<int>(qq[blockIdx.x]);
+  double y1 = 0.0, y2 = 0.0, y3 = 0.0;
+  for (int t = threadIdx.x; t < n * n; t += kFockThreads) {
+    const int m = t / n, k = t % n;
+    y1 += y_term(half, g2, n, p, q, p, q, m, k);
+    y2 += y_term(half, g2, n, p, q, q, p, m, k);
+    y3 += y_term(half, g2, n, q, p, q, p, m, k);
+  }
+  __shared__ double red[3][kFockThreads / 32];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    y1 += __shfl_xor_sync(kFull, y1, o);
+    y2 += __shfl_xor_sync(kFull, y2, o);
+    y3 += __shfl_xor_sync(kFull, y3, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = y1;
+    red[1][threadIdx.x >> 5] = y2;
+    red[2][threadIdx.x >> 5] = y3;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double Y1 = 0.0, Y2 = 0.0, Y3 = 0.0;
+    for (int w = 0; w < kFockThreads / 32; w++) {
+      Y1 += red[0][w];
+      Y2 += red[1][w];
+      Y3 += red[2][w];
+    }
+    // hessian_part(p,q,p,q) - 2 hessian_part(p,q,q,p) + hessian_part(q,p,q,p)
+    const double a = 2 * g1[p * n + p] * h1[q * n + q] - 2 * F[p * n + p] + 2 * Y1;
+    const double b = 2 * g1[p * n + q] * h1[q * n + p] + 2 * Y2;
+    const double c = 2 * g1[q * n + q] * h1[p * n + p] - 2 * F[q * n + q] + 2 * Y3;
+    out[blockIdx.x] = a - 2 * b + c;
+  }
+}
+
+}  // namespace
+
+void orbital_hessian_diagonal(shci_ctx* c, const unsigned* p, const unsigned* q, size_t n_param,
+                              double* hdiag) {
+  const int n = c->I.n;
+  const size_t nn = (size_t)n * n, hs = nn * (nn + 1) / 2;
+  cudaStream_t s = c->stream;
+  DevBuf<double> g1, half, F, out;
+  DevBuf<unsigned> dp, dq;
+  g1.mt = half.mt = F.mt = out.mt = &c->mem;
+  dp.mt = dq.mt = &c->mem;
+  g1.resize(nn);
+  half.resize(hs);
+  F.resize(nn);
+  state_rdms(c, g1, half);
+  std::vector<double> Fh(nn);
+  generalized_fock_from(c, g1, half, F, Fh.data());
+  if (!n_param) return;
+  dp.resize(n_param);
+  dq.resize(n_param);
+  out.resize(n_param);
+  SHCI_CUDA(cudaMemcpyAsync(dp.p, p, n_param * 4, cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemcpyAsync(dq.p, q, n_param * 4, cudaMemcpyHostToDevice, s));
+  k_hess_diag<<<static_cast<unsigned>(n_param), kFockThreads, 0, s>>>(g1.p, half.p, F.p, c->h1.p,
+                                                                      c->g2.p, n, dp.p, dq.p,
+                                                                      out.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaMemcpyAsync(hdiag, out.p, n_param * 8, cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  c->launches += 1;
+}
+
+void rotation_from_parameters(int n, const unsigned* p, const unsigned* q, const double* kappa,
+                              size_t n_param, double* rot) {
+  std::vector<double> X((size_t)n * n, 0.0), X2((size_t)n * n, 0.0);
+  for (size_t k = 0; k < n_param; k++) {
+    X[p[k] * n + q[k]] = -kappa[k];
+    X[q[k] * n + p[k]] = kappa[k];
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double v = 0.0;
+      for (int l = 0; l < n; l++) v += X[i * n + l] * X[l * n + j];
+      X2[i * n + j] = v;
+    }
+  std::vector<double> tau2(n), W((size_t)n * n), WX((size_t)n * n, 0.0);
+  jacobi_eig(n, X2.data(), n, tau2.data(), W.data());  // W[i * n + k]: component i of vector k
+  for (int k = 0; k < n; k++)
+    for (int j = 0; j < n; j++) {
+      double v = 0.0;
+      for (int l = 0; l < n; l++) v += W[l * n + k] * X[l * n + j];
+      WX[k * n + j] = v;
+    }
+  for (int i = 0; i < n * n; i++) rot[i] = 0.0;
+  for (int k = 0; k < n; k++) {
+    double cs = 1.0, sc = 1.0;
+    if (std::fabs(tau2[k]) >= 1e-10) {
+      const double tau = std::sqrt(-tau2[k]);
+      cs = std::cos(tau);
+      sc = std::sin(tau) / tau;
+    }
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++)
+        rot[i * n + j] += cs * W[i * n + k] * W[j * n + k] + sc * W[i * n + k] * WX[k * n + j];
+  }
 }
 
 }  // namespace shci

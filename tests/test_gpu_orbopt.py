@@ -160,3 +160,68 @@ def test_rotated_integrals_keep_the_spectrum(data_dir):
     with pytest.raises(S.ShciError):
         c.rotate_integrals(2 * np.eye(8))
     c.close()
+
+
+def _gamma_dense(half, n):
+    """Gamma(P, Q, R, S) = <a+_P a+_Q a_R a_S> from the half storage (pairs P n + S, Q n + R)."""
+    P, Q, R, Sx = np.meshgrid(*(np.arange(n),) * 4, indexing="ij")
+    a, b = P * n + Sx, Q * n + R
+    hi, lo = np.maximum(a, b), np.minimum(a, b)
+    return half[hi * (hi + 1) // 2 + lo]
+
+
+def test_orbital_hessian_diagonal_and_newton_step(c_atom_var):
+    """Hessian diagonal (optimization.cc:605-618, 652-676) against a numpy restatement of the
+    reference's formulas on the oracle's RDMs and against second differences of the energy
+    with the RDMs fixed; the approximate Newton step's rotation exp(X) (:524-563) equals
+    scipy's matrix exponential and lowers the fixed-RDM energy."""
+    from scipy.linalg import expm
+    c, o = c_atom_var["c"], c_atom_var["o"]
+    h1, g2, _, _, e_core = c.integrals()
+    n = h1.shape[0]
+    g1, half = o.rdm1(), o.rdm2_half()
+    F = o.generalized_fock(g1, half)
+    G = _gamma_dense(half, n)
+    p, q = c.orbital_parameters()
+    hd = c.orbital_hessian_diagonal(p, q)
+
+    def Y(a, b, cc, d):
+        return (np.sum((G[a, cc, :, :] + G[a, :, cc, :]).T * g2[b, :, :, d])
+                + np.sum(G[a, :, :, cc] * g2[b, d, :, :]))
+
+    def hp(a, b, cc, d):
+        v = 2 * g1[a, cc] * h1[b, d] + 2 * Y(a, b, cc, d)
+        return v - (F[a, cc] + F[cc, a]) if b == d else v
+
+    want = np.array([hp(a, b, a, b) - 2 * hp(a, b, b, a) + hp(b, a, b, a) for a, b in zip(p, q)])
+    assert np.max(np.abs(hd - want)) < 1e-9 * max(1.0, np.max(np.abs(want)))
+    # second differences of E(kappa) with the RDMs fixed
+    step = 1e-3
+
+    def energy(K):
+        U = expm(K)
+        h1r = U.T @ h1 @ U
+        g2r = np.einsum("pi,qj,rk,sl,pqrs->ijkl", U, U, U, U, g2, optimize=True)
+        return _energy_from_rdms(g1, half, h1r, g2r, e_core)
+
+    e0 = energy(np.zeros((n, n)))
+    for k in np.argsort(-np.abs(hd))[:3]:
+        es = []
+        for sgn in (1, -1):
+            K = np.zeros((n, n))
+            K[p[k], q[k]] = -sgn * step
+            K[q[k], p[k]] = sgn * step
+            es.append(energy(K))
+        fd2 = (es[0] - 2 * e0 + es[1]) / step ** 2
+        assert abs(fd2 - hd[k]) < 1e-4 * max(1.0, abs(hd[k]))
+    # the approximate Newton step and its rotation
+    g = c.orbital_gradient(p, q)
+    kappa = -g / np.maximum(hd, 1e-5) * 0.1
+    rot = c.orbital_rotation(p, q, kappa)
+    X = np.zeros((n, n))
+    X[p, q] = -kappa
+    X[q, p] = kappa
+    # (the reference's formula takes cos = sinc = 1 for tau^2 < 1e-10: errors ~ tau^2 / 2)
+    assert np.max(np.abs(rot - expm(X))) < 1e-9
+    assert np.max(np.abs(rot.T @ rot - np.eye(n))) < 1e-9
+    assert energy(X) < e0
